@@ -1,0 +1,251 @@
+"""ORACLE -- test infrastructure only.
+
+ctypes bindings for oracle/_build/liboracle.so (the C++ restatement of the
+reference path in weavess_oracle.cpp) and readers for the reference driver's
+dump files.  Imported only by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
+
+_lib = None
+
+u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(
+            os.path.join(HERE, "weavess_oracle.cpp")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "port"])
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        L.orc_rand_create.restype = C.c_void_p
+        L.orc_rand_create.argtypes = [C.c_uint]
+        L.orc_rand_destroy.argtypes = [C.c_void_p]
+        L.orc_rand_next.argtypes = [C.c_void_p]
+        L.orc_rand_fill.argtypes = [C.c_void_p, i32p, C.c_uint]
+        L.orc_l2_rows.argtypes = [f32p, f32p, C.c_uint, C.c_uint, f32p]
+        L.orc_init_random.argtypes = [f32p, C.c_uint, C.c_uint, C.c_uint, C.c_void_p, u32p, f32p, u32p]
+        L.orc_nndescent.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint, C.c_uint,
+                                    C.c_uint, C.c_uint, C.c_uint, C.c_void_p, C.c_int, u32p, f32p, u32p, u64p]
+        L.orc_nndescent_pools.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint,
+                                          C.c_uint, C.c_uint, C.c_uint, C.c_void_p, u32p, f32p, u8p, u32p, u32p]
+        L.orc_vamana.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint, C.c_uint,
+                                 C.c_float, C.c_uint, C.c_void_p, C.c_int, u32p, f32p, u32p, u32p]
+        L.orc_nsg.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint, C.c_uint, C.c_uint,
+                              C.c_void_p, C.c_int, u32p, f32p, u32p, C.c_uint, u32p, u32p]
+        L.orc_search.argtypes = [f32p, C.c_uint, C.c_uint, f32p, C.c_uint, u32p, u32p, C.c_uint, C.c_uint,
+                                 C.c_int, C.c_uint, C.c_uint, C.c_void_p, C.c_int, u32p, u64p]
+        L.orc_search_seeds.argtypes = [C.c_uint, C.c_uint, u32p, u32p, C.c_uint, C.c_uint, C.c_int, C.c_uint,
+                                       C.c_void_p, u32p]
+        _lib = L
+    return _lib
+
+
+class Rand:
+    """glibc-compatible rand() stream (default seed 1, as a fresh process)."""
+
+    def __init__(self, seed: int = 1):
+        self.h = lib().orc_rand_create(seed)
+
+    def next(self) -> int:
+        return lib().orc_rand_next(self.h)
+
+    def take(self, n: int) -> np.ndarray:
+        out = np.empty(n, dtype=np.int32)
+        lib().orc_rand_fill(self.h, out, n)
+        return out
+
+    def __del__(self):
+        try:
+            lib().orc_rand_destroy(self.h)
+        except Exception:
+            pass
+
+
+class Graph:
+    """Fixed-width adjacency: ids[n, w], dist[n, w], deg[n] (+ entry point)."""
+
+    def __init__(self, ids, dist, deg, ep=None):
+        self.ids, self.dist, self.deg, self.ep = ids, dist, deg, ep
+
+    @property
+    def n(self):
+        return self.ids.shape[0]
+
+    @property
+    def width(self):
+        return self.ids.shape[1]
+
+    def rows(self):
+        return [list(zip(self.ids[i, : self.deg[i]].tolist(), self.dist[i, : self.deg[i]].tolist()))
+                for i in range(self.n)]
+
+
+def _c(x, dt):
+    return np.ascontiguousarray(x, dtype=dt)
+
+
+def l2_rows(a, b):
+    a, b = _c(a, np.float32), _c(b, np.float32)
+    out = np.empty(a.shape[0], dtype=np.float32)
+    lib().orc_l2_rows(a, b, a.shape[0], a.shape[1], out)
+    return out
+
+
+def init_random(base, S, rnd: Rand) -> Graph:
+    base = _c(base, np.float32)
+    n, d = base.shape
+    ids = np.zeros((n, S), np.uint32)
+    dist = np.zeros((n, S), np.float32)
+    deg = np.zeros(n, np.uint32)
+    assert lib().orc_init_random(base, n, d, S, rnd.h, ids, dist, deg) == 0
+    return Graph(ids, dist, deg)
+
+
+def nndescent(base, init: Graph, S, K, L, ITER, R, rnd: Rand, threads=1):
+    base = _c(base, np.float32)
+    n, d = base.shape
+    ids = np.zeros((n, K), np.uint32)
+    dist = np.zeros((n, K), np.float32)
+    deg = np.zeros(n, np.uint32)
+    stats = np.zeros(2, np.uint64)
+    assert lib().orc_nndescent(base, n, d, _c(init.ids, np.uint32), _c(init.dist, np.float32),
+                               _c(init.deg, np.uint32), init.width, S, K, L, ITER, R, rnd.h, threads,
+                               ids, dist, deg, stats) == 0
+    g = Graph(ids, dist, deg)
+    g.overflow_events = int(stats[0])
+    return g
+
+
+def nndescent_pools(base, init: Graph, S, L, iters, R, rnd: Rand):
+    base = _c(base, np.float32)
+    n, d = base.shape
+    ids = np.zeros((n, L), np.uint32)
+    dist = np.zeros((n, L), np.float32)
+    flag = np.zeros((n, L), np.uint8)
+    deg = np.zeros(n, np.uint32)
+    M = np.zeros(n, np.uint32)
+    lib().orc_nndescent_pools(base, n, d, _c(init.ids, np.uint32), _c(init.dist, np.float32),
+                              _c(init.deg, np.uint32), init.width, S, L, iters, R, rnd.h, ids, dist, flag, deg, M)
+    return ids, dist, flag, deg, M
+
+
+def vamana(base, g: Graph, L_refine, R_refine, alpha, rnd: Rand, entry_L=0, threads=1) -> Graph:
+    base = _c(base, np.float32)
+    n, d = base.shape
+    ids = np.zeros((n, R_refine), np.uint32)
+    dist = np.zeros((n, R_refine), np.float32)
+    deg = np.zeros(n, np.uint32)
+    ep = np.zeros(1, np.uint32)
+    assert lib().orc_vamana(base, n, d, _c(g.ids, np.uint32), _c(g.dist, np.float32), _c(g.deg, np.uint32),
+                            g.width, L_refine, R_refine, alpha, entry_L, rnd.h, threads, ids, dist, deg, ep) == 0
+    return Graph(ids, dist, deg, int(ep[0]))
+
+
+def nsg(base, g: Graph, L_refine, R_refine, C_refine, rnd: Rand, threads=1, out_w=None) -> Graph:
+    base = _c(base, np.float32)
+    n, d = base.shape
+    out_w = out_w or R_refine + 32
+    ids = np.zeros((n, out_w), np.uint32)
+    dist = np.zeros((n, out_w), np.float32)
+    deg = np.zeros(n, np.uint32)
+    ep = np.zeros(1, np.uint32)
+    added = np.zeros(1, np.uint32)
+    assert lib().orc_nsg(base, n, d, _c(g.ids, np.uint32), _c(g.dist, np.float32), _c(g.deg, np.uint32),
+                         g.width, L_refine, R_refine, C_refine, rnd.h, threads, ids, dist, deg, out_w, ep,
+                         added) == 0
+    out = Graph(ids, dist, deg, int(ep[0]))
+    out.conn_added = int(added[0])
+    return out
+
+
+def search(base, query, g: Graph, L, rnd: Rand, entry="rand", K=10, threads=1):
+    base, query = _c(base, np.float32), _c(query, np.float32)
+    n, d = base.shape
+    nq = query.shape[0]
+    res = np.zeros((nq, K), np.uint32)
+    cnt = np.zeros(2, np.uint64)
+    rc = lib().orc_search(base, n, d, query, nq, _c(g.ids, np.uint32), _c(g.deg, np.uint32), g.width,
+                          int(g.ep or 0), 0 if entry == "rand" else 1, L, K, rnd.h, threads, res, cnt)
+    assert rc == 0
+    return res, int(cnt[0]), int(cnt[1])
+
+
+def search_seeds(n, nq, g: Graph, L, rnd: Rand, entry="rand"):
+    seeds = np.zeros((nq, L), np.uint32)
+    lib().orc_search_seeds(n, nq, _c(g.ids, np.uint32), _c(g.deg, np.uint32), g.width, int(g.ep or 0),
+                           0 if entry == "rand" else 1, L, rnd.h, seeds)
+    return seeds
+
+
+# ---------------------------------------------------------------- ref dumps
+def read_graph_dump(path: str) -> Graph:
+    """Read a ref_driver graph dump: u32 n, u32 ep, then per node u32 deg and
+    deg x (u32 id, f32 dist)."""
+    raw = np.fromfile(path, dtype=np.uint32)
+    n, ep = int(raw[0]), int(raw[1])
+    pos = 2
+    rows = []
+    for _ in range(n):
+        deg = int(raw[pos])
+        pos += 1
+        rows.append(raw[pos: pos + 2 * deg].reshape(deg, 2))
+        pos += 2 * deg
+    w = max(1, max(r.shape[0] for r in rows))
+    ids = np.zeros((n, w), np.uint32)
+    dist = np.zeros((n, w), np.float32)
+    deg = np.zeros(n, np.uint32)
+    for i, r in enumerate(rows):
+        deg[i] = r.shape[0]
+        ids[i, : r.shape[0]] = r[:, 0]
+        dist[i, : r.shape[0]] = r[:, 1].view(np.float32)
+    return Graph(ids, dist, deg, None if ep == 0xFFFFFFFF else ep)
+
+
+def read_search_dump(path: str):
+    raw = np.fromfile(path, dtype=np.uint32)
+    nq, k = int(raw[0]), int(raw[1])
+    res = raw[2: 2 + nq * k].reshape(nq, k)
+    dc, hc = int(raw[2 + nq * k]), int(raw[3 + nq * k])
+    return res, dc, hc
+
+
+def graphs_equal(a: Graph, b: Graph, check_dist=True) -> bool:
+    if a.n != b.n or not np.array_equal(a.deg, b.deg):
+        return False
+    for i in range(a.n):
+        k = int(a.deg[i])
+        if not np.array_equal(a.ids[i, :k], b.ids[i, :k]):
+            return False
+        if check_dist and not np.array_equal(a.dist[i, :k].view(np.uint32), b.dist[i, :k].view(np.uint32)):
+            return False
+    return True
+
+
+def row_mismatches(a: Graph, b: Graph) -> int:
+    bad = 0
+    for i in range(a.n):
+        k = int(a.deg[i])
+        if a.deg[i] != b.deg[i] or not np.array_equal(a.ids[i, :k], b.ids[i, :k]):
+            bad += 1
+    return bad

@@ -1,0 +1,150 @@
+// Reference driver: runs the UNMODIFIED WEAVESS component sources (compiled from
+// where they lie by oracle/Makefile) on seeded inputs and dumps every
+// intermediate result the GPU path is checked against.  Test infrastructure
+// only -- never linked into the product.
+//
+// It follows the reference pipelines:
+//   KGraph build   test/main.cpp:15-21   (init INIT_RANDOM, refine REFINE_NN_DESCENT)
+//   Vamana link    src/component_refine.cpp:794-872 (alpha set on the index, as
+//                  the reference has no parameter for it, index.h:213-216)
+//   NSG link       src/component_refine.cpp:393-472
+//   search loop    src/builder.cpp:445-454 (L_SEARCH_ASSIGN, serial), with the
+//                  result ids kept instead of only the recall print.
+// One thread (IndexBuilder(1)), so the glibc rand() stream and every sort are
+// deterministic.
+//
+// usage: ref_driver base.fvecs query.fvecs gt.ivecs outprefix key=val ... -- step ...
+//   steps: init_random | init_rand | nndescent | vamana | nsg | load:<kgraph|vamana|nsg>
+//          | search_rand:<L> | search_centroid:<L> | rand_probe
+#include <bits/stdc++.h>
+#include <omp.h>
+#include <boost/dynamic_bitset.hpp>
+#include <boost/shared_ptr.hpp>
+#include <boost/heap/d_ary_heap.hpp>
+#define private public
+#define protected public
+#include <weavess/builder.h>
+#include <weavess/component.h>
+#undef private
+#undef protected
+
+using namespace weavess;
+
+static void write_final_graph(const std::string &path, Index *idx, bool with_ep) {
+  FILE *f = fopen(path.c_str(), "wb");
+  unsigned n = idx->getBaseLen();
+  unsigned ep = with_ep ? idx->ep_ : 0xffffffffu;
+  fwrite(&n, 4, 1, f);
+  fwrite(&ep, 4, 1, f);
+  auto &g = idx->getFinalGraph();
+  for (unsigned i = 0; i < n; i++) {
+    unsigned deg = (unsigned)g[i].size();
+    fwrite(&deg, 4, 1, f);
+    for (unsigned j = 0; j < deg; j++) {
+      fwrite(&g[i][j].id, 4, 1, f);
+      fwrite(&g[i][j].distance, 4, 1, f);
+    }
+  }
+  fclose(f);
+}
+
+int main(int argc, char **argv) {
+  if (argc < 6) {
+    fprintf(stderr, "usage: %s base query gt outprefix k=v ... -- steps\n", argv[0]);
+    return 2;
+  }
+  std::string prefix = argv[4];
+  Parameters params;
+  float alpha = 1.0f;
+  int a = 5;
+  for (; a < argc && std::string(argv[a]) != "--"; a++) {
+    std::string kv = argv[a];
+    auto p = kv.find('=');
+    std::string k = kv.substr(0, p), v = kv.substr(p + 1);
+    if (k == "alpha") alpha = std::stof(v);
+    else params.set<std::string>(k, v);
+  }
+  a++;
+  auto *builder = new IndexBuilder(1);
+  builder->load(argv[1], argv[2], argv[3], params);
+  Index *idx = builder->final_index_;
+  // Members the reference reads without ever setting on these paths
+  // (e.g. L_refine for the Vamana entry, component_entry.cpp:32) start at 0,
+  // as they do in a fresh process where `new Index()` gets zeroed pages.
+  idx->L_refine = 0;
+  idx->R_refine = 0;
+  idx->C_refine = 0;
+  idx->alpha = alpha;
+  for (; a < argc; a++) {
+    std::string step = argv[a];
+    std::string arg;
+    auto c = step.find(':');
+    if (c != std::string::npos) {
+      arg = step.substr(c + 1);
+      step = step.substr(0, c);
+    }
+    auto t0 = std::chrono::high_resolution_clock::now();
+    if (step == "init_random") {
+      builder->init(INIT_RANDOM, false);
+      write_final_graph(prefix + ".init.bin", idx, false);
+    } else if (step == "init_rand") {
+      builder->init(INIT_RAND, false);
+      write_final_graph(prefix + ".initrand.bin", idx, false);
+    } else if (step == "nndescent") {
+      builder->refine(REFINE_NN_DESCENT, false);
+      write_final_graph(prefix + ".nnd.bin", idx, false);
+    } else if (step == "vamana") {
+      // alpha is set once, at load; the reference itself sets it to 2 at the
+      // end of every Vamana link (component_refine.cpp:871)
+      builder->refine(REFINE_VAMANA, false);
+      write_final_graph(prefix + ".vamana.bin", idx, true);
+    } else if (step == "nsg") {
+      builder->refine(REFINE_NSG, false);
+      write_final_graph(prefix + ".nsg.bin", idx, true);
+    } else if (step == "load") {
+      TYPE t = arg == "kgraph" ? INDEX_KGRAPH : (arg == "vamana" ? INDEX_VAMANA : INDEX_NSG);
+      std::string gf = prefix + "." + arg + ".graph";
+      builder->save_graph(t, &gf[0]);
+      idx->getLoadGraph().clear();
+      builder->load_graph(t, &gf[0]);
+    } else if (step == "search_rand" || step == "search_centroid") {
+      unsigned L = (unsigned)std::stoul(arg);
+      idx->getParam().set<unsigned>("K_search", 10);
+      idx->getParam().set<unsigned>("L_search", L);
+      ComponentSearchEntry *e = step == "search_rand" ? (ComponentSearchEntry *)new ComponentSearchEntryRand(idx)
+                                                      : (ComponentSearchEntry *)new ComponentSearchEntryCentroid(idx);
+      auto *r = new ComponentSearchRouteGreedy(idx);
+      idx->resetDistCount();
+      idx->resetHopCount();
+      unsigned nq = idx->getQueryLen();
+      std::vector<std::vector<unsigned>> res(nq);
+      for (unsigned i = 0; i < nq; i++) {
+        std::vector<Index::Neighbor> pool;
+        e->SearchEntryInner(i, pool);
+        r->RouteInner(i, pool, res[i]);
+      }
+      std::string out = prefix + "." + step + "_" + arg + ".bin";
+      FILE *f = fopen(out.c_str(), "wb");
+      fwrite(&nq, 4, 1, f);
+      unsigned k = 10;
+      fwrite(&k, 4, 1, f);
+      for (unsigned i = 0; i < nq; i++) fwrite(res[i].data(), 4, 10, f);
+      unsigned dc = idx->getDistCount(), hc = idx->getHopCount();
+      fwrite(&dc, 4, 1, f);
+      fwrite(&hc, 4, 1, f);
+      fclose(f);
+      // components own (and would delete) the index; leak them as the reference does
+    } else if (step == "rand_probe") {
+      // consumes one value of the process rand() stream and reports it
+      printf("rand_probe %d\n", rand());
+    } else {
+      fprintf(stderr, "unknown step %s\n", step.c_str());
+      return 2;
+    }
+    auto t1 = std::chrono::high_resolution_clock::now();
+    printf("step %s%s%s %.6f s\n", step.c_str(), arg.empty() ? "" : ":", arg.c_str(),
+           std::chrono::duration<double>(t1 - t0).count());
+    fflush(stdout);
+  }
+  return 0;
+}

@@ -1,0 +1,923 @@
+// ORACLE -- test infrastructure only.
+//
+// A plain C++ restatement of the WEAVESS hot path, used by tests/ (and by the
+// CPU-baseline leg of bench.py) as the checker for the GPU implementation.
+// Nothing in the product links, loads or calls this file.  Its parity with the
+// reference itself is pinned by tests/test_oracle_golden.py against fixtures
+// produced by the unmodified reference sources (oracle/ref_driver.cpp,
+// tests/golden/make_golden.py).
+//
+// Every routine cites the reference function it restates.  Single-threaded
+// calls reproduce the reference's single-threaded results bit for bit,
+// including the glibc rand() stream, std::sort/std::make_heap tie behaviour
+// and the reference's known defects.  With threads > 1 the OpenMP structure of
+// the reference is kept (the results are then as nondeterministic as the
+// reference's; this mode is only used for timing).
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <random>
+#include <stack>
+#include <vector>
+#include <omp.h>
+
+namespace {
+
+// ---------------------------------------------------------------- rand()
+// glibc's default rand() (TYPE_3 additive feedback generator, degree 31,
+// separation 3): r[i] = r[i-31] + r[i-3] mod 2^32, output r[i] >> 1, with a
+// Lehmer (16807) seeding of the first 31 words and 310 discarded outputs.
+// This is the generator the reference's rand() calls draw from (srand is never
+// called on the hot path, so the seed is glibc's default 1).
+struct GlibcRand {
+  uint32_t r[34];
+  int i = 0;  // ring position
+  std::mutex mu;
+  explicit GlibcRand(uint32_t seed) { reseed(seed); }
+  void reseed(uint32_t seed) {
+    if (seed == 0) seed = 1;
+    int32_t w[34];
+    w[0] = (int32_t)seed;
+    for (int k = 1; k < 31; k++) {
+      // 16807 * w mod (2^31 - 1) via Schrage's method, as glibc does
+      int32_t hi = w[k - 1] / 127773, lo = w[k - 1] % 127773;
+      int32_t word = 16807 * lo - 2836 * hi;
+      if (word < 0) word += 2147483647;
+      w[k] = word;
+    }
+    for (int k = 31; k < 34; k++) w[k] = w[k - 31];
+    for (int k = 0; k < 34; k++) r[k] = (uint32_t)w[k];
+    i = 0;
+    // ring holds the last 34 words; position i is the oldest
+    for (int k = 0; k < 310; k++) step();
+  }
+  // advance: new word = r[n-31] + r[n-3]; return it
+  uint32_t step() {
+    // ring of 34 words where r[(i + 34 - m) % 34] is r[n - m] for the next n
+    uint32_t v = r[(i + 34 - 31) % 34] + r[(i + 34 - 3) % 34];
+    r[i] = v;
+    i = (i + 1) % 34;
+    return v;
+  }
+  int next() { return (int)(step() >> 1); }
+  int next_locked() {
+    std::lock_guard<std::mutex> g(mu);
+    return next();
+  }
+};
+
+// ---------------------------------------------------------------- distance
+// Distance::compare (include/weavess/distance.h:12-36): groups of four,
+// result += d0*d0 + d1*d1 + d2*d2 + d3*d3 in that order, then the tail.
+// Built with -ffp-contract=off so no FMA changes the rounding.
+inline float l2(const float *a, const float *b, unsigned d) {
+  float result = 0;
+  unsigned k = 0;
+  for (; k + 3 < d; k += 4) {
+    float d0 = a[k] - b[k], d1 = a[k + 1] - b[k + 1], d2 = a[k + 2] - b[k + 2], d3 = a[k + 3] - b[k + 3];
+    result += d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3;
+  }
+  for (; k < d; k++) {
+    float t = a[k] - b[k];
+    result += t * t;
+  }
+  return result;
+}
+
+struct Neighbor {  // NNDescent::Neighbor (index.h:66-82)
+  unsigned id;
+  float distance;
+  bool flag;
+  Neighbor() = default;
+  Neighbor(unsigned i, float dd, bool f) : id(i), distance(dd), flag(f) {}
+  bool operator<(const Neighbor &o) const { return distance < o.distance; }
+};
+struct SimpleNeighbor {  // Index::SimpleNeighbor (index.h:1530-1541)
+  unsigned id;
+  float distance;
+  SimpleNeighbor() = default;
+  SimpleNeighbor(unsigned i, float dd) : id(i), distance(dd) {}
+  bool operator<(const SimpleNeighbor &o) const { return distance < o.distance; }
+};
+
+// Index::MinHeap (index.h:339-382): std heap with an inverted comparator
+struct MinHeapItem {
+  float key;
+  SimpleNeighbor data;
+  bool operator<(const MinHeapItem &o) const { return key > o.key; }
+};
+struct MinHeap {
+  std::vector<MinHeapItem> v;
+  void push(float k, const SimpleNeighbor &d) {
+    v.push_back(MinHeapItem{k, d});
+    std::push_heap(v.begin(), v.end());
+  }
+  const MinHeapItem &top() const { return v[0]; }
+  void pop() {
+    std::pop_heap(v.begin(), v.end());
+    v.pop_back();
+  }
+  size_t size() const { return v.size(); }
+};
+
+// NNDescent::InsertIntoPool (index.h:152-180)
+int insert_into_pool(Neighbor *addr, unsigned K, Neighbor nn) {
+  int left = 0, right = (int)K - 1;
+  if (addr[left].distance > nn.distance) {
+    memmove((char *)&addr[left + 1], &addr[left], K * sizeof(Neighbor));
+    addr[left] = nn;
+    return left;
+  }
+  if (addr[right].distance < nn.distance) {
+    addr[K] = nn;
+    return (int)K;
+  }
+  while (left < right - 1) {
+    int mid = (left + right) / 2;
+    if (addr[mid].distance > nn.distance) right = mid;
+    else left = mid;
+  }
+  while (left > 0) {
+    if (addr[left].distance < nn.distance) break;
+    if (addr[left].id == nn.id) return (int)K + 1;
+    left--;
+  }
+  if (addr[left].id == nn.id || addr[right].id == nn.id) return (int)K + 1;
+  memmove((char *)&addr[right + 1], &addr[right], (K - right) * sizeof(Neighbor));
+  addr[right] = nn;
+  return right;
+}
+
+// GenRandom (util.h:13-27; same body as ComponentInitRandom::GenRandom,
+// component_init.cpp:51-68)
+void gen_random(std::mt19937 &rng, unsigned *addr, unsigned size, unsigned N) {
+  for (unsigned i = 0; i < size; ++i) addr[i] = rng() % (N - size);
+  std::sort(addr, addr + size);
+  for (unsigned i = 1; i < size; ++i)
+    if (addr[i] <= addr[i - 1]) addr[i] = addr[i - 1] + 1;
+  unsigned off = rng() % N;
+  for (unsigned i = 0; i < size; ++i) addr[i] = (addr[i] + off) % N;
+}
+
+struct Data {
+  const float *base;
+  unsigned n, d;
+  const float *row(size_t i) const { return base + i * (size_t)d; }
+};
+
+typedef std::vector<std::vector<SimpleNeighbor>> FinalGraph;
+
+FinalGraph graph_from_arrays(const unsigned *ids, const float *dist, const unsigned *deg, unsigned n, unsigned w) {
+  FinalGraph g(n);
+  for (unsigned i = 0; i < n; i++) {
+    g[i].reserve(deg[i]);
+    for (unsigned j = 0; j < deg[i]; j++) g[i].emplace_back(ids[(size_t)i * w + j], dist ? dist[(size_t)i * w + j] : 0.f);
+  }
+  return g;
+}
+
+int graph_to_arrays(const FinalGraph &g, unsigned *ids, float *dist, unsigned *deg, unsigned w) {
+  for (size_t i = 0; i < g.size(); i++) {
+    if (g[i].size() > w) return -1;
+    deg[i] = (unsigned)g[i].size();
+    for (size_t j = 0; j < g[i].size(); j++) {
+      ids[i * w + j] = g[i][j].id;
+      if (dist) dist[i * w + j] = g[i][j].distance;
+    }
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------- NN-Descent
+struct NHood {  // NNDescent::nhood (index.h:86-150)
+  std::mutex lock;
+  std::vector<Neighbor> pool;
+  unsigned M = 0;
+  std::vector<unsigned> nn_old, nn_new, rnn_old, rnn_new;
+};
+
+struct NNDescent {
+  const Data &D;
+  unsigned S, K, L, ITER, R;
+  GlibcRand &rnd;
+  int threads;
+  std::vector<NHood> graph;
+  uint64_t overflow_events = 0, dist_evals = 0;
+
+  NNDescent(const Data &d, unsigned s, unsigned k, unsigned l, unsigned it, unsigned r, GlibcRand &rr, int th)
+      : D(d), S(s), K(k), L(l), ITER(it), R(r), rnd(rr), threads(th), graph(d.n) {}
+
+  // nhood::insert (index.h:120-135); pool capacity is L (reserved once)
+  void insert(unsigned t, unsigned id, float dist) {
+    NHood &h = graph[t];
+    std::lock_guard<std::mutex> guard(h.lock);
+    if (dist > h.pool.front().distance) return;
+    for (unsigned i = 0; i < h.pool.size(); i++)
+      if (id == h.pool[i].id) return;
+    if (h.pool.size() < L) {
+      h.pool.push_back(Neighbor(id, dist, true));
+      std::push_heap(h.pool.begin(), h.pool.end());
+    } else {
+      std::pop_heap(h.pool.begin(), h.pool.end());
+      h.pool[h.pool.size() - 1] = Neighbor(id, dist, true);
+      std::push_heap(h.pool.begin(), h.pool.end());
+    }
+  }
+
+  // ComponentRefineNNDescent::init (component_refine.cpp:87-104); nhood(L,S)
+  // leaves nn_new as 2S zeros (index.h:98-103), so the first join does nothing
+  void init(const FinalGraph &fg) {
+    for (unsigned i = 0; i < D.n; i++) {
+      graph[i].M = S;
+      graph[i].nn_new.assign(2 * S, 0u);
+      graph[i].pool.reserve(L);
+      for (auto &nb : fg[i]) graph[i].pool.emplace_back(nb.id, nb.distance, true);
+      std::make_heap(graph[i].pool.begin(), graph[i].pool.end());
+    }
+  }
+
+  // ComponentRefineNNDescent::join (component_refine.cpp:127-143) with
+  // nhood::join (index.h:137-149)
+  void join() {
+#pragma omp parallel for schedule(dynamic, 100) num_threads(threads)
+    for (unsigned n = 0; n < D.n; n++) {
+      auto cb = [&](unsigned i, unsigned j) {
+        if (i != j) {
+          float dist = l2(D.row(i), D.row(j), D.d);
+          insert(i, j, dist);
+          insert(j, i, dist);
+        }
+      };
+      const NHood &h = graph[n];
+      for (unsigned const i : h.nn_new) {
+        for (unsigned const j : h.nn_new)
+          if (i < j) cb(i, j);
+        for (unsigned j : h.nn_old) cb(i, j);
+      }
+    }
+  }
+
+  // ComponentRefineNNDescent::update (component_refine.cpp:145-239)
+  void update() {
+#pragma omp parallel for num_threads(threads)
+    for (unsigned i = 0; i < D.n; i++) {
+      std::vector<unsigned>().swap(graph[i].nn_new);
+      std::vector<unsigned>().swap(graph[i].nn_old);
+    }
+#pragma omp parallel for num_threads(threads)
+    for (unsigned n = 0; n < D.n; ++n) {
+      auto &nn = graph[n];
+      std::sort(nn.pool.begin(), nn.pool.end());
+      if (nn.pool.size() > L) nn.pool.resize(L);
+      unsigned maxl = std::min(nn.M + S, (unsigned)nn.pool.size());
+      unsigned c = 0, l = 0;
+      while ((l < maxl) && (c < S)) {
+        if (nn.pool[l].flag) ++c;
+        ++l;
+      }
+      nn.M = l;
+    }
+#pragma omp parallel for num_threads(threads)
+    for (unsigned n = 0; n < D.n; ++n) {
+      auto &nnhd = graph[n];
+      for (unsigned l = 0; l < nnhd.M; ++l) {
+        auto &nn = nnhd.pool[l];
+        auto &nhood_o = graph[nn.id];
+        // pool.back() of the other node: the max if it is still sorted, the
+        // last slot of its heap if it was already make_heap'd this pass
+        if (nn.flag) {
+          nnhd.nn_new.push_back(nn.id);
+          if (nn.distance > nhood_o.pool.back().distance) {
+            std::lock_guard<std::mutex> guard(nhood_o.lock);
+            if (nhood_o.rnn_new.size() < R) nhood_o.rnn_new.push_back(n);
+            else {
+              unsigned pos = (unsigned)rnd.next_locked() % R;
+              nhood_o.rnn_new[pos] = n;
+              overflow_events++;
+            }
+          }
+          nn.flag = false;
+        } else {
+          nnhd.nn_old.push_back(nn.id);
+          if (nn.distance > nhood_o.pool.back().distance) {
+            std::lock_guard<std::mutex> guard(nhood_o.lock);
+            if (nhood_o.rnn_old.size() < R) nhood_o.rnn_old.push_back(n);
+            else {
+              unsigned pos = (unsigned)rnd.next_locked() % R;
+              nhood_o.rnn_old[pos] = n;
+              overflow_events++;
+            }
+          }
+        }
+      }
+      std::make_heap(nnhd.pool.begin(), nnhd.pool.end());
+    }
+#pragma omp parallel for num_threads(threads)
+    for (unsigned i = 0; i < D.n; ++i) {
+      auto &g = graph[i];
+      // the random_shuffle branches of the reference are unreachable: the
+      // reverse lists are capped at R when they are filled
+      g.nn_new.insert(g.nn_new.end(), g.rnn_new.begin(), g.rnn_new.end());
+      g.nn_old.insert(g.nn_old.end(), g.rnn_old.begin(), g.rnn_old.end());
+      if (g.nn_old.size() > R * 2) g.nn_old.resize(R * 2);
+      std::vector<unsigned>().swap(g.rnn_new);
+      std::vector<unsigned>().swap(g.rnn_old);
+    }
+  }
+
+  // RefineInner tail (component_refine.cpp:21-74): sort pools, naive prune to K
+  FinalGraph finish() {
+    FinalGraph fg(D.n);
+    for (unsigned i = 0; i < D.n; i++) {
+      std::sort(graph[i].pool.begin(), graph[i].pool.end());
+      unsigned len = std::min<unsigned>((unsigned)graph[i].pool.size(), K);  // PruneNaive
+      for (unsigned j = 0; j < len; j++) fg[i].emplace_back(graph[i].pool[j].id, graph[i].pool[j].distance);
+    }
+    return fg;
+  }
+};
+
+// ComponentInitRandom::InitInner (component_init.cpp:11-45)
+FinalGraph init_random(const Data &D, unsigned S, GlibcRand &rnd) {
+  FinalGraph g(D.n);
+  std::mt19937 rng(rnd.next());
+  std::vector<unsigned> tmp(S);
+  for (unsigned i = 0; i < D.n; i++) {
+    g[i].reserve(S);
+    gen_random(rng, tmp.data(), S, D.n);
+    for (unsigned j = 0; j < S; j++) {
+      unsigned id = tmp[j];
+      if (id == i) continue;
+      g[i].emplace_back(id, l2(D.row(i), D.row(id), D.d));
+    }
+    std::sort(g[i].begin(), g[i].end());
+  }
+  return g;
+}
+
+// ---------------------------------------------------------------- greedy searches
+// Seeds for a build-time greedy search: the first L ids of `enter`'s row, then
+// rand() % N draws that skip flagged ids (component_candidate.cpp:17-31,
+// component_entry.cpp:39-52, component_conn.cpp:93-106).
+void build_seeds(const FinalGraph &g, unsigned enter, unsigned L, unsigned N, GlibcRand &rnd,
+                 std::vector<unsigned> &init_ids, std::vector<char> &flags) {
+  init_ids.assign(L, 0);
+  unsigned l = 0;
+  for (unsigned i = 0; i < init_ids.size() && i < g[enter].size(); i++) {
+    init_ids[i] = g[enter][i].id;
+    flags[init_ids[i]] = 1;
+    l++;
+  }
+  while (l < init_ids.size()) {
+    unsigned id = (unsigned)rnd.next_locked() % N;
+    if (flags[id]) continue;
+    init_ids[l] = id;
+    l++;
+    flags[id] = 1;
+  }
+}
+
+// The greedy loop shared by CandidateNSG::CandidateInner
+// (component_candidate.cpp:46-81), EntryCentroid::get_neighbors
+// (component_entry.cpp:66-91) and ConnNSGDFS::get_neighbors
+// (component_conn.cpp:121-159).  `visit` is called with every newly flagged
+// (id, dist) in visit order.
+template <class F>
+void greedy_expand(const Data &D, const FinalGraph &g, const float *q, std::vector<Neighbor> &retset, unsigned L,
+                   std::vector<char> &flags, F visit) {
+  int k = 0;
+  while (k < (int)L) {
+    int nk = (int)L;
+    if (retset[k].flag) {
+      retset[k].flag = false;
+      unsigned n = retset[k].id;
+      for (unsigned m = 0; m < g[n].size(); ++m) {
+        unsigned id = g[n][m].id;
+        if (flags[id]) continue;
+        flags[id] = 1;
+        float dist = l2(q, D.row(id), D.d);
+        Neighbor nn(id, dist, true);
+        visit(nn);
+        if (dist >= retset[L - 1].distance) continue;
+        int r = insert_into_pool(retset.data(), L, nn);
+        if (L + 1 < retset.size()) ++L;
+        if (r < nk) nk = r;
+      }
+    }
+    if (nk <= k) k = nk;
+    else ++k;
+  }
+}
+
+// ComponentCandidateNSG::CandidateInner (component_candidate.cpp:10-85)
+void candidate_nsg(const Data &D, const FinalGraph &g, unsigned query, unsigned enter, unsigned Lr, GlibcRand &rnd,
+                   std::vector<SimpleNeighbor> &result, std::vector<char> &flags) {
+  std::vector<unsigned> init_ids;
+  build_seeds(g, enter, Lr, D.n, rnd, init_ids, flags);
+  std::vector<Neighbor> retset(Lr + 1);
+  unsigned L = 0;
+  for (unsigned i = 0; i < init_ids.size(); i++) {
+    unsigned id = init_ids[i];
+    float dist = l2(D.row(id), D.row(query), D.d);
+    retset[i] = Neighbor(id, dist, true);
+    result.emplace_back(id, dist);
+    L++;
+  }
+  std::sort(retset.begin(), retset.begin() + L);
+  greedy_expand(D, g, D.row(query), retset, L, flags,
+                [&](const Neighbor &nn) { result.push_back(SimpleNeighbor(nn.id, nn.distance)); });
+}
+
+// greedy search for an arbitrary vector (EntryCentroid / ConnNSGDFS
+// get_neighbors); returns retset, fills fullset with the expansion visits
+void get_neighbors(const Data &D, const FinalGraph &g, unsigned ep, const float *q, unsigned Lr, GlibcRand &rnd,
+                   std::vector<Neighbor> &retset, std::vector<Neighbor> *fullset) {
+  std::vector<char> flags(D.n, 0);
+  std::vector<unsigned> init_ids;
+  build_seeds(g, ep, Lr, D.n, rnd, init_ids, flags);
+  retset.assign(Lr + 1, Neighbor(0, 0.f, false));
+  unsigned L = 0;
+  for (unsigned i = 0; i < init_ids.size(); i++) {
+    unsigned id = init_ids[i];
+    retset[i] = Neighbor(id, l2(D.row(id), q, D.d), true);
+    L++;
+  }
+  std::sort(retset.begin(), retset.begin() + L);
+  greedy_expand(D, g, q, retset, L, flags, [&](const Neighbor &nn) {
+    if (fullset) fullset->push_back(nn);
+  });
+}
+
+// ComponentRefineEntryCentroid::EntryInner (component_entry.cpp:9-28).
+// `entry_L` is the index's L_refine member: the NSG refine sets it, the
+// Vamana refine never does, so there it is 0 and ep_ ends as node 0.
+unsigned entry_centroid(const Data &D, const FinalGraph &g, unsigned entry_L, GlibcRand &rnd) {
+  std::vector<float> center(D.d, 0.f);
+  for (unsigned i = 0; i < D.n; i++)
+    for (unsigned j = 0; j < D.d; j++) center[j] += D.row(i)[j];
+  for (unsigned j = 0; j < D.d; j++) center[j] /= D.n;
+  unsigned ep = (unsigned)rnd.next() % D.n;
+  std::vector<Neighbor> tmp;
+  if (entry_L == 0) return 0;  // retset of one value-initialised Neighbor
+  get_neighbors(D, g, ep, center.data(), entry_L, rnd, tmp, nullptr);
+  return tmp[0].id;
+}
+
+// ComponentPruneNSG::PruneInner (component_prune.cpp:20-69)
+void prune_nsg(const Data &D, const FinalGraph &g, unsigned query, unsigned range, unsigned maxc,
+               std::vector<SimpleNeighbor> &pool, SimpleNeighbor *cut_graph) {
+  unsigned start = 0;
+  for (unsigned nn = 0; nn < g[query].size(); nn++) {
+    unsigned id = g[query][nn].id;
+    pool.push_back(SimpleNeighbor(id, l2(D.row(query), D.row(id), D.d)));
+  }
+  std::sort(pool.begin(), pool.end());
+  std::vector<SimpleNeighbor> result;
+  if (pool[start].id == query) start++;
+  result.push_back(pool[start]);
+  while (result.size() < range && (++start) < pool.size() && start < maxc) {
+    auto &p = pool[start];
+    bool occlude = false;
+    for (unsigned t = 0; t < result.size(); t++) {
+      if (p.id == result[t].id) {
+        occlude = true;
+        break;
+      }
+      float djk = l2(D.row(result[t].id), D.row(p.id), D.d);
+      if (djk < p.distance) {
+        occlude = true;
+        break;
+      }
+    }
+    if (!occlude) result.push_back(p);
+  }
+  SimpleNeighbor *des = cut_graph + (size_t)query * range;
+  for (size_t t = 0; t < result.size(); t++) des[t] = result[t];
+  if (result.size() < range) des[result.size()].distance = -1;
+}
+
+// ComponentPruneVAMANA::PruneInner (component_prune.cpp:245-300)
+void prune_vamana(const Data &D, unsigned query, unsigned range, float alpha, std::vector<SimpleNeighbor> &pool,
+                  SimpleNeighbor *cut_graph) {
+  std::vector<SimpleNeighbor> picked;
+  if (pool.size() > range) {
+    std::sort(pool.begin(), pool.end());
+    MinHeap skipped;
+    for (size_t i = 0; i < pool.size(); i++) {
+      bool skip = false;
+      float cur_dist = pool[i].distance;
+      for (size_t j = 0; j < picked.size(); j++) {
+        float dist = l2(D.row(picked[j].id), D.row(pool[i].id), D.d);
+        if (alpha * dist < cur_dist) {
+          skip = true;
+          break;
+        }
+      }
+      if (!skip) picked.push_back(pool[i]);
+      else skipped.push(cur_dist, pool[i]);
+      if (picked.size() == range) break;
+    }
+    while (picked.size() < range && skipped.size()) {
+      picked.push_back(skipped.top().data);
+      skipped.pop();
+    }
+  } else {
+    for (size_t i = 0; i < pool.size(); i++) picked.push_back(pool[i]);
+  }
+  SimpleNeighbor *des = cut_graph + (size_t)query * range;
+  for (size_t t = 0; t < picked.size(); t++) des[t] = picked[t];
+  if (picked.size() < range) des[picked.size()].distance = -1;
+}
+
+// ComponentRefineNSG::InterInsert (component_refine.cpp:474-541) and
+// ComponentRefineVAMANA::InterInsert (component_refine.cpp:874-950).  The
+// Vamana re-prune reads temp_pool[i] (the outer index) as the distance to
+// beat, as the reference does at component_refine.cpp:907.
+void inter_insert(const Data &D, unsigned n, unsigned range, bool vamana, float alpha, std::vector<std::mutex> &locks,
+                  SimpleNeighbor *cut_graph) {
+  SimpleNeighbor *src_pool = cut_graph + (size_t)n * range;
+  for (size_t i = 0; i < range; i++) {
+    if (src_pool[i].distance == -1) break;
+    SimpleNeighbor sn(n, src_pool[i].distance);
+    size_t des = src_pool[i].id;
+    SimpleNeighbor *des_pool = cut_graph + des * range;
+    std::vector<SimpleNeighbor> temp_pool;
+    int dup = 0;
+    {
+      std::lock_guard<std::mutex> guard(locks[des]);
+      for (size_t j = 0; j < range; j++) {
+        if (des_pool[j].distance == -1) break;
+        if (n == des_pool[j].id) {
+          dup = 1;
+          break;
+        }
+        temp_pool.push_back(des_pool[j]);
+      }
+    }
+    if (dup) continue;
+    temp_pool.push_back(sn);
+    if (temp_pool.size() > range) {
+      std::vector<SimpleNeighbor> result;
+      std::sort(temp_pool.begin(), temp_pool.end());
+      if (!vamana) {
+        unsigned start = 0;
+        result.push_back(temp_pool[start]);
+        while (result.size() < range && (++start) < temp_pool.size()) {
+          auto &p = temp_pool[start];
+          bool occlude = false;
+          for (unsigned t = 0; t < result.size(); t++) {
+            if (p.id == result[t].id) {
+              occlude = true;
+              break;
+            }
+            float djk = l2(D.row(result[t].id), D.row(p.id), D.d);
+            if (djk < p.distance) {
+              occlude = true;
+              break;
+            }
+          }
+          if (!occlude) result.push_back(p);
+        }
+      } else {
+        MinHeap skipped;
+        for (int k = (int)temp_pool.size() - 1; k >= 0; --k) {
+          bool skip = false;
+          float cur_dist = temp_pool[i].distance;
+          for (size_t j = 0; j < result.size(); j++) {
+            float dist = l2(D.row(result[j].id), D.row(temp_pool[k].id), D.d);
+            if (alpha * dist < cur_dist) {
+              skip = true;
+              break;
+            }
+          }
+          if (!skip) result.push_back(temp_pool[k]);
+          else skipped.push(cur_dist, temp_pool[k]);
+          if (result.size() == range) break;
+        }
+        while (result.size() < range && skipped.size()) {
+          result.push_back(skipped.top().data);
+          skipped.pop();
+        }
+      }
+      std::lock_guard<std::mutex> guard(locks[des]);
+      for (unsigned t = 0; t < result.size(); t++) des_pool[t] = result[t];
+    } else {
+      std::lock_guard<std::mutex> guard(locks[des]);
+      for (unsigned t = 0; t < range; t++) {
+        if (des_pool[t].distance == -1) {
+          des_pool[t] = sn;
+          if (t + 1 < range) des_pool[t + 1].distance = -1;
+          break;
+        }
+      }
+    }
+  }
+}
+
+// cut_graph_ -> final_graph_ (component_refine.cpp:406-421, 807-824),
+// including the reference's row length rule (an empty row keeps one entry)
+FinalGraph cut_to_final(const std::vector<SimpleNeighbor> &cut, unsigned n, unsigned range) {
+  FinalGraph fg(n);
+  for (size_t i = 0; i < n; i++) {
+    const SimpleNeighbor *pool = cut.data() + i * range;
+    unsigned pool_size = 0;
+    for (unsigned j = 0; j < range; j++) {
+      if (pool[j].distance == -1) break;
+      pool_size = j;
+    }
+    pool_size++;
+    fg[i].assign(pool, pool + pool_size);
+  }
+  return fg;
+}
+
+// Link for both refines (component_refine.cpp:438-472, 835-872)
+FinalGraph link(const Data &D, const FinalGraph &g, unsigned ep, unsigned Lr, unsigned Rr, unsigned Cr, bool vamana,
+                float alpha, GlibcRand &rnd, int threads) {
+  std::vector<SimpleNeighbor> cut((size_t)D.n * Rr);
+  std::vector<std::mutex> locks(D.n);
+#pragma omp parallel num_threads(threads)
+  {
+    std::vector<SimpleNeighbor> pool;
+    std::vector<char> flags(D.n);
+#pragma omp for schedule(dynamic, 100)
+    for (unsigned n = 0; n < D.n; ++n) {
+      pool.clear();
+      std::fill(flags.begin(), flags.end(), 0);
+      candidate_nsg(D, g, n, ep, Lr, rnd, pool, flags);
+      if (vamana) prune_vamana(D, n, Rr, alpha, pool, cut.data());
+      else prune_nsg(D, g, n, Rr, Cr, pool, cut.data());
+    }
+#pragma omp for schedule(dynamic, 100)
+    for (unsigned n = 0; n < D.n; ++n) inter_insert(D, n, Rr, vamana, alpha, locks, cut.data());
+  }
+  return cut_to_final(cut, D.n, Rr);
+}
+
+// ComponentConnNSGDFS (component_conn.cpp:10-166)
+void conn_dfs(const Data &D, FinalGraph &g, unsigned ep, unsigned Lr, GlibcRand &rnd, unsigned *added) {
+  std::vector<char> flag(D.n, 0);
+  unsigned root = ep, cnt = 0;
+  *added = 0;
+  while (cnt < D.n) {
+    // DFS (component_conn.cpp:30-58)
+    unsigned tmp = root;
+    std::stack<unsigned> s;
+    s.push(root);
+    if (!flag[root]) cnt++;
+    flag[root] = 1;
+    while (!s.empty()) {
+      unsigned next = D.n + 1;
+      for (unsigned i = 0; i < g[tmp].size(); i++)
+        if (!flag[g[tmp][i].id]) {
+          next = g[tmp][i].id;
+          break;
+        }
+      if (next == D.n + 1) {
+        s.pop();
+        if (s.empty()) break;
+        tmp = s.top();
+        continue;
+      }
+      tmp = next;
+      flag[tmp] = 1;
+      s.push(tmp);
+      cnt++;
+    }
+    if (cnt >= D.n) break;
+    // findroot (component_conn.cpp:60-91)
+    unsigned id = D.n;
+    for (unsigned i = 0; i < D.n; i++)
+      if (!flag[i]) {
+        id = i;
+        break;
+      }
+    if (id == D.n) break;
+    std::vector<Neighbor> tmpv, pool;
+    get_neighbors(D, g, ep, D.row(id), Lr, rnd, tmpv, &pool);
+    std::sort(pool.begin(), pool.end());
+    bool found = false;
+    for (unsigned i = 0; i < pool.size(); i++)
+      if (flag[pool[i].id]) {
+        root = pool[i].id;
+        found = true;
+        break;
+      }
+    if (!found) {
+      while (true) {
+        unsigned rid = (unsigned)rnd.next() % D.n;
+        if (flag[rid]) {
+          root = rid;
+          break;
+        }
+      }
+    }
+    g[root].push_back(SimpleNeighbor(id, l2(D.row(root), D.row(id), D.d)));
+    (*added)++;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void *orc_rand_create(unsigned seed) { return new GlibcRand(seed); }
+void orc_rand_destroy(void *r) { delete (GlibcRand *)r; }
+int orc_rand_next(void *r) { return ((GlibcRand *)r)->next(); }
+void orc_rand_fill(void *r, int *out, unsigned n) {
+  for (unsigned i = 0; i < n; i++) out[i] = ((GlibcRand *)r)->next();
+}
+
+// L2 in the reference's summation order, row by row (for tests)
+void orc_l2_rows(const float *a, const float *b, unsigned n, unsigned d, float *out) {
+  for (unsigned i = 0; i < n; i++) out[i] = l2(a + (size_t)i * d, b + (size_t)i * d, d);
+}
+
+// INIT_RANDOM: out rows of width S (self hits dropped, so deg may be S-1)
+int orc_init_random(const float *base, unsigned n, unsigned d, unsigned S, void *rnd, unsigned *ids, float *dist,
+                    unsigned *deg) {
+  Data D{base, n, d};
+  FinalGraph g = init_random(D, S, *(GlibcRand *)rnd);
+  return graph_to_arrays(g, ids, dist, deg, S);
+}
+
+// REFINE_NN_DESCENT from a given init graph; out rows of width K.
+// stats[0] = reverse-list overflow events (rand() draws), stats[1] unused
+int orc_nndescent(const float *base, unsigned n, unsigned d, const unsigned *in_ids, const float *in_dist,
+                  const unsigned *in_deg, unsigned in_w, unsigned S, unsigned K, unsigned L, unsigned ITER, unsigned R,
+                  void *rnd, int threads, unsigned *ids, float *dist, unsigned *deg, unsigned long long *stats) {
+  Data D{base, n, d};
+  FinalGraph init = graph_from_arrays(in_ids, in_dist, in_deg, n, in_w);
+  NNDescent nd(D, S, K, L, ITER, R, *(GlibcRand *)rnd, threads < 1 ? 1 : threads);
+  nd.init(init);
+  for (unsigned it = 0; it < ITER; it++) {
+    nd.join();
+    nd.update();
+  }
+  FinalGraph fg = nd.finish();
+  if (stats) stats[0] = nd.overflow_events;
+  return graph_to_arrays(fg, ids, dist, deg, K);
+}
+
+// NN-Descent pool state after `iters` iterations (debug / fine-grained parity):
+// pools sorted, with flags; width L
+int orc_nndescent_pools(const float *base, unsigned n, unsigned d, const unsigned *in_ids, const float *in_dist,
+                        const unsigned *in_deg, unsigned in_w, unsigned S, unsigned L, unsigned iters, unsigned R,
+                        void *rnd, unsigned *ids, float *dist, unsigned char *flag, unsigned *deg, unsigned *M) {
+  Data D{base, n, d};
+  FinalGraph init = graph_from_arrays(in_ids, in_dist, in_deg, n, in_w);
+  NNDescent nd(D, S, L, L, iters, R, *(GlibcRand *)rnd, 1);
+  nd.init(init);
+  for (unsigned it = 0; it < iters; it++) {
+    nd.join();
+    nd.update();
+  }
+  for (unsigned i = 0; i < n; i++) {
+    // the pool as the update left it (a heap); report it as stored
+    deg[i] = (unsigned)nd.graph[i].pool.size();
+    M[i] = nd.graph[i].M;
+    for (unsigned j = 0; j < deg[i]; j++) {
+      ids[(size_t)i * L + j] = nd.graph[i].pool[j].id;
+      dist[(size_t)i * L + j] = nd.graph[i].pool[j].distance;
+      flag[(size_t)i * L + j] = nd.graph[i].pool[j].flag;
+    }
+  }
+  return 0;
+}
+
+// REFINE_VAMANA (component_refine.cpp:794-872) on graph `in`; entry_L is the
+// index's L_refine member (0 unless an NSG refine ran before).  Out width R.
+int orc_vamana(const float *base, unsigned n, unsigned d, const unsigned *in_ids, const float *in_dist,
+               const unsigned *in_deg, unsigned in_w, unsigned L_refine, unsigned R_refine, float alpha,
+               unsigned entry_L, void *rnd, int threads, unsigned *ids, float *dist, unsigned *deg, unsigned *ep) {
+  Data D{base, n, d};
+  GlibcRand &r = *(GlibcRand *)rnd;
+  FinalGraph g = graph_from_arrays(in_ids, in_dist, in_deg, n, in_w);
+  unsigned e = entry_centroid(D, g, entry_L, r);
+  FinalGraph out = link(D, g, e, L_refine, R_refine, 0, true, alpha, r, threads < 1 ? 1 : threads);
+  *ep = e;
+  return graph_to_arrays(out, ids, dist, deg, R_refine);
+}
+
+// REFINE_NSG (component_refine.cpp:393-428) incl. ConnNSGDFS; out width out_w
+// (>= R_refine: the connectivity pass may lengthen rows)
+int orc_nsg(const float *base, unsigned n, unsigned d, const unsigned *in_ids, const float *in_dist,
+            const unsigned *in_deg, unsigned in_w, unsigned L_refine, unsigned R_refine, unsigned C_refine,
+            void *rnd, int threads, unsigned *ids, float *dist, unsigned *deg, unsigned out_w, unsigned *ep,
+            unsigned *conn_added) {
+  Data D{base, n, d};
+  GlibcRand &r = *(GlibcRand *)rnd;
+  FinalGraph g = graph_from_arrays(in_ids, in_dist, in_deg, n, in_w);
+  unsigned e = entry_centroid(D, g, L_refine, r);
+  FinalGraph out = link(D, g, e, L_refine, R_refine, C_refine, false, 1.0f, r, threads < 1 ? 1 : threads);
+  conn_dfs(D, out, e, L_refine, r, conn_added);
+  *ep = e;
+  return graph_to_arrays(out, ids, dist, deg, out_w);
+}
+
+// IndexBuilder::search with L_SEARCH_ASSIGN (builder.cpp:430-454):
+// entry 0 = SearchEntryRand (component_search_entry.cpp:9-30),
+// entry 1 = SearchEntryCentroid (component_search_entry.cpp:33-67),
+// route = ComponentSearchRouteGreedy (component_route.cpp:9-53).
+// res: nq x K ids; counters: [dist_count, hop_count].  With threads > 1 the
+// seed draws are made first in query order (so results stay deterministic)
+// and the queries then run in an OpenMP loop like builder.cpp:285-295.
+int orc_search(const float *base, unsigned n, unsigned d, const float *query, unsigned nq, const unsigned *g_ids,
+               const unsigned *g_deg, unsigned g_w, unsigned ep, int entry, unsigned L, unsigned K, void *rnd,
+               int threads, unsigned *res, unsigned long long *counters) {
+  if (L < K) return -1;
+  GlibcRand &r = *(GlibcRand *)rnd;
+  std::vector<std::vector<unsigned>> seeds(nq, std::vector<unsigned>(L));
+  for (unsigned q = 0; q < nq; q++) {
+    if (entry == 0) {
+      std::mt19937 rng(r.next());
+      gen_random(rng, seeds[q].data(), L, n);
+    } else {
+      std::vector<char> flags(n, 0);
+      unsigned t = 0;
+      for (; t < L && t < g_deg[ep]; t++) {
+        seeds[q][t] = g_ids[(size_t)ep * g_w + t];
+        flags[seeds[q][t]] = 1;
+      }
+      while (t < L) {
+        unsigned id = (unsigned)r.next() % n;
+        if (flags[id]) continue;
+        flags[id] = 1;
+        seeds[q][t++] = id;
+      }
+    }
+  }
+  unsigned long long dc = 0, hc = 0;
+#pragma omp parallel num_threads(threads < 1 ? 1 : threads) reduction(+ : dc, hc)
+  {
+    std::vector<char> flags(n);
+    std::vector<Neighbor> pool(L + 1);
+#pragma omp for schedule(dynamic, 16)
+    for (unsigned q = 0; q < nq; q++) {
+      const float *qv = query + (size_t)q * d;
+      for (unsigned i = 0; i < L; i++) {
+        unsigned id = seeds[q][i];
+        pool[i] = Neighbor(id, l2(qv, base + (size_t)id * d, d), true);
+        dc++;
+      }
+      std::sort(pool.begin(), pool.begin() + L);
+      std::fill(flags.begin(), flags.end(), 0);
+      int k = 0;
+      while (k < (int)L) {
+        int nk = (int)L;
+        if (pool[k].flag) {
+          pool[k].flag = false;
+          unsigned nd = pool[k].id;
+          hc++;
+          for (unsigned m = 0; m < g_deg[nd]; ++m) {
+            unsigned id = g_ids[(size_t)nd * g_w + m];
+            if (flags[id]) continue;
+            flags[id] = 1;
+            float dist = l2(qv, base + (size_t)id * d, d);
+            dc++;
+            if (dist >= pool[L - 1].distance) continue;
+            int rr = insert_into_pool(pool.data(), L, Neighbor(id, dist, true));
+            if (rr < nk) nk = rr;
+          }
+        }
+        if (nk <= k) k = nk;
+        else ++k;
+      }
+      for (unsigned i = 0; i < K; i++) res[(size_t)q * K + i] = pool[i].id;
+    }
+  }
+  counters[0] = dc;
+  counters[1] = hc;
+  return 0;
+}
+
+// Seeds only (the host side of the GPU search does the same draws)
+int orc_search_seeds(unsigned n, unsigned nq, const unsigned *g_ids, const unsigned *g_deg, unsigned g_w, unsigned ep,
+                     int entry, unsigned L, void *rnd, unsigned *seeds) {
+  GlibcRand &r = *(GlibcRand *)rnd;
+  for (unsigned q = 0; q < nq; q++) {
+    unsigned *s = seeds + (size_t)q * L;
+    if (entry == 0) {
+      std::mt19937 rng(r.next());
+      gen_random(rng, s, L, n);
+    } else {
+      std::vector<char> flags(n, 0);
+      unsigned t = 0;
+      for (; t < L && t < g_deg[ep]; t++) {
+        s[t] = g_ids[(size_t)ep * g_w + t];
+        flags[s[t]] = 1;
+      }
+      while (t < L) {
+        unsigned id = (unsigned)r.next() % n;
+        if (flags[id]) continue;
+        flags[id] = 1;
+        s[t++] = id;
+      }
+    }
+  }
+  return 0;
+}
+
+}  // extern "C"

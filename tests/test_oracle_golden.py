@@ -1,0 +1,67 @@
+"""The oracle (C++ restatement, oracle/weavess_oracle.cpp) against fixtures
+produced by the unmodified reference: every graph row, entry point, search
+result id and DistCount/HopCount must be identical."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as O
+from golden_util import cases, load, graph_of, rows_equal
+
+
+def test_rand_stream_matches_glibc():
+    libc = ctypes.CDLL("libc.so.6")
+    libc.srand(1)
+    r = O.Rand(1)
+    assert all(r.next() == libc.rand() for _ in range(20000))
+    libc.srand(12345)
+    r = O.Rand(12345)
+    assert all(r.next() == libc.rand() for _ in range(20000))
+
+
+@pytest.mark.parametrize("name", cases())
+def test_oracle_replays_reference(name):
+    f = load(name)
+    p = f["params"]
+    base, query = f["base"], f["query"]
+    for pi, steps in enumerate(f["pipelines"]):
+        rnd = O.Rand(1)
+        g = None
+        loaded = None
+        entry_L = 0
+        alpha = p["alpha"]
+        vam_pass = 0
+        for s in steps:
+            kind, _, arg = s.partition(":")
+            key = f"p{pi}."
+            if kind == "init_random":
+                g = O.init_random(base, p["S"], rnd)
+                exp = graph_of(f, key + "init")
+            elif kind == "nndescent":
+                g = O.nndescent(base, g, p["S"], p["K"], p["L"], p["ITER"], p["R"], rnd)
+                exp = graph_of(f, key + "nnd")
+            elif kind == "vamana":
+                vam_pass += 1
+                g = O.vamana(base, g, p["L_refine"], p["R_refine"], alpha, rnd, entry_L=entry_L)
+                alpha = 2.0  # the reference sets alpha = 2 after a Vamana link
+                last = vam_pass == steps.count("vamana")
+                exp = graph_of(f, key + ("vamana" if last else f"vamana{vam_pass}"))
+            elif kind == "nsg":
+                g = O.nsg(base, g, p["L_refine"], p["R_refine"], p["C_refine"], rnd)
+                entry_L = p["L_refine"]
+                exp = graph_of(f, key + "nsg")
+            elif kind == "load":
+                loaded = g
+                continue
+            elif kind.startswith("search"):
+                entry = "rand" if kind == "search_rand" else "centroid"
+                res, dc, hc = O.search(base, query, loaded, int(arg), rnd, entry=entry)
+                k = f"{key}{kind}_{arg}"
+                assert np.array_equal(res, f[k + ".res"]), (name, s)
+                assert [dc, hc] == f[k + ".counts"].tolist(), (name, s)
+                continue
+            ids, dist, deg, ep = exp
+            assert rows_equal(g.ids, g.dist, g.deg, ids, dist, deg) == 0, (name, s)
+            if ep is not None:
+                assert g.ep == ep, (name, s)
