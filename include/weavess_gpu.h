@@ -1,0 +1,98 @@
+/* weavess_gpu.h -- C ABI of the GB300 implementation of the WEAVESS hot path.
+ *
+ * The reference exposes this path as per-item C++ virtuals called from
+ * OpenMP loops inside IndexBuilder (include/weavess/component.h).  A GPU
+ * wants whole batches, so each entry point below replaces one of those
+ * components for ALL items at once, reading and writing the reference's own
+ * layouts (row-major float base, per-node adjacency rows with distances).
+ *
+ * Conventions: every call returns a wv_status; wv_last_error() describes the
+ * last failure.  No exception crosses the ABI.  Host buffers are owned by the
+ * caller.  A context owns one GPU's device memory and stream; calls on one
+ * context must not overlap (one context per thread).  Random draws come from
+ * a per-context stream that reproduces glibc rand() (seeded 1 like a fresh
+ * process), or from a caller-supplied rand function (wv_set_rand_source),
+ * consumed in the same order as the reference consumes rand().
+ */
+#ifndef WEAVESS_GPU_H
+#define WEAVESS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  WV_OK = 0,
+  WV_ERR_ARG = 1,      /* invalid argument (sizes, NULL, L < K ...) */
+  WV_ERR_CUDA = 2,     /* a CUDA call failed */
+  WV_ERR_STATE = 3,    /* missing base/graph, or no device */
+  WV_ERR_NOMEM = 4,    /* device allocation failed */
+  WV_ERR_LIMIT = 5,    /* a size beyond what this build supports */
+  WV_ERR_DEVICE = 6    /* a kernel reported corrupt input or a bounded wait ran out */
+} wv_status;
+
+typedef enum {
+  WV_ENTRY_RAND = 0,     /* ComponentSearchEntryRand (component_search_entry.cpp:9-30) */
+  WV_ENTRY_CENTROID = 1, /* ComponentSearchEntryCentroid (component_search_entry.cpp:33-67) */
+  WV_ENTRY_SEEDS = 2     /* caller-supplied seed ids (nq x L) */
+} wv_entry;
+
+typedef struct wv_ctx wv_ctx;
+
+typedef struct {
+  unsigned long long dist_count; /* Index::addDistCount calls (entry + route) */
+  unsigned long long hop_count;  /* Index::addHopCount calls (expansions) */
+} wv_counters;
+
+/* ---- context ---------------------------------------------------------- */
+int wv_ctx_create(wv_ctx **ctx, int device);
+int wv_ctx_destroy(wv_ctx *ctx);
+const char *wv_last_error(const wv_ctx *ctx);
+/* glibc-compatible rand() stream of the context (srand semantics) */
+int wv_srand(wv_ctx *ctx, unsigned seed);
+/* draw from `fn` instead (e.g. the process's own rand, to share its stream
+ * with the rest of a reference process); NULL restores the context stream */
+int wv_set_rand_source(wv_ctx *ctx, int (*fn)(void));
+/* next value of the context's rand stream (for callers that interleave) */
+int wv_rand(wv_ctx *ctx, int *out);
+
+/* ---- data --------------------------------------------------------------- */
+/* Replaces the base arrays ComponentLoad::LoadInner hands to the index
+ * (component_load.cpp:67-104): n x d float32, row-major. */
+int wv_upload_base(wv_ctx *ctx, const float *base, uint32_t n, uint32_t d);
+/* Replaces IndexBuilder::load_graph (builder.cpp:1083-1311): the search graph
+ * (load_graph_) as fixed-width rows, ids[n*width], deg[n], entry point ep_. */
+int wv_upload_graph(wv_ctx *ctx, const uint32_t *ids, const uint32_t *deg, uint32_t n, uint32_t width,
+                    uint32_t ep);
+
+/* ---- search ------------------------------------------------------------- */
+/* Replaces the query loop of IndexBuilder::search with L_SEARCH_ASSIGN
+ * (builder.cpp:430-454): SearchEntryInner (entry) + ComponentSearchRouteGreedy
+ * ::RouteInner (component_route.cpp:9-53) for every query, K_search = K.
+ * queries: nq x d host floats; out_ids: nq x K; out_dist (nullable): nq x K.
+ * seeds: nq x L ids when entry == WV_ENTRY_SEEDS, else NULL. */
+int wv_search(wv_ctx *ctx, const float *queries, uint32_t nq, int entry, uint32_t L, uint32_t K,
+              const uint32_t *seeds, uint32_t *out_ids, float *out_dist, wv_counters *counters);
+
+/* Mixed beam widths in one launch: per-query L[q] and K[q]; results at
+ * out_ids[q*out_stride + j], j < K[q]. */
+int wv_search_batch(wv_ctx *ctx, const float *queries, uint32_t nq, int entry, const uint32_t *L,
+                    const uint32_t *K, uint32_t out_stride, uint32_t *out_ids, float *out_dist,
+                    wv_counters *counters);
+
+/* Same as wv_search, with queries / seeds / outputs already in device memory
+ * (d_seeds required: the caller drew them, e.g. with wv_draw_seeds). */
+int wv_search_device(wv_ctx *ctx, const float *d_queries, uint32_t nq, uint32_t L, uint32_t K,
+                     const uint32_t *d_seeds, uint32_t *d_out_ids, float *d_out_dist, wv_counters *counters);
+
+/* The seed ids SearchEntryInner would draw for nq queries (host nq x L),
+ * consuming the context's rand stream exactly as the reference does. */
+int wv_draw_seeds(wv_ctx *ctx, uint32_t nq, int entry, uint32_t L, uint32_t *seeds);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WEAVESS_GPU_H */

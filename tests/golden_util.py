@@ -43,3 +43,53 @@ def rows_equal(ids_a, dist_a, deg_a, ids_b, dist_b, deg_b, check_dist=True):
                                                np.asarray(dist_b[i, :k], np.float32).view(np.uint32)):
             bad += 1
     return bad
+
+
+def replay_oracle(f, pi, on_search=None, on_graph=None):
+    """Replays pipeline `pi` of fixture `f` with the oracle (single thread,
+    glibc rand stream seeded 1).  For each search step, on_search(kind, L,
+    graph, rnd) may return (res, dc, hc) from the implementation under test
+    (default: the oracle).  For each graph step, on_graph(kind, graph, rnd)
+    may return a graph to continue with.  Yields (step, expected_key, got)."""
+    import oracle as O
+    p = f["params"]
+    base, query = f["base"], f["query"]
+    steps = f["pipelines"][pi]
+    rnd = O.Rand(1)
+    g = loaded = None
+    entry_L = 0
+    alpha = p["alpha"]
+    vam_pass = 0
+    for s in steps:
+        kind, _, arg = s.partition(":")
+        key = f"p{pi}."
+        if kind == "init_random":
+            g = O.init_random(base, p["S"], rnd)
+            exp = key + "init"
+        elif kind == "nndescent":
+            g = O.nndescent(base, g, p["S"], p["K"], p["L"], p["ITER"], p["R"], rnd)
+            exp = key + "nnd"
+        elif kind == "vamana":
+            vam_pass += 1
+            g = O.vamana(base, g, p["L_refine"], p["R_refine"], alpha, rnd, entry_L=entry_L)
+            alpha = 2.0
+            exp = key + ("vamana" if vam_pass == steps.count("vamana") else f"vamana{vam_pass}")
+        elif kind == "nsg":
+            g = O.nsg(base, g, p["L_refine"], p["R_refine"], p["C_refine"], rnd)
+            entry_L = p["L_refine"]
+            exp = key + "nsg"
+        elif kind == "load":
+            loaded = g
+            continue
+        else:
+            entry = "rand" if kind == "search_rand" else "centroid"
+            L = int(arg)
+            got = on_search(entry, L, loaded, rnd) if on_search else O.search(base, query, loaded, L, rnd,
+                                                                              entry=entry)
+            yield s, f"{key}{kind}_{arg}", got
+            continue
+        if on_graph is not None:
+            g2 = on_graph(kind, g, rnd)
+            if g2 is not None:
+                g = g2
+        yield s, exp, g

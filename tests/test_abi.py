@@ -1,0 +1,23 @@
+"""The C-ABI library builds, loads and exports every function the header
+declares (no GPU needed)."""
+import ctypes
+
+from weavess_gb300 import _lib, build
+
+
+def test_library_exports_header_symbols():
+    path = build.build()
+    lib = ctypes.CDLL(path)
+    names = _lib.declared_functions()
+    assert len(names) >= 10
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_ctx_create_without_gpu_fails_cleanly():
+    import torch
+    if torch.cuda.is_available():
+        return
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    assert lib.wv_ctx_create(ctypes.byref(h), 0) != 0

@@ -1,0 +1,66 @@
+"""ctypes binding of libweavess_gpu.so (the C ABI in include/weavess_gpu.h).
+
+There is no fallback: if the library is missing or a call fails, this raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+HEADER = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "include", "weavess_gpu.h")
+
+u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+
+
+class WeavessError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class Counters(C.Structure):
+    _fields_ = [("dist_count", C.c_ulonglong), ("hop_count", C.c_ulonglong)]
+
+
+def declared_functions():
+    """Names of every function the C header declares."""
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(wv_\w+)\s*\(", txt, re.M)))
+
+
+def load(build_if_needed: bool = True):
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_needed:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise WeavessError(-1, f"{path} is missing: build it with weavess_gb300.build.build()")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.wv_ctx_create.argtypes = [C.POINTER(vp), C.c_int]
+    L.wv_ctx_destroy.argtypes = [vp]
+    L.wv_last_error.argtypes = [vp]
+    L.wv_last_error.restype = C.c_char_p
+    L.wv_srand.argtypes = [vp, C.c_uint]
+    L.wv_set_rand_source.argtypes = [vp, vp]
+    L.wv_rand.argtypes = [vp, C.POINTER(C.c_int)]
+    L.wv_upload_base.argtypes = [vp, f32p, C.c_uint32, C.c_uint32]
+    L.wv_upload_graph.argtypes = [vp, u32p, u32p, C.c_uint32, C.c_uint32, C.c_uint32]
+    L.wv_search.argtypes = [vp, f32p, C.c_uint32, C.c_int, C.c_uint32, C.c_uint32, vp, u32p, vp,
+                            C.POINTER(Counters)]
+    L.wv_search_batch.argtypes = [vp, f32p, C.c_uint32, C.c_int, u32p, u32p, C.c_uint32, u32p, vp,
+                                  C.POINTER(Counters)]
+    L.wv_search_device.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp, vp, C.POINTER(Counters)]
+    L.wv_draw_seeds.argtypes = [vp, C.c_uint32, C.c_int, C.c_uint32, u32p]
+    _lib = L
+    return L

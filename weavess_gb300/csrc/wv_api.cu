@@ -1,0 +1,311 @@
+// C ABI: context, data upload and search entry points (include/weavess_gpu.h).
+#include <algorithm>
+#include <cstring>
+
+#include "wv_ctx.h"
+#include "wv_search.h"
+
+using namespace wv;
+
+namespace wv {
+
+int check_device_status(wv_ctx *c, const char *what) {
+  int st = 0;
+  WV_CUDA(c, cudaMemcpyAsync(&st, c->d_status(), sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (st != 0) {
+    WV_CUDA(c, cudaMemsetAsync(c->d_status(), 0, sizeof(int), c->stream));
+    const char *why = st == 1 ? "an id >= n or a row longer than the graph width"
+                      : st == 2 ? "a bounded device buffer overflowed"
+                                : "a bounded wait timed out";
+    return fail(c, WV_ERR_DEVICE, "%s: kernel reported %s (code %d)", what, why, st);
+  }
+  return WV_OK;
+}
+
+}  // namespace wv
+
+namespace {
+
+int ensure_search_scratch(wv_ctx *c, uint32_t Lmax) {
+  const uint32_t cap = c->gw + 32;
+  int blocks = search_grid(c->d, Lmax, cap, c->device);
+  WV_CHECK(c, blocks > 0, WV_ERR_LIMIT, "search kernel cannot run with d=%u L=%u width=%u (shared memory)", c->d,
+           Lmax, c->gw);
+  size_t slots = (size_t)blocks * search_warps_per_block();
+  size_t words = (c->n + 31) / 32;
+  if (slots > c->vis_slots || words != c->vis_words) {
+    c->visited.release();
+    c->touched.release();
+    WV_CUDA(c, c->visited.ensure(slots * words * 4));
+    WV_CUDA(c, c->touched.ensure(slots * words * 4));
+    WV_CUDA(c, cudaMemsetAsync(c->visited.p, 0, slots * words * 4, c->stream));
+    c->vis_slots = slots;
+    c->vis_words = words;
+  }
+  return blocks;
+}
+
+// runs the kernel on device-resident queries / seeds / outputs
+int run_search(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t *d_seeds, uint32_t seed_stride,
+               const uint32_t *d_L, const uint32_t *d_K, uint32_t L, uint32_t K, uint32_t Lmax, uint32_t *d_out,
+               float *d_dist, uint32_t out_stride, wv_counters *counters) {
+  int blocks = ensure_search_scratch(c, Lmax);
+  if (blocks <= 0) return blocks < 0 ? -blocks : WV_ERR_LIMIT;
+  WV_CUDA(c, cudaMemsetAsync(c->misc.p, 0, 32, c->stream));
+  SearchArgs a{};
+  a.base = c->base.as<float>();
+  a.n = c->n;
+  a.d = c->d;
+  a.gids = c->gids.as<uint32_t>();
+  a.gdeg = c->gdeg.as<uint32_t>();
+  a.gw = c->gw;
+  a.queries = d_q;
+  a.nq = nq;
+  a.seeds = d_seeds;
+  a.seed_stride = seed_stride;
+  a.Lq = d_L;
+  a.Kq = d_K;
+  a.L = L;
+  a.K = K;
+  a.Lmax = Lmax;
+  a.out_ids = d_out;
+  a.out_dist = d_dist;
+  a.out_stride = out_stride;
+  a.counters = c->d_counters();
+  a.visited = c->visited.as<uint32_t>();
+  a.touched = c->touched.as<uint32_t>();
+  a.words = (uint32_t)c->vis_words;
+  a.cap = c->gw + 32;
+  a.next_query = c->d_next();
+  a.status = c->d_status();
+  int nb = std::min<long>(blocks, ((long)nq + search_warps_per_block() - 1) / search_warps_per_block());
+  if (nb < 1) nb = 1;
+  WV_CUDA(c, launch_search_exact(a, nb, c->stream));
+  if (counters) {
+    unsigned long long h[2];
+    WV_CUDA(c, cudaMemcpyAsync(h, c->d_counters(), 16, cudaMemcpyDeviceToHost, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    counters->dist_count = h[0];
+    counters->hop_count = h[1];
+  }
+  return check_device_status(c, "search");
+}
+
+int check_search_args(wv_ctx *c, uint32_t nq, uint32_t L, uint32_t K) {
+  WV_CHECK(c, c->n > 0, WV_ERR_STATE, "no base uploaded");
+  WV_CHECK(c, c->gn == c->n, WV_ERR_STATE, "no search graph for the uploaded base (graph n=%u, base n=%u)", c->gn,
+           c->n);
+  WV_CHECK(c, c->d % 4 == 0, WV_ERR_LIMIT, "dimension %u is not a multiple of 4", c->d);
+  WV_CHECK(c, K >= 1 && L >= K, WV_ERR_ARG, "search_L cannot be smaller than search_K (L=%u K=%u)", L, K);
+  WV_CHECK(c, L < c->n, WV_ERR_ARG, "L=%u must be smaller than n=%u", L, c->n);
+  WV_CHECK(c, L <= SEARCH_MAX_L, WV_ERR_LIMIT, "L=%u above the supported maximum %u", L, SEARCH_MAX_L);
+  (void)nq;
+  return WV_OK;
+}
+
+int draw(wv_ctx *c, uint32_t nq, int entry, uint32_t L, uint32_t *seeds, uint32_t stride) {
+  if (entry == WV_ENTRY_RAND) {
+    draw_seeds_rand(c->rnd, nq, L, c->n, seeds, stride);
+  } else if (entry == WV_ENTRY_CENTROID) {
+    WV_CHECK(c, c->gn == c->n, WV_ERR_STATE, "centroid entry needs the search graph");
+    draw_seeds_centroid(c->rnd, nq, L, c->n, c->ep_row.data(), (uint32_t)c->ep_row.size(), seeds, stride);
+  } else {
+    return fail(c, WV_ERR_ARG, "unknown entry %d", entry);
+  }
+  return WV_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wv_ctx_create(wv_ctx **out, int device) {
+  if (!out) return WV_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return WV_ERR_STATE;
+  wv_ctx *c = new wv_ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) !=
+                                                  cudaSuccess) {
+    delete c;
+    return WV_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+  if (c->misc.ensure(64) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return WV_ERR_NOMEM;
+  }
+  cudaMemset(c->misc.p, 0, 64);
+  *out = c;
+  return WV_OK;
+}
+
+int wv_ctx_destroy(wv_ctx *c) {
+  if (!c) return WV_ERR_ARG;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (DevBuf *b : {&c->base, &c->gids, &c->gdeg, &c->visited, &c->touched, &c->misc, &c->q_buf, &c->seed_buf,
+                    &c->out_ids_buf, &c->out_dist_buf, &c->lq_buf, &c->kq_buf})
+    b->release();
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return WV_OK;
+}
+
+const char *wv_last_error(const wv_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int wv_srand(wv_ctx *c, unsigned seed) {
+  if (!c) return WV_ERR_ARG;
+  c->rnd.own.seed_with(seed);
+  return WV_OK;
+}
+
+int wv_set_rand_source(wv_ctx *c, int (*fn)(void)) {
+  if (!c) return WV_ERR_ARG;
+  c->rnd.fn = fn;
+  return WV_OK;
+}
+
+int wv_rand(wv_ctx *c, int *out) {
+  if (!c || !out) return WV_ERR_ARG;
+  *out = c->rnd.next();
+  return WV_OK;
+}
+
+int wv_upload_base(wv_ctx *c, const float *base, uint32_t n, uint32_t d) {
+  if (!c) return WV_ERR_ARG;
+  WV_CHECK(c, base && n > 0 && d > 0, WV_ERR_ARG, "empty base");
+  WV_CHECK(c, (uint64_t)n * d < (1ull << 32), WV_ERR_LIMIT, "n*d=%llu overflows the reference's 32-bit offsets",
+           (unsigned long long)n * d);
+  WV_CUDA(c, cudaSetDevice(c->device));
+  WV_CUDA(c, c->base.ensure((size_t)n * d * 4));
+  WV_CUDA(c, cudaMemcpyAsync(c->base.p, base, (size_t)n * d * 4, cudaMemcpyHostToDevice, c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (c->n != n) c->gn = 0;  // the old graph no longer matches
+  c->n = n;
+  c->d = d;
+  return WV_OK;
+}
+
+int wv_upload_graph(wv_ctx *c, const uint32_t *ids, const uint32_t *deg, uint32_t n, uint32_t width, uint32_t ep) {
+  if (!c) return WV_ERR_ARG;
+  WV_CHECK(c, ids && deg && n > 0 && width > 0, WV_ERR_ARG, "empty graph");
+  WV_CHECK(c, width <= SEARCH_MAX_WIDTH, WV_ERR_LIMIT, "graph width %u above %u", width, SEARCH_MAX_WIDTH);
+  WV_CHECK(c, ep < n, WV_ERR_ARG, "entry point %u >= n=%u", ep, n);
+  for (uint32_t i = 0; i < n; i++) WV_CHECK(c, deg[i] <= width, WV_ERR_ARG, "row %u has degree %u > width %u", i, deg[i], width);
+  WV_CUDA(c, cudaSetDevice(c->device));
+  WV_CUDA(c, c->gids.ensure((size_t)n * width * 4));
+  WV_CUDA(c, c->gdeg.ensure((size_t)n * 4));
+  WV_CUDA(c, cudaMemcpyAsync(c->gids.p, ids, (size_t)n * width * 4, cudaMemcpyHostToDevice, c->stream));
+  WV_CUDA(c, cudaMemcpyAsync(c->gdeg.p, deg, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->gn = n;
+  c->gw = width;
+  c->ep = ep;
+  c->ep_row.assign(ids + (size_t)ep * width, ids + (size_t)ep * width + deg[ep]);
+  if (c->vis_words != (n + 31) / 32) c->vis_slots = 0;
+  return WV_OK;
+}
+
+int wv_draw_seeds(wv_ctx *c, uint32_t nq, int entry, uint32_t L, uint32_t *seeds) {
+  if (!c || !seeds) return WV_ERR_ARG;
+  WV_CHECK(c, c->n > 0 && L < c->n, WV_ERR_ARG, "L=%u must be smaller than n=%u", L, c->n);
+  return draw(c, nq, entry, L, seeds, L);
+}
+
+int wv_search(wv_ctx *c, const float *queries, uint32_t nq, int entry, uint32_t L, uint32_t K,
+              const uint32_t *seeds, uint32_t *out_ids, float *out_dist, wv_counters *counters) {
+  if (!c) return WV_ERR_ARG;
+  WV_CHECK(c, queries && out_ids, WV_ERR_ARG, "null buffer");
+  int rc = check_search_args(c, nq, L, K);
+  if (rc) return rc;
+  if (counters) *counters = wv_counters{0, 0};
+  if (nq == 0) return WV_OK;
+  WV_CUDA(c, cudaSetDevice(c->device));
+  std::vector<uint32_t> hs;
+  if (entry == WV_ENTRY_SEEDS) {
+    WV_CHECK(c, seeds != nullptr, WV_ERR_ARG, "WV_ENTRY_SEEDS needs seeds");
+    for (size_t i = 0; i < (size_t)nq * L; i++) WV_CHECK(c, seeds[i] < c->n, WV_ERR_ARG, "seed id %u >= n", seeds[i]);
+  } else {
+    hs.resize((size_t)nq * L);
+    rc = draw(c, nq, entry, L, hs.data(), L);
+    if (rc) return rc;
+    seeds = hs.data();
+  }
+  WV_CUDA(c, c->q_buf.ensure((size_t)nq * c->d * 4));
+  WV_CUDA(c, c->seed_buf.ensure((size_t)nq * L * 4));
+  WV_CUDA(c, c->out_ids_buf.ensure((size_t)nq * K * 4));
+  if (out_dist) WV_CUDA(c, c->out_dist_buf.ensure((size_t)nq * K * 4));
+  WV_CUDA(c, cudaMemcpyAsync(c->q_buf.p, queries, (size_t)nq * c->d * 4, cudaMemcpyHostToDevice, c->stream));
+  WV_CUDA(c, cudaMemcpyAsync(c->seed_buf.p, seeds, (size_t)nq * L * 4, cudaMemcpyHostToDevice, c->stream));
+  rc = run_search(c, c->q_buf.as<float>(), nq, c->seed_buf.as<uint32_t>(), L, nullptr, nullptr, L, K, L,
+                  c->out_ids_buf.as<uint32_t>(), out_dist ? c->out_dist_buf.as<float>() : nullptr, K, counters);
+  if (rc) return rc;
+  WV_CUDA(c, cudaMemcpyAsync(out_ids, c->out_ids_buf.p, (size_t)nq * K * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (out_dist)
+    WV_CUDA(c, cudaMemcpyAsync(out_dist, c->out_dist_buf.p, (size_t)nq * K * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WV_OK;
+}
+
+int wv_search_batch(wv_ctx *c, const float *queries, uint32_t nq, int entry, const uint32_t *L, const uint32_t *K,
+                    uint32_t out_stride, uint32_t *out_ids, float *out_dist, wv_counters *counters) {
+  if (!c) return WV_ERR_ARG;
+  WV_CHECK(c, queries && L && K && out_ids, WV_ERR_ARG, "null buffer");
+  WV_CHECK(c, entry == WV_ENTRY_RAND || entry == WV_ENTRY_CENTROID, WV_ERR_ARG, "batch search draws its seeds");
+  if (counters) *counters = wv_counters{0, 0};
+  if (nq == 0) return WV_OK;
+  uint32_t Lmax = 0;
+  for (uint32_t q = 0; q < nq; q++) {
+    int rc = check_search_args(c, nq, L[q], K[q]);
+    if (rc) return rc;
+    WV_CHECK(c, K[q] <= out_stride, WV_ERR_ARG, "K[%u]=%u > out_stride", q, K[q]);
+    Lmax = std::max(Lmax, L[q]);
+  }
+  WV_CUDA(c, cudaSetDevice(c->device));
+  // seeds drawn query by query with each query's own L, as the reference's
+  // loop would draw them
+  std::vector<uint32_t> hs((size_t)nq * Lmax);
+  for (uint32_t q = 0; q < nq; q++) {
+    int rc = draw(c, 1, entry, L[q], hs.data() + (size_t)q * Lmax, Lmax);
+    if (rc) return rc;
+  }
+  WV_CUDA(c, c->q_buf.ensure((size_t)nq * c->d * 4));
+  WV_CUDA(c, c->seed_buf.ensure(hs.size() * 4));
+  WV_CUDA(c, c->out_ids_buf.ensure((size_t)nq * out_stride * 4));
+  WV_CUDA(c, c->lq_buf.ensure((size_t)nq * 4));
+  WV_CUDA(c, c->kq_buf.ensure((size_t)nq * 4));
+  if (out_dist) WV_CUDA(c, c->out_dist_buf.ensure((size_t)nq * out_stride * 4));
+  WV_CUDA(c, cudaMemcpyAsync(c->q_buf.p, queries, (size_t)nq * c->d * 4, cudaMemcpyHostToDevice, c->stream));
+  WV_CUDA(c, cudaMemcpyAsync(c->seed_buf.p, hs.data(), hs.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  WV_CUDA(c, cudaMemcpyAsync(c->lq_buf.p, L, (size_t)nq * 4, cudaMemcpyHostToDevice, c->stream));
+  WV_CUDA(c, cudaMemcpyAsync(c->kq_buf.p, K, (size_t)nq * 4, cudaMemcpyHostToDevice, c->stream));
+  int rc = run_search(c, c->q_buf.as<float>(), nq, c->seed_buf.as<uint32_t>(), Lmax, c->lq_buf.as<uint32_t>(),
+                      c->kq_buf.as<uint32_t>(), 0, 0, Lmax, c->out_ids_buf.as<uint32_t>(),
+                      out_dist ? c->out_dist_buf.as<float>() : nullptr, out_stride, counters);
+  if (rc) return rc;
+  WV_CUDA(c, cudaMemcpyAsync(out_ids, c->out_ids_buf.p, (size_t)nq * out_stride * 4, cudaMemcpyDeviceToHost,
+                             c->stream));
+  if (out_dist)
+    WV_CUDA(c, cudaMemcpyAsync(out_dist, c->out_dist_buf.p, (size_t)nq * out_stride * 4, cudaMemcpyDeviceToHost,
+                               c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  return WV_OK;
+}
+
+int wv_search_device(wv_ctx *c, const float *d_queries, uint32_t nq, uint32_t L, uint32_t K, const uint32_t *d_seeds,
+                     uint32_t *d_out_ids, float *d_out_dist, wv_counters *counters) {
+  if (!c) return WV_ERR_ARG;
+  WV_CHECK(c, d_queries && d_seeds && d_out_ids, WV_ERR_ARG, "null buffer");
+  int rc = check_search_args(c, nq, L, K);
+  if (rc) return rc;
+  if (counters) *counters = wv_counters{0, 0};
+  if (nq == 0) return WV_OK;
+  WV_CUDA(c, cudaSetDevice(c->device));
+  return run_search(c, d_queries, nq, d_seeds, L, nullptr, nullptr, L, K, L, d_out_ids, d_out_dist, K, counters);
+}
+
+}  // extern "C"

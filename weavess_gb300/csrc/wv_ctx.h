@@ -1,0 +1,100 @@
+// The context behind the C ABI: device memory, stream and rand stream of one
+// GPU.  Shared by the translation units that implement the entry points.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/weavess_gpu.h"
+#include "wv_host.h"
+
+namespace wv {
+
+// grow-only device buffer
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t want) {
+    if (want <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) bytes = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T>
+  T *as() const {
+    return reinterpret_cast<T *>(p);
+  }
+};
+
+}  // namespace wv
+
+struct wv_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  wv::RandSource rnd;
+  int sms = 0;
+
+  // base vectors
+  wv::DevBuf base;
+  uint32_t n = 0, d = 0;
+
+  // search graph (load_graph_)
+  wv::DevBuf gids, gdeg;
+  uint32_t gn = 0, gw = 0, ep = 0;
+  std::vector<uint32_t> ep_row;  // host copy of the entry point's row
+
+  // search scratch
+  wv::DevBuf visited, touched;
+  size_t vis_slots = 0, vis_words = 0;
+  wv::DevBuf misc;  // [0] query counter (u32), [8..24) counters (u64 x2), [32] status (i32)
+
+  // per-call staging
+  wv::DevBuf q_buf, seed_buf, out_ids_buf, out_dist_buf, lq_buf, kq_buf;
+
+  unsigned *d_next() { return misc.as<unsigned>(); }
+  unsigned long long *d_counters() { return reinterpret_cast<unsigned long long *>(misc.as<char>() + 8); }
+  int *d_status() { return reinterpret_cast<int *>(misc.as<char>() + 32); }
+};
+
+namespace wv {
+
+inline int fail(wv_ctx *c, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define WV_CUDA(ctx, call)                                                                         \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      return ::wv::fail(ctx, e_ == cudaErrorMemoryAllocation ? WV_ERR_NOMEM : WV_ERR_CUDA, "%s: %s (%s:%d)", #call, \
+                        cudaGetErrorString(e_), __FILE__, __LINE__);                               \
+  } while (0)
+
+#define WV_CHECK(ctx, cond, code, ...)                      \
+  do {                                                      \
+    if (!(cond)) return ::wv::fail(ctx, code, __VA_ARGS__); \
+  } while (0)
+
+// reads the device status word after a launch; maps kernel-reported errors
+int check_device_status(wv_ctx *c, const char *what);
+
+}  // namespace wv

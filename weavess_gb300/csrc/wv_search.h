@@ -1,0 +1,44 @@
+// Launch interface of the beam-search kernels (wv_search.cu).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wv {
+
+struct SearchArgs {
+  const float *base;
+  uint32_t n, d;
+  const uint32_t *gids;  // graph rows, width gw
+  const uint32_t *gdeg;
+  uint32_t gw;
+  const float *queries;  // nq x d
+  uint32_t nq;
+  const uint32_t *seeds;  // nq x seed_stride
+  uint32_t seed_stride;
+  const uint32_t *Lq;  // per-query beam width (or null: L)
+  const uint32_t *Kq;  // per-query result size (or null: K)
+  uint32_t L, K, Lmax;
+  uint32_t *out_ids;
+  float *out_dist;
+  uint32_t out_stride;
+  unsigned long long *counters;  // [dist_count, hop_count]
+  uint32_t *visited;             // slots x words bitsets, all zero between queries
+  uint32_t *touched;             // slots x words
+  uint32_t words;
+  uint32_t cap;  // candidate buffer entries per warp (graph width + 32)
+  unsigned *next_query;
+  int *status;
+};
+
+constexpr uint32_t SEARCH_MAX_WIDTH = 256;  // graph row width the kernel accepts
+constexpr uint32_t SEARCH_MAX_L = 2048;
+
+// bytes of dynamic shared memory per block and warps per block
+size_t search_block_smem(uint32_t d, uint32_t Lmax, uint32_t cap);
+int search_warps_per_block();
+// blocks to launch for one persistent wave on this device (0 if it cannot run)
+int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device);
+cudaError_t launch_search_exact(const SearchArgs &a, int blocks, cudaStream_t stream);
+
+}  // namespace wv

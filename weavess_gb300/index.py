@@ -1,0 +1,110 @@
+"""Host-side API over the C ABI.
+
+`Context` is one GPU's view of an index: base vectors, the current graph and
+the rand() stream, with one method per reference component it replaces.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+ENTRY = {"rand": 0, "centroid": 1, "seeds": 2}
+
+
+def _u32(x):
+    return np.ascontiguousarray(x, dtype=np.uint32)
+
+
+def _f32(x):
+    return np.ascontiguousarray(x, dtype=np.float32)
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self.L = _lib.load()
+        h = C.c_void_p()
+        rc = self.L.wv_ctx_create(C.byref(h), device)
+        if rc != 0:
+            raise _lib.WeavessError(rc, f"wv_ctx_create(device={device}) failed")
+        self.h = h
+        self.n = self.d = 0
+
+    # -- plumbing
+    def _check(self, rc):
+        if rc != 0:
+            raise _lib.WeavessError(rc, self.L.wv_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.wv_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- rand stream
+    def srand(self, seed: int):
+        self._check(self.L.wv_srand(self.h, seed))
+
+    def rand(self) -> int:
+        v = C.c_int()
+        self._check(self.L.wv_rand(self.h, C.byref(v)))
+        return v.value
+
+    # -- data
+    def upload_base(self, base: np.ndarray):
+        base = _f32(base)
+        self._check(self.L.wv_upload_base(self.h, base, base.shape[0], base.shape[1]))
+        self.n, self.d = base.shape
+
+    def upload_graph(self, ids: np.ndarray, deg: np.ndarray, ep: int = 0):
+        ids = _u32(ids)
+        self._check(self.L.wv_upload_graph(self.h, ids, _u32(deg), ids.shape[0], ids.shape[1], int(ep or 0)))
+
+    # -- search (IndexBuilder::search, L_SEARCH_ASSIGN)
+    def search(self, queries, L: int, K: int = 10, entry="rand", return_dist=False):
+        q = _f32(queries)
+        nq = q.shape[0]
+        out = np.zeros((nq, K), np.uint32)
+        dist = np.zeros((nq, K), np.float32) if return_dist else None
+        cnt = _lib.Counters()
+        if isinstance(entry, np.ndarray):
+            seeds = _u32(entry)
+            assert seeds.shape == (nq, L)
+            rc = self.L.wv_search(self.h, q, nq, ENTRY["seeds"], L, K, seeds.ctypes.data, out,
+                                  None if dist is None else dist.ctypes.data, C.byref(cnt))
+        else:
+            rc = self.L.wv_search(self.h, q, nq, ENTRY[entry], L, K, None, out,
+                                  None if dist is None else dist.ctypes.data, C.byref(cnt))
+        self._check(rc)
+        res = (out, int(cnt.dist_count), int(cnt.hop_count))
+        return res + (dist,) if return_dist else res
+
+    def search_batch(self, queries, L, K, entry="rand"):
+        q = _f32(queries)
+        nq = q.shape[0]
+        L, K = _u32(L), _u32(K)
+        stride = int(K.max())
+        out = np.zeros((nq, stride), np.uint32)
+        cnt = _lib.Counters()
+        self._check(self.L.wv_search_batch(self.h, q, nq, ENTRY[entry], L, K, stride, out, None, C.byref(cnt)))
+        return out, int(cnt.dist_count), int(cnt.hop_count)
+
+    def draw_seeds(self, nq: int, L: int, entry="rand"):
+        out = np.zeros((nq, L), np.uint32)
+        self._check(self.L.wv_draw_seeds(self.h, nq, ENTRY[entry], L, out))
+        return out
+
+    def search_device(self, d_queries_ptr: int, nq: int, L: int, K: int, d_seeds_ptr: int, d_out_ptr: int,
+                      d_dist_ptr: int = 0, counters: bool = False):
+        cnt = _lib.Counters() if counters else None
+        self._check(self.L.wv_search_device(self.h, C.c_void_p(d_queries_ptr), nq, L, K, C.c_void_p(d_seeds_ptr),
+                                            C.c_void_p(d_out_ptr), C.c_void_p(d_dist_ptr or None),
+                                            C.byref(cnt) if counters else None))
+        return (int(cnt.dist_count), int(cnt.hop_count)) if counters else None
