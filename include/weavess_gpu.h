@@ -67,6 +67,40 @@ int wv_upload_base(wv_ctx *ctx, const float *base, uint32_t n, uint32_t d);
 int wv_upload_graph(wv_ctx *ctx, const uint32_t *ids, const uint32_t *deg, uint32_t n, uint32_t width,
                     uint32_t ep);
 
+/* ---- build ------------------------------------------------------------- */
+typedef struct {
+  unsigned long long rand_draws; /* values taken from the rand stream */
+  unsigned long long offers;     /* join offers that reached the per-node merge */
+  unsigned long long pairs;      /* local-join distance evaluations */
+  unsigned chunks;               /* join chunks over all iterations */
+  float ms_join, ms_update, ms_total;
+} wv_build_stats;
+
+/* The graph the build components hand to each other (final_graph_ of the
+ * reference's Index, include/weavess/index.h:1658): fixed-width rows of ids
+ * and distances, deg[n] entries each.  Set it from the host, or read back the
+ * result of the last build step.  out arrays are n x width (width >= the
+ * current row width, see wv_graph_width). */
+int wv_set_graph(wv_ctx *ctx, const uint32_t *ids, const float *dist, const uint32_t *deg, uint32_t n,
+                 uint32_t width, uint32_t ep);
+int wv_graph_width(wv_ctx *ctx, uint32_t *width, uint32_t *ep);
+int wv_get_graph(wv_ctx *ctx, uint32_t *ids, float *dist, uint32_t *deg, uint32_t width);
+/* IndexBuilder::save_graph + load_graph (builder.cpp:918-1311) without the
+ * host round trip: the current build graph becomes the search graph. */
+int wv_load_built_graph(wv_ctx *ctx);
+
+/* ComponentInitRandom::InitInner (component_init.cpp:11-45): S random
+ * neighbours per node from one mt19937 seeded by one rand() draw, sorted by
+ * distance.  Result: the current graph (width S). */
+int wv_init_random(wv_ctx *ctx, uint32_t S, wv_build_stats *stats);
+
+/* ComponentRefineNNDescent::RefineInner (component_refine.cpp:12-239) on the
+ * current graph: ITER rounds of join + update with pool size L, sample S,
+ * reverse cap R, then sorted rows truncated to K (PruneNaive).  Result: the
+ * current graph (width K). */
+int wv_nnd_refine(wv_ctx *ctx, uint32_t S, uint32_t K, uint32_t L, uint32_t ITER, uint32_t R,
+                  wv_build_stats *stats);
+
 /* ---- search ------------------------------------------------------------- */
 /* Replaces the query loop of IndexBuilder::search with L_SEARCH_ASSIGN
  * (builder.cpp:430-454): SearchEntryInner (entry) + ComponentSearchRouteGreedy

@@ -30,6 +30,14 @@ class Counters(C.Structure):
     _fields_ = [("dist_count", C.c_ulonglong), ("hop_count", C.c_ulonglong)]
 
 
+class BuildStats(C.Structure):
+    _fields_ = [("rand_draws", C.c_ulonglong), ("offers", C.c_ulonglong), ("pairs", C.c_ulonglong),
+                ("chunks", C.c_uint), ("ms_join", C.c_float), ("ms_update", C.c_float), ("ms_total", C.c_float)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 def declared_functions():
     """Names of every function the C header declares."""
     txt = open(HEADER).read()
@@ -62,5 +70,12 @@ def load(build_if_needed: bool = True):
                                   C.POINTER(Counters)]
     L.wv_search_device.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp, vp, C.POINTER(Counters)]
     L.wv_draw_seeds.argtypes = [vp, C.c_uint32, C.c_int, C.c_uint32, u32p]
+    L.wv_set_graph.argtypes = [vp, u32p, vp, u32p, C.c_uint32, C.c_uint32, C.c_uint32]
+    L.wv_graph_width.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+    L.wv_get_graph.argtypes = [vp, vp, vp, vp, C.c_uint32]
+    L.wv_load_built_graph.argtypes = [vp]
+    L.wv_init_random.argtypes = [vp, C.c_uint32, C.POINTER(BuildStats)]
+    L.wv_nnd_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                C.POINTER(BuildStats)]
     _lib = L
     return L

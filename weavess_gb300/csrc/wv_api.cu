@@ -148,8 +148,10 @@ int wv_ctx_destroy(wv_ctx *c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   for (DevBuf *b : {&c->base, &c->gids, &c->gdeg, &c->visited, &c->touched, &c->misc, &c->q_buf, &c->seed_buf,
-                    &c->out_ids_buf, &c->out_dist_buf, &c->lq_buf, &c->kq_buf})
+                    &c->out_ids_buf, &c->out_dist_buf, &c->lq_buf, &c->kq_buf, &c->fg_ids, &c->fg_dist,
+                    &c->fg_deg})
     b->release();
+  c->release_work();
   cudaStreamDestroy(c->stream);
   delete c;
   return WV_OK;

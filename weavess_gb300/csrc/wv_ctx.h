@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -64,9 +65,28 @@ struct wv_ctx {
   // per-call staging
   wv::DevBuf q_buf, seed_buf, out_ids_buf, out_dist_buf, lq_buf, kq_buf;
 
+  // the graph the build components pass along (final_graph_): fixed-width
+  // rows of (id, distance) with a degree per node, plus the entry point
+  wv::DevBuf fg_ids, fg_dist, fg_deg;
+  uint32_t fg_n = 0, fg_w = 0, fg_ep = 0;
+  bool fg_has_ep = false;
+
+  // named grow-only work buffers of the build kernels
+  std::map<std::string, wv::DevBuf> work;
+  template <class T>
+  T *buf(const char *name, size_t count, cudaError_t *err) {
+    cudaError_t e = work[name].ensure(count * sizeof(T) + 16);
+    if (e != cudaSuccess && err) *err = e;
+    return work[name].as<T>();
+  }
+
   unsigned *d_next() { return misc.as<unsigned>(); }
   unsigned long long *d_counters() { return reinterpret_cast<unsigned long long *>(misc.as<char>() + 8); }
   int *d_status() { return reinterpret_cast<int *>(misc.as<char>() + 32); }
+  void release_work() {
+    for (auto &kv : work) kv.second.release();
+    work.clear();
+  }
 };
 
 namespace wv {

@@ -67,6 +67,36 @@ class Context:
         ids = _u32(ids)
         self._check(self.L.wv_upload_graph(self.h, ids, _u32(deg), ids.shape[0], ids.shape[1], int(ep or 0)))
 
+    # -- build graph (final_graph_)
+    def set_graph(self, ids, deg, dist=None, ep=0):
+        ids = _u32(ids)
+        d = None if dist is None else _f32(dist)
+        self._check(self.L.wv_set_graph(self.h, ids, None if d is None else d.ctypes.data, _u32(deg), ids.shape[0],
+                                        ids.shape[1], int(ep or 0)))
+
+    def get_graph(self):
+        """(ids [n, w], dist [n, w], deg [n], ep) of the current build graph."""
+        w, ep = C.c_uint32(), C.c_uint32()
+        self._check(self.L.wv_graph_width(self.h, C.byref(w), C.byref(ep)))
+        ids = np.zeros((self.n, w.value), np.uint32)
+        dist = np.zeros((self.n, w.value), np.float32)
+        deg = np.zeros(self.n, np.uint32)
+        self._check(self.L.wv_get_graph(self.h, ids.ctypes.data, dist.ctypes.data, deg.ctypes.data, w.value))
+        return ids, dist, deg, int(ep.value)
+
+    def load_built_graph(self):
+        self._check(self.L.wv_load_built_graph(self.h))
+
+    def init_random(self, S: int):
+        st = _lib.BuildStats()
+        self._check(self.L.wv_init_random(self.h, S, C.byref(st)))
+        return st.as_dict()
+
+    def nnd_refine(self, S: int, K: int, L: int, ITER: int, R: int):
+        st = _lib.BuildStats()
+        self._check(self.L.wv_nnd_refine(self.h, S, K, L, ITER, R, C.byref(st)))
+        return st.as_dict()
+
     # -- search (IndexBuilder::search, L_SEARCH_ASSIGN)
     def search(self, queries, L: int, K: int = 10, entry="rand", return_dist=False):
         q = _f32(queries)
