@@ -1,0 +1,315 @@
+"""Benchmark of the WEAVESS hot path on one GB300.
+
+Workload (default): N=1,000,000 base vectors, d=128, integer-valued Gaussian
+mixture (256 centres uniform in [0,255], sigma 20, rounded, clipped), 10,000
+queries from the same mixture (seeded synthetic stand-in for the 1M x 128
+configuration).  Build: INIT_RANDOM (S=20) -> NN-Descent (K=64, L=80, ITER=8,
+R=100) -> Vamana link (alpha=1.2, R=32, L_refine=64) when available.  Search:
+SEARCH_ENTRY_RAND + ROUTER_GREEDY, top-10, at the smallest beam width L that
+reaches recall@10 >= 0.95 against FP64 brute-force ground truth.
+
+One step = one search of all 10,000 queries.  `value` is QPS with queries and
+seeds resident in HBM (device-timed with CUDA events, L2 flushed between
+steps); `e2e` is QPS through the public C-ABI call with host buffers (seed
+draws, H2D of queries + seeds, D2H of the result ids inside the timed
+region).  `--impl reference` times the CPU implementation of the same path
+(the oracle restatement of the reference, OpenMP over queries) on the host.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from weavess_gb300 import datasets as ds  # noqa: E402
+
+CFG = dict(n=1_000_000, d=128, centers=256, nq=10_000, seed=7, S=20, K=64, L=80, ITER=8, R=100,
+           alpha=1.2, R_refine=32, L_refine=64, k=10, target_recall=0.95,
+           L_grid=[10, 16, 20, 24, 32, 40, 48, 64, 80, 96, 128, 160, 192, 224, 256, 300])
+METRIC = "QPS at recall@10>=0.95 (plain FP32 greedy search, 1M x 128)"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+class Clocks:
+    """nvidia-smi samples while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.rows, self.proc = [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def make_data(cfg):
+    t = time.time()
+    base, query = ds.int_mixture(cfg["n"], cfg["d"], cfg["centers"], seed=cfg["seed"], n_query=cfg["nq"])
+    log(f"data {base.shape} {query.shape} in {time.time() - t:.1f}s")
+    return base, query
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def recall(res, gt, k=10):
+    g = gt[:, :k]
+    hit = (res[:, :k, None] == g[:, None, :]).any(2).sum()
+    return float(hit) / (res.shape[0] * k)
+
+
+def build_index(ctx, base, cfg):
+    """GPU build; returns build seconds and per-stage stats."""
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.time()
+    ctx.upload_base(base)
+    ctx.srand(1)
+    st0 = ctx.init_random(cfg["S"])
+    st1 = ctx.nnd_refine(cfg["S"], cfg["K"], cfg["L"], cfg["ITER"], cfg["R"])
+    stages = {"init_random": st0, "nndescent": st1}
+    if hasattr(ctx, "vamana_refine"):
+        stages["vamana"] = ctx.vamana_refine(cfg["L_refine"], cfg["R_refine"], cfg["alpha"])
+    ctx.load_built_graph()
+    torch.cuda.synchronize()
+    return time.time() - t0, stages
+
+
+def cpu_search_qps(base, query, g_ids, g_deg, L, threads, sample):
+    """The oracle restatement (OpenMP over queries) on the host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    g = O.Graph(g_ids, np.zeros(g_ids.shape, np.float32), g_deg, 0)
+    q = query[:sample]
+    O.search(base, q[:8], g, L, O.Rand(1), threads=threads)  # warm
+    t = time.perf_counter()
+    res, dc, hc = O.search(base, q, g, L, O.Rand(1), threads=threads)
+    dt = time.perf_counter() - t
+    return sample / dt, dt, res
+
+
+def run_ours(args):
+    import torch
+    from weavess_gb300 import Context
+    from weavess_gb300.groundtruth import knn_fp64
+    cfg = dict(CFG)
+    if args.small:
+        cfg.update(n=100_000, centers=64, nq=1000, S=10, K=20, L=40, ITER=8, R=100, R_refine=32)
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    base, query = make_data(cfg)
+    ctx = Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    build_s, stages = build_index(ctx, base, cfg)
+    log(f"build {build_s:.2f}s {stages}")
+    t = time.time()
+    gt = knn_fp64(base, query, 100)
+    log(f"ground truth {time.time() - t:.1f}s")
+    # ---- calibration: smallest L with recall >= target (untimed)
+    sweep = {}
+    Lsel = None
+    for L in cfg["L_grid"]:
+        ctx.srand(12345)
+        res, dc, hc = ctx.search(query, L, cfg["k"], entry="rand")
+        r = recall(res, gt, cfg["k"])
+        sweep[L] = round(r, 4)
+        log(f"L={L} recall={r:.4f}")
+        if r >= cfg["target_recall"]:
+            Lsel = L
+            break
+    if Lsel is None:
+        Lsel = cfg["L_grid"][-1]
+    nq, d, K = query.shape[0], cfg["d"], cfg["k"]
+    # ---- device-resident timed steps
+    ctx.srand(777)
+    seeds = ctx.draw_seeds(nq, Lsel, "rand")
+    dq = torch.from_numpy(query).to(dev)
+    ds_ = torch.from_numpy(seeds.astype(np.int32)).to(dev)
+    dout = torch.empty((nq, K), dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # 256 MB > 129 MB L2
+    counters = None
+    for _ in range(args.warmup):
+        counters = ctx.search_device(dq.data_ptr(), nq, Lsel, K, ds_.data_ptr(), dout.data_ptr(), counters=True)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with Clocks() as clk:
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            ctx.search_device(dq.data_ptr(), nq, Lsel, K, ds_.data_ptr(), dout.data_ptr())
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = float(np.mean(step_ms))
+    value = nq / (ms / 1e3)
+    res_dev = dout.cpu().numpy().astype(np.uint32)
+    r_dev = recall(res_dev, gt, K)
+    # ---- roofline of the search kernel (algorithmic bytes per launch)
+    dc, hc = counters
+    g_ids, _, g_deg, _ = ctx.get_graph()
+    avg_deg = float(g_deg.mean())
+    alg_bytes = dc * d * 4 + hc * (avg_deg * 4 + 4) + nq * d * 4
+    hbm, peak_kind = peaks()
+    achieved = alg_bytes / (ms / 1e3) / 1e9
+    # ---- e2e through the public call (host buffers, pinned)
+    qpin = torch.from_numpy(query).pin_memory().numpy()
+    ctx.srand(777)
+    for _ in range(max(1, args.warmup // 2)):
+        ctx.search(qpin, Lsel, K, entry="rand")
+    torch.cuda.synchronize()
+    e2e_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        out, _, _ = ctx.search(qpin, Lsel, K, entry="rand")
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_qps = nq / float(np.mean(e2e_t))
+    # ---- CPU baseline: the oracle on the host cores, bounded sample
+    threads = os.cpu_count() or 1
+    sample = 2000 if not args.small else 1000
+    cpu_qps, cpu_dt, _ = cpu_search_qps(base, query, g_ids, g_deg, Lsel, threads, sample)
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded integer Gaussian mixture)",
+        "config": {"workload": f"{cfg['n']}x{cfg['d']} int-mixture({cfg['centers']}), {nq} queries, top-{K}, "
+                               f"KGraph NN-Descent S={cfg['S']} K={cfg['K']} L={cfg['L']} ITER={cfg['ITER']} "
+                               f"R={cfg['R']}" + (" + Vamana" if "vamana" in stages else ""),
+                   "entry": "SEARCH_ENTRY_RAND", "L_search": Lsel, "recall@10": round(r_dev, 4),
+                   "recall_sweep": sweep, "l2": "flushed (256 MB write) between steps; base 512 MB > L2",
+                   "build_s": round(build_s, 3),
+                   "build_stages": {k: {kk: (round(vv, 2) if isinstance(vv, float) else vv) for kk, vv in v.items()}
+                                    for k, v in stages.items()}},
+        "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": nq * d * 4 + nq * Lsel * 4,
+                "d2h_bytes_per_step": nq * K * 4},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
+                     "alg_bytes_per_launch": int(alg_bytes), "dist_count": dc, "hop_count": hc},
+        "cpu_baseline": {"value": round(cpu_qps, 1), "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": f"first {sample} queries, same graph and L, oracle OpenMP search "
+                                   f"({cpu_dt:.2f}s)"},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_reference(args):
+    """CPU implementation of the path (oracle port of the reference, OpenMP)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    cfg = dict(CFG)
+    if args.small:
+        cfg.update(n=100_000, centers=64, nq=1000, S=10, K=20, L=40, ITER=8, R=100)
+    threads = os.cpu_count() or 1
+    # a bounded sample of the workload: the first n_s base vectors, built and
+    # searched by the CPU path with every host thread
+    n_s = min(cfg["n"], 100_000)
+    base, query = ds.int_mixture(n_s, cfg["d"], max(8, cfg["centers"] * n_s // cfg["n"]), seed=cfg["seed"],
+                                 n_query=1000)
+    t = time.time()
+    r = O.Rand(1)
+    g = O.init_random(base, cfg["S"], r)
+    g = O.nndescent(base, g, cfg["S"], cfg["K"], cfg["L"], cfg["ITER"], cfg["R"], r, threads=threads)
+    build_s = time.time() - t
+    gt = ds.groundtruth_fp64(base, query, 10)
+    Lsel = cfg["L_grid"][-1]
+    for L in cfg["L_grid"]:
+        res, _, _ = O.search(base, query, g, L, O.Rand(5), threads=threads)
+        if recall(res, gt) >= cfg["target_recall"]:
+            Lsel = L
+            break
+    for _ in range(args.warmup):
+        O.search(base, query, g, Lsel, O.Rand(5), threads=threads)
+    ts = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        O.search(base, query, g, Lsel, O.Rand(5), threads=threads)
+        ts.append(time.perf_counter() - t)
+    qps = query.shape[0] / float(np.mean(ts))
+    line = {"impl": "reference", "metric": METRIC, "value": round(qps, 1), "unit": "queries/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(float(np.mean(ts)) * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded integer Gaussian mixture)",
+            "config": {"workload": f"CPU sample: {n_s}x{cfg['d']} of the same mixture, 1000 queries",
+                       "L_search": Lsel, "build_s": round(build_s, 2)},
+            "cpu_baseline": {"value": round(qps, 1), "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": f"{n_s} base vectors, 1000 queries, same build parameters"},
+            "e2e": {"value": round(qps, 1), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="N=1e5 configuration (quick check)")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    if args.gpus > 1:
+        # search shards by query; this build measures one GPU (replicas only)
+        if rank != 0:
+            return
+    run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

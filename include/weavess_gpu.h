@@ -57,6 +57,9 @@ int wv_srand(wv_ctx *ctx, unsigned seed);
 int wv_set_rand_source(wv_ctx *ctx, int (*fn)(void));
 /* next value of the context's rand stream (for callers that interleave) */
 int wv_rand(wv_ctx *ctx, int *out);
+/* run the context's work on `stream` (a cudaStream_t of the same device);
+ * NULL restores the context's own stream */
+int wv_set_stream(wv_ctx *ctx, void *stream);
 
 /* ---- data --------------------------------------------------------------- */
 /* Replaces the base arrays ComponentLoad::LoadInner hands to the index

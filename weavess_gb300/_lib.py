@@ -62,6 +62,7 @@ def load(build_if_needed: bool = True):
     L.wv_srand.argtypes = [vp, C.c_uint]
     L.wv_set_rand_source.argtypes = [vp, vp]
     L.wv_rand.argtypes = [vp, C.POINTER(C.c_int)]
+    L.wv_set_stream.argtypes = [vp, vp]
     L.wv_upload_base.argtypes = [vp, f32p, C.c_uint32, C.c_uint32]
     L.wv_upload_graph.argtypes = [vp, u32p, u32p, C.c_uint32, C.c_uint32, C.c_uint32]
     L.wv_search.argtypes = [vp, f32p, C.c_uint32, C.c_int, C.c_uint32, C.c_uint32, vp, u32p, vp,

@@ -132,6 +132,7 @@ int wv_ctx_create(wv_ctx **out, int device) {
     delete c;
     return WV_ERR_CUDA;
   }
+  c->own_stream = c->stream;
   cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
   if (c->misc.ensure(64) != cudaSuccess) {
     cudaStreamDestroy(c->stream);
@@ -152,7 +153,7 @@ int wv_ctx_destroy(wv_ctx *c) {
                     &c->fg_deg})
     b->release();
   c->release_work();
-  cudaStreamDestroy(c->stream);
+  cudaStreamDestroy(c->own_stream);
   delete c;
   return WV_OK;
 }
@@ -168,6 +169,13 @@ int wv_srand(wv_ctx *c, unsigned seed) {
 int wv_set_rand_source(wv_ctx *c, int (*fn)(void)) {
   if (!c) return WV_ERR_ARG;
   c->rnd.fn = fn;
+  return WV_OK;
+}
+
+int wv_set_stream(wv_ctx *c, void *stream) {
+  if (!c) return WV_ERR_ARG;
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
   return WV_OK;
 }
 

@@ -43,7 +43,8 @@ struct DevBuf {
 
 struct wv_ctx {
   int device = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;      // the stream all work is issued on
+  cudaStream_t own_stream = nullptr;  // the context's own stream
   std::string err;
   wv::RandSource rnd;
   int sms = 0;

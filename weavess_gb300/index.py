@@ -48,6 +48,10 @@ class Context:
         except Exception:
             pass
 
+    def set_stream(self, stream_ptr: int = 0):
+        """Issue all work on this CUDA stream (e.g. torch.cuda.current_stream().cuda_stream)."""
+        self._check(self.L.wv_set_stream(self.h, C.c_void_p(stream_ptr or None)))
+
     # -- rand stream
     def srand(self, seed: int):
         self._check(self.L.wv_srand(self.h, seed))
