@@ -128,6 +128,13 @@ int wv_search_device(wv_ctx *ctx, const float *d_queries, uint32_t nq, uint32_t 
  * consuming the context's rand stream exactly as the reference does. */
 int wv_draw_seeds(wv_ctx *ctx, uint32_t nq, int entry, uint32_t L, uint32_t *seeds);
 
+/* ---- diagnostics -------------------------------------------------------- */
+/* Sorts narr arrays of (key, value) pairs, array i being
+ * [offsets[i], offsets[i+1]), with the device replica of std::sort (mode 0:
+ * warp-parallel, mode 1: one thread), in place, so a test can compare the
+ * order of tied keys with the host's std::sort.  Arrays of up to 4096. */
+int wv_debug_sort(wv_ctx *ctx, float *keys, uint32_t *vals, const uint32_t *offsets, uint32_t narr, int mode);
+
 #ifdef __cplusplus
 }
 #endif

@@ -78,5 +78,6 @@ def load(build_if_needed: bool = True):
     L.wv_init_random.argtypes = [vp, C.c_uint32, C.POINTER(BuildStats)]
     L.wv_nnd_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                 C.POINTER(BuildStats)]
+    L.wv_debug_sort.argtypes = [vp, f32p, u32p, u32p, C.c_uint32, C.c_int]
     _lib = L
     return L

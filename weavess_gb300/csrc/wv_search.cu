@@ -23,6 +23,7 @@
 //    are not marked, as in the reference.
 #include <cstdio>
 
+#include "warp_sort.cuh"
 #include "wv_common.cuh"
 #include "wv_search.h"
 
@@ -106,7 +107,10 @@ __device__ inline int lower_bound_f(const float *a, int n, float x) {
 }
 
 // Orders the L seeds (pa_*, in drawn order) into pb_* exactly as std::sort
-// would, flags set.  Uses stage as scratch.
+// would, flags set.  A bitonic sort on (dist, seed position) gives the stable
+// order, which is std::sort's whenever L <= 16 or no two seed distances tie;
+// otherwise the warp replays libstdc++'s introsort (warp_sort.cuh).  Uses
+// stage as scratch.
 __device__ void sort_seeds(WarpSmem &s, int L, int lane) {
   int P = 1;
   while (P < L) P <<= 1;
@@ -148,22 +152,34 @@ __device__ void sort_seeds(WarpSmem &s, int L, int lane) {
       s.pb_i[i] = s.pa_i[x] | FLAG;
     }
   } else {
-    // ties and L > 16: replay libstdc++ introsort on the drawn order
-    DI *tmp = reinterpret_cast<DI *>(s.stage);
+    // ties and L > 16: replay libstdc++ introsort on the drawn order.  The
+    // pairs sort in the B pool region (2 x (Lmax+1) words), the partition
+    // scratch sits in stage; the result goes through stage into B.
     __syncwarp();
+    DI *tmp = reinterpret_cast<DI *>(s.pb_d);
     for (int i = lane; i < L; i += 32) tmp[i] = DI{s.pa_d[i], s.pa_i[i]};
+    int *scr = reinterpret_cast<int *>(s.stage);
     __syncwarp();
-    if (lane == 0) stl::sort(tmp, L, DILess());
+    warp_std_sort(tmp, L, DILess(), WarpSortScratch{scr, scr + L, scr + 2 * L, scr + 2 * L + 192}, lane);
+    DI *out = reinterpret_cast<DI *>(s.stage);
+    for (int i = lane; i < L; i += 32) out[i] = tmp[i];
     __syncwarp();
     for (int i = lane; i < L; i += 32) {
-      s.pb_d[i] = tmp[i].d;
-      s.pb_i[i] = tmp[i].i | FLAG;
+      s.pb_d[i] = out[i].d;
+      s.pb_i[i] = out[i].i | FLAG;
     }
   }
   __syncwarp();
 }
 
-__global__ void __launch_bounds__(WARPS * 32) k_search_exact(SearchArgs a) {
+// BUILD = false: SearchEntry* + ROUTER_GREEDY (seeds not marked visited,
+//   DistCount / HopCount kept, top-K written).
+// BUILD = true: CandidateNSG::CandidateInner (component_candidate.cpp:10-85)
+//   for base points: seeds are marked visited, and every visited (id, dist)
+//   -- the seeds in drawn order, then each newly visited id in visit order --
+//   is appended to the query's visit list (vis, vcap entries, count in vcnt).
+template <bool BUILD>
+__global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t wbytes = warp_smem_bytes(a.d, a.Lmax, a.cap);
@@ -184,6 +200,9 @@ __global__ void __launch_bounds__(WARPS * 32) k_search_exact(SearchArgs a) {
     for (uint32_t i = lane; i < a.d; i += 32) s.qv[i] = qsrc[i];
     // ---- seeds (SearchEntryInner): distances in drawn order ----
     const uint32_t *seeds = a.seeds + (size_t)q * a.seed_stride;
+    uint32_t ntouch = 0;
+    uint32_t nvis = 0;
+    DI *vis_out = BUILD ? a.vis + (size_t)q * a.vcap : nullptr;
     __syncwarp();
     for (int b = 0; b < L; b += 32) {
       int cnt = min(32, L - b);
@@ -192,11 +211,24 @@ __global__ void __launch_bounds__(WARPS * 32) k_search_exact(SearchArgs a) {
         set_err(a.status, DEV_BAD_ID);
         id = 0;
       }
+      if (BUILD) {
+        // CandidateNSG flags its seeds (component_candidate.cpp:21-29)
+        bool newword = false;
+        if (lane < cnt) {
+          const uint32_t bit = 1u << (id & 31);
+          newword = atomicOr(vis + (id >> 5), bit) == 0;
+        }
+        const unsigned nwm = __ballot_sync(FULL, newword);
+        if (newword) touched[ntouch + __popc(nwm & ((1u << lane) - 1u))] = id >> 5;
+        ntouch += __popc(nwm);
+      }
       float dist = warp_l2_rows(a.base, a.d, id, cnt, s.qv, s.stage, lane);
       if (lane < cnt) {
         s.pa_d[b + lane] = dist;
         s.pa_i[b + lane] = id;
+        if (BUILD && nvis + lane < a.vcap) vis_out[nvis + lane] = DI{dist, id};
       }
+      nvis += cnt;
     }
     dcount += L;
     __syncwarp();
@@ -205,7 +237,6 @@ __global__ void __launch_bounds__(WARPS * 32) k_search_exact(SearchArgs a) {
     uint32_t *pi = s.pb_i, *oi = s.pa_i;
 
     // ---- route (RouteInner) ----
-    uint32_t ntouch = 0;
     int k = first_flag(pi, 0, L, lane);
     while (k < L) {
       const uint32_t node = pi[k] & ID_MASK;
@@ -254,6 +285,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_search_exact(SearchArgs a) {
         __syncwarp();
         float dist = warp_l2_rows(a.base, a.d, my, cnt, s.qv, s.stage, lane);
         dcount += cnt;
+        if (BUILD) {
+          if (lane < cnt && nvis + lane < a.vcap) vis_out[nvis + lane] = DI{dist, my};
+          nvis += cnt;
+        }
         bool acc = false;
         if (lane < cnt && dist < thr) {
           // reject an id already in the pool (an unvisited seed): same id
@@ -327,16 +362,28 @@ __global__ void __launch_bounds__(WARPS * 32) k_search_exact(SearchArgs a) {
       k = first_flag(pi, next, L, lane);
     }
     // ---- results ----
-    for (int i = lane; i < K; i += 32) {
-      a.out_ids[(size_t)q * a.out_stride + i] = pi[i] & ID_MASK;
-      if (a.out_dist) a.out_dist[(size_t)q * a.out_stride + i] = pd[i];
+    if (BUILD) {
+      if (lane == 0) {
+        a.vcnt[q] = nvis;
+        if (nvis > a.vcap) set_err(a.status, DEV_OVERFLOW);
+      }
+      if (a.out_ids)
+        for (int i = lane; i < K; i += 32) {
+          a.out_ids[(size_t)q * a.out_stride + i] = pi[i] & ID_MASK;
+          if (a.out_dist) a.out_dist[(size_t)q * a.out_stride + i] = pd[i];
+        }
+    } else {
+      for (int i = lane; i < K; i += 32) {
+        a.out_ids[(size_t)q * a.out_stride + i] = pi[i] & ID_MASK;
+        if (a.out_dist) a.out_dist[(size_t)q * a.out_stride + i] = pd[i];
+      }
     }
     // clear this query's visited words for the warp's next query
     __syncwarp();
     for (uint32_t i = lane; i < ntouch; i += 32) vis[touched[i]] = 0u;
     __syncwarp();
   }
-  if (lane == 0 && a.counters) {
+  if (!BUILD && lane == 0 && a.counters) {
     atomicAdd(a.counters + 0, dcount);
     atomicAdd(a.counters + 1, hcount);
   }
@@ -354,10 +401,11 @@ int search_warps_per_block() { return WARPS; }
 
 int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device) {
   size_t smem = search_block_smem(d, Lmax, cap);
-  if (cudaFuncSetAttribute(k_search_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_search<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+      cudaFuncSetAttribute(k_search<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return 0;
   int per_sm = 0, sms = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_exact, WARPS * 32, smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<true>, WARPS * 32, smem) != cudaSuccess)
     return 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
   return per_sm * sms;
@@ -365,7 +413,8 @@ int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device) {
 
 cudaError_t launch_search_exact(const SearchArgs &a, int blocks, cudaStream_t stream) {
   size_t smem = search_block_smem(a.d, a.Lmax, a.cap);
-  k_search_exact<<<blocks, WARPS * 32, smem, stream>>>(a);
+  if (a.vis) k_search<true><<<blocks, WARPS * 32, smem, stream>>>(a);
+  else k_search<false><<<blocks, WARPS * 32, smem, stream>>>(a);
   return cudaGetLastError();
 }
 

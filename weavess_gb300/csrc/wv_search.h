@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "wv_common.cuh"
+
 namespace wv {
 
 struct SearchArgs {
@@ -29,10 +31,14 @@ struct SearchArgs {
   uint32_t cap;  // candidate buffer entries per warp (graph width + 32)
   unsigned *next_query;
   int *status;
+  // candidate-search (build) mode: visit lists, vcap entries per query
+  ::wv::DI *vis;
+  uint32_t *vcnt;
+  uint32_t vcap;
 };
 
 constexpr uint32_t SEARCH_MAX_WIDTH = 256;  // graph row width the kernel accepts
-constexpr uint32_t SEARCH_MAX_L = 2048;
+constexpr uint32_t SEARCH_MAX_L = 1536;  // exact seed sort scratch: 2L + 256 words of stage
 
 // bytes of dynamic shared memory per block and warps per block
 size_t search_block_smem(uint32_t d, uint32_t Lmax, uint32_t cap);
