@@ -128,6 +128,26 @@ int wv_search_device(wv_ctx *ctx, const float *d_queries, uint32_t nq, uint32_t 
  * consuming the context's rand stream exactly as the reference does. */
 int wv_draw_seeds(wv_ctx *ctx, uint32_t nq, int entry, uint32_t L, uint32_t *seeds);
 
+/* ---- allocation-free search ---------------------------------------------- */
+/* No counterpart in the reference: an extra entry point for callers that
+ * cannot call cudaMalloc -- a process whose GPU memory belongs to another
+ * allocator that forbids driver allocations once it is running, or a
+ * latency-critical thread where cudaMalloc / cudaFree would synchronize the
+ * device.  It runs the same greedy search as wv_search_device with every
+ * input and output in caller-owned device memory (base n x d, graph rows
+ * n x width with degrees, queries nq x d, seeds nq x L, out_ids nq x K,
+ * out_dist nq x K or NULL) on `stream` (a cudaStream_t, NULL = default).
+ * It needs no context and allocates nothing: its working memory is a fixed
+ * 64 MiB device array inside this library, shared by every call, so calls
+ * that overlap on the GPU race on it.  The first call on a device looks that
+ * array up (make it before any stream capture).  Returns WV_ERR_LIMIT when n
+ * is too large for the fixed array (about 130 million nodes) or L / width
+ * exceed the search limits, WV_ERR_DEVICE if the kernel saw an id >= n. */
+int wv_search_noalloc(const float *d_base, uint32_t n, uint32_t d, const uint32_t *d_graph_ids,
+                      const uint32_t *d_graph_deg, uint32_t width, const float *d_queries, uint32_t nq,
+                      const uint32_t *d_seeds, uint32_t L, uint32_t K, uint32_t *d_out_ids, float *d_out_dist,
+                      void *stream);
+
 /* ---- diagnostics -------------------------------------------------------- */
 /* Sorts narr arrays of (key, value) pairs, array i being
  * [offsets[i], offsets[i+1]), with the device replica of std::sort (mode 0:

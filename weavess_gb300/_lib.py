@@ -79,5 +79,7 @@ def load(build_if_needed: bool = True):
     L.wv_nnd_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                 C.POINTER(BuildStats)]
     L.wv_debug_sort.argtypes = [vp, f32p, u32p, u32p, C.c_uint32, C.c_int]
+    L.wv_search_noalloc.argtypes = [vp, C.c_uint32, C.c_uint32, vp, vp, C.c_uint32, vp, C.c_uint32, vp, C.c_uint32,
+                                    C.c_uint32, vp, vp, vp]
     _lib = L
     return L
