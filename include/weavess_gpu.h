@@ -77,6 +77,9 @@ typedef struct {
   unsigned long long pairs;      /* local-join distance evaluations */
   unsigned chunks;               /* join chunks over all iterations */
   float ms_join, ms_update, ms_total;
+  unsigned levels;               /* InterInsert dependency levels (link) */
+  unsigned ep;                   /* entry point chosen (link) */
+  unsigned conn_added;           /* edges added by the NSG connectivity pass */
 } wv_build_stats;
 
 /* The graph the build components hand to each other (final_graph_ of the
@@ -103,6 +106,24 @@ int wv_init_random(wv_ctx *ctx, uint32_t S, wv_build_stats *stats);
  * current graph (width K). */
 int wv_nnd_refine(wv_ctx *ctx, uint32_t S, uint32_t K, uint32_t L, uint32_t ITER, uint32_t R,
                   wv_build_stats *stats);
+
+/* ComponentRefineVAMANA::RefineInner (component_refine.cpp:794-950) on the
+ * current graph: entry point (ComponentRefineEntryCentroid), a greedy
+ * candidate search of L_refine per node (ComponentCandidateNSG), the alpha
+ * prune to R_refine (ComponentPruneVAMANA) and InterInsert.  entry_L is the
+ * index's L_refine member the entry search reads: the Vamana refine never
+ * sets it, so in a NN-Descent -> Vamana pipeline it is 0 and the entry point
+ * is node 0.  The reference sets alpha = 2 after a link; pass alpha for each
+ * call.  Result: the current graph (width R_refine) with its entry point. */
+int wv_vamana_refine(wv_ctx *ctx, uint32_t L_refine, uint32_t R_refine, float alpha, uint32_t entry_L,
+                     wv_build_stats *stats);
+
+/* ComponentRefineNSG::RefineInner (component_refine.cpp:393-541) on the
+ * current graph: centroid entry point with L_refine, candidate search, the
+ * RNG prune (ComponentPruneNSG, C_refine candidates), InterInsert, then
+ * ComponentConnNSGDFS.  Result: the current graph (rows may exceed R_refine
+ * after the connectivity pass) with its entry point. */
+int wv_nsg_refine(wv_ctx *ctx, uint32_t L_refine, uint32_t R_refine, uint32_t C_refine, wv_build_stats *stats);
 
 /* ---- search ------------------------------------------------------------- */
 /* Replaces the query loop of IndexBuilder::search with L_SEARCH_ASSIGN

@@ -1,0 +1,113 @@
+"""GPU Vamana / NSG link (candidate search, prune, InterInsert, entry point,
+connectivity) against the reference: every row, the entry point and the
+searches that follow must be identical."""
+import numpy as np
+import pytest
+
+import oracle as O
+from golden_util import cases, load, graph_of, rows_equal
+from weavess_gb300 import datasets as ds
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from weavess_gb300 import Context
+    return Context(0)
+
+
+def _replay(ctx, f, pi):
+    """Runs pipeline pi of a golden case on the GPU; checks every graph and
+    search step against the reference's dumps."""
+    p = f["params"]
+    base, query = f["base"], f["query"]
+    steps = f["pipelines"][pi]
+    ctx.upload_base(base)
+    ctx.srand(1)
+    alpha = p["alpha"]
+    entry_L = 0
+    vam = 0
+    checked = []
+    for s in steps:
+        kind, _, arg = s.partition(":")
+        key = f"p{pi}."
+        if kind == "init_random":
+            ctx.init_random(p["S"])
+            exp = key + "init"
+        elif kind == "nndescent":
+            ctx.nnd_refine(p["S"], p["K"], p["L"], p["ITER"], p["R"])
+            exp = key + "nnd"
+        elif kind == "vamana":
+            vam += 1
+            ctx.vamana_refine(p["L_refine"], p["R_refine"], alpha, entry_L)
+            alpha = 2.0
+            exp = key + ("vamana" if vam == steps.count("vamana") else f"vamana{vam}")
+        elif kind == "nsg":
+            ctx.nsg_refine(p["L_refine"], p["R_refine"], p["C_refine"])
+            entry_L = p["L_refine"]
+            exp = key + "nsg"
+        elif kind == "load":
+            ctx.load_built_graph()
+            continue
+        else:
+            entry = "rand" if kind == "search_rand" else "centroid"
+            res, dc, hc = ctx.search(query, int(arg), 10, entry=entry)
+            k = f"{key}{kind}_{arg}"
+            assert np.array_equal(res, f[k + ".res"]), s
+            assert [dc, hc] == f[k + ".counts"].tolist(), s
+            checked.append(s)
+            continue
+        ids, dist, deg, ep = ctx.get_graph()
+        e = graph_of(f, exp)
+        assert rows_equal(ids, dist, deg, *e[:3]) == 0, s
+        if e[3] is not None:
+            assert ep == e[3], s
+        checked.append(s)
+    return checked
+
+
+@pytest.mark.parametrize("name", cases())
+def test_full_pipelines_match_reference_golden(ctx, name):
+    f = load(name)
+    for pi in range(len(f["pipelines"])):
+        assert _replay(ctx, f, pi)
+
+
+@pytest.fixture(scope="module")
+def mix20k():
+    base, query = ds.int_mixture(20000, 128, 32, seed=21, n_query=200)
+    return base, query, None
+
+
+@pytest.mark.parametrize("alpha,L_refine", [(1.2, 24), (1.2, 48), (2.0, 24)])
+def test_vamana_matches_oracle_20k(ctx, mix20k, alpha, L_refine):
+    base, query, g = mix20k
+    # the GPU and the oracle each run the whole pipeline from rand seed 1
+    ctx.upload_base(base)
+    ctx.srand(1)
+    ctx.init_random(10)
+    ctx.nnd_refine(10, 24, 40, 6, 50)
+    ro = O.Rand(1)
+    go = O.nndescent(base, O.init_random(base, 10, ro), 10, 24, 40, 6, 50, ro)
+    gv = O.vamana(base, go, L_refine, 32, alpha, ro)
+    st = ctx.vamana_refine(L_refine, 32, alpha, 0)
+    ids, dist, deg, ep = ctx.get_graph()
+    assert ep == gv.ep
+    assert rows_equal(ids, dist, deg, gv.ids, gv.dist, gv.deg) == 0, st
+
+
+def test_nsg_matches_oracle_20k(ctx, mix20k):
+    base, query, g = mix20k
+    ctx.upload_base(base)
+    ctx.srand(1)
+    ctx.init_random(10)
+    ctx.nnd_refine(10, 24, 40, 6, 50)
+    ro = O.Rand(1)
+    go = O.nndescent(base, O.init_random(base, 10, ro), 10, 24, 40, 6, 50, ro)
+    gn = O.nsg(base, go, 40, 24, 200, ro)
+    st = ctx.nsg_refine(40, 24, 200)
+    ids, dist, deg, ep = ctx.get_graph()
+    assert ep == gn.ep
+    assert st["conn_added"] == gn.conn_added
+    assert rows_equal(ids, dist, deg, gn.ids, gn.dist, gn.deg) == 0, st

@@ -32,7 +32,8 @@ class Counters(C.Structure):
 
 class BuildStats(C.Structure):
     _fields_ = [("rand_draws", C.c_ulonglong), ("offers", C.c_ulonglong), ("pairs", C.c_ulonglong),
-                ("chunks", C.c_uint), ("ms_join", C.c_float), ("ms_update", C.c_float), ("ms_total", C.c_float)]
+                ("chunks", C.c_uint), ("ms_join", C.c_float), ("ms_update", C.c_float), ("ms_total", C.c_float),
+                ("levels", C.c_uint), ("ep", C.c_uint), ("conn_added", C.c_uint)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -78,6 +79,8 @@ def load(build_if_needed: bool = True):
     L.wv_init_random.argtypes = [vp, C.c_uint32, C.POINTER(BuildStats)]
     L.wv_nnd_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                 C.POINTER(BuildStats)]
+    L.wv_vamana_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, C.POINTER(BuildStats)]
+    L.wv_nsg_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(BuildStats)]
     L.wv_debug_sort.argtypes = [vp, f32p, u32p, u32p, C.c_uint32, C.c_int]
     L.wv_search_noalloc.argtypes = [vp, C.c_uint32, C.c_uint32, vp, vp, C.c_uint32, vp, C.c_uint32, vp, C.c_uint32,
                                     C.c_uint32, vp, vp, vp]

@@ -2,6 +2,7 @@
 #include <chrono>
 
 #include "wv_ctx.h"
+#include "wv_link.h"
 #include "wv_nnd.h"
 #include "wv_search.h"
 
@@ -107,6 +108,44 @@ int wv_nnd_refine(wv_ctx *c, uint32_t S, uint32_t K, uint32_t L, uint32_t ITER, 
     stats->chunks = st.chunks;
     stats->ms_join = st.ms_join;
     stats->ms_update = st.ms_update;
+    stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return rc;
+}
+
+int wv_vamana_refine(wv_ctx *c, uint32_t L_refine, uint32_t R_refine, float alpha, uint32_t entry_L,
+                     wv_build_stats *stats) {
+  if (!c) return WV_ERR_ARG;
+  WV_CUDA(c, cudaSetDevice(c->device));
+  auto t0 = std::chrono::steady_clock::now();
+  const unsigned long long d0 = c->rnd.drawn;
+  LinkStats st;
+  int rc = link_gpu(c, LinkParams{L_refine, R_refine, 0, alpha, entry_L, false}, &st);
+  if (stats) {
+    *stats = wv_build_stats{};
+    stats->rand_draws = c->rnd.drawn - d0;
+    stats->levels = st.levels;
+    stats->ep = st.ep;
+    stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return rc;
+}
+
+int wv_nsg_refine(wv_ctx *c, uint32_t L_refine, uint32_t R_refine, uint32_t C_refine, wv_build_stats *stats) {
+  if (!c) return WV_ERR_ARG;
+  WV_CUDA(c, cudaSetDevice(c->device));
+  auto t0 = std::chrono::steady_clock::now();
+  const unsigned long long d0 = c->rnd.drawn;
+  LinkStats st;
+  int rc = link_gpu(c, LinkParams{L_refine, R_refine, C_refine, 1.0f, L_refine, true}, &st);
+  uint32_t added = 0;
+  if (rc == WV_OK) rc = conn_dfs_gpu(c, L_refine, &added);
+  if (stats) {
+    *stats = wv_build_stats{};
+    stats->rand_draws = c->rnd.drawn - d0;
+    stats->levels = st.levels;
+    stats->ep = st.ep;
+    stats->conn_added = added;
     stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
   return rc;

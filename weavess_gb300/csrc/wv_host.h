@@ -34,7 +34,11 @@ class GlibcRand {
 struct RandSource {
   GlibcRand own;
   int (*fn)(void) = nullptr;
-  int next() { return fn ? fn() : own.next(); }
+  unsigned long long drawn = 0;  // values handed out
+  int next() {
+    drawn++;
+    return fn ? fn() : own.next();
+  }
 };
 
 // GenRandom (include/weavess/util.h:13-27): `size` distinct ids in [0, N)

@@ -1,0 +1,966 @@
+// K3/K4/K5: the Vamana and NSG link (REFINE_VAMANA / REFINE_NSG) on GB300.
+//
+// Replaces ComponentRefineVAMANA::RefineInner / Link / InterInsert
+// (src/component_refine.cpp:794-950), ComponentRefineNSG::RefineInner / Link /
+// InterInsert (component_refine.cpp:393-541), ComponentCandidateNSG
+// (component_candidate.cpp:10-85), ComponentPruneVAMANA / ComponentPruneNSG
+// (component_prune.cpp:20-69, 245-300) and ComponentRefineEntryCentroid
+// (component_entry.cpp:9-92).  ComponentConnNSGDFS runs on the host (a serial
+// depth-first walk), with its greedy searches on the GPU.
+//
+// Plain form, bit-exact with the single-threaded reference:
+//  * candidates: the beam kernel in build mode (seeds flagged, every visit
+//    recorded in order), seeds drawn on the host in node order;
+//  * prune: one warp per node sorts the visit pool with the warp replica of
+//    std::sort, then picks in pool order 32 candidates at a time: each lane
+//    tests its candidate against the rows picked before the batch, and a
+//    bitmask records which earlier batch members would occlude it, so the
+//    sequential pick/skip walk over the batch needs no further distances.
+//    VAMANA refills from the skipped items through libstdc++'s heap steps;
+//  * InterInsert: sequentially, node n walks its current row and inserts
+//    itself into each neighbour's row (dedup, append, or re-prune).  Node n's
+//    row at that moment is its pruned row plus the insertions from nodes < n
+//    that still listed n -- and those can only be nodes m < n with n in m's
+//    PRUNED row.  So nodes are processed by level (level(n) = 1 + max level
+//    of such m): all nodes of a level run in parallel, each applying the
+//    insertions from lower ids in id order, which gives its row at its turn
+//    (kept as a snapshot).  Then every row applies, in id order, the
+//    insertions from higher ids, read from their snapshots.  Each warp keeps
+//    the vectors' pairwise distances of its row in shared memory, so an
+//    insertion costs one new distance column.
+#include <algorithm>
+#include <vector>
+
+#include "warp_sort.cuh"
+#include "wv_common.cuh"
+#include "wv_link.h"
+#include "wv_scan.h"
+#include "wv_search.h"
+#include "wv_segsort.h"
+
+namespace wv {
+namespace {
+
+constexpr int PR_WARPS = 4;
+constexpr uint32_t LINK_MAX_R = 63;  // row slots (R + 1) index a 64-bit mask
+
+// exact-order squared L2 of two base rows, read from global memory by one lane
+__device__ __forceinline__ float l2g(const float *__restrict__ base, uint32_t d, uint32_t a, uint32_t b) {
+  const float4 *x = reinterpret_cast<const float4 *>(base + (size_t)a * d);
+  const float4 *y = reinterpret_cast<const float4 *>(base + (size_t)b * d);
+  float acc = 0.f;
+  const uint32_t d4 = d >> 2;
+#pragma unroll 4
+  for (uint32_t g = 0; g < d4; g++) acc = __fadd_rn(acc, group4(__ldg(x + g), __ldg(y + g)));
+  return acc;
+}
+
+struct HeapItem {  // Index::MinHeap<float, SimpleNeighbor>::Item
+  float key;
+  DI data;
+};
+struct HeapItemLess {  // Item::operator< is key > other.key
+  __device__ bool operator()(const HeapItem &a, const HeapItem &b) const { return a.key > b.key; }
+};
+
+// ---------------------------------------------------------------- prune
+struct PruneArgs {
+  const float *base;
+  uint32_t d, n;
+  DI *vis;              // chunk x vcap pools (sorted in place)
+  const uint32_t *vcnt;
+  uint32_t vcap;
+  uint32_t n0, cnt;     // nodes [n0, n0 + cnt)
+  uint32_t R;
+  float alpha;
+  uint32_t maxc;        // NSG: C_refine
+  const uint32_t *g_ids;  // NSG: the candidate graph (final_graph_)
+  const uint32_t *g_deg;
+  uint32_t gw;
+  int *gscr;            // per warp: 2 * vcap + 256 ints
+  HeapItem *hscr;       // per warp: vcap items (VAMANA refill)
+  uint32_t *out_ids;    // rows of width R, indexed by node
+  float *out_dist;
+  uint32_t *out_deg;
+  int *status;
+};
+
+template <bool NSG>
+__global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
+  __shared__ uint32_t pk_id[PR_WARPS][LINK_MAX_R];
+  __shared__ float pk_d[PR_WARPS][LINK_MAX_R];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t gwarp = blockIdx.x * PR_WARPS + warp, nwarps = gridDim.x * PR_WARPS;
+  int *scr = a.gscr + (size_t)gwarp * (2 * a.vcap + 256);
+  HeapItem *heap = a.hscr + (size_t)gwarp * a.vcap;
+  uint32_t *pid = pk_id[warp];
+  float *pd = pk_d[warp];
+  for (uint32_t qi = gwarp; qi < a.cnt; qi += nwarps) {
+    const uint32_t node = a.n0 + qi;
+    DI *pool = a.vis + (size_t)qi * a.vcap;
+    uint32_t m = min(a.vcnt[qi], a.vcap);
+    uint32_t *oid = a.out_ids + (size_t)node * a.R;
+    float *od = a.out_dist + (size_t)node * a.R;
+    if (NSG) {
+      // the node's own row joins the pool, distances recomputed
+      // (component_prune.cpp:26-34); vcap leaves room for it
+      const uint32_t deg = min(a.g_deg[node], a.gw);
+      for (uint32_t j = lane; j < deg; j += 32) {
+        uint32_t id = a.g_ids[(size_t)node * a.gw + j];
+        if (id >= a.n) {
+          set_err(a.status, DEV_BAD_ID);
+          id = 0;
+        }
+        if (m + j < a.vcap) pool[m + j] = DI{l2g(a.base, a.d, node, id), id};
+      }
+      if (m + deg > a.vcap) set_err(a.status, DEV_OVERFLOW);
+      m = min(m + deg, a.vcap);
+      __syncwarp();
+    }
+    if (!NSG && m <= a.R) {  // PruneVAMANA keeps a short pool unsorted
+      for (uint32_t j = lane; j < m; j += 32) {
+        oid[j] = pool[j].i;
+        od[j] = pool[j].d;
+      }
+      if (lane == 0) a.out_deg[node] = m;
+      continue;
+    }
+    if (m == 0) {
+      if (lane == 0) a.out_deg[node] = 0;
+      continue;
+    }
+    warp_std_sort(pool, (int)m, DILess(), WarpSortScratch{scr, scr + a.vcap, scr + 2 * a.vcap,
+                                                          scr + 2 * a.vcap + 192}, lane);
+    uint32_t np = 0;   // picked
+    uint32_t ex = 0;   // next pool index to examine
+    uint32_t end = m;  // examination bound
+    uint32_t nskip = 0;
+    if (NSG) {
+      // start skips the node itself at position 0; pool[start] is taken as is
+      uint32_t start = pool[0].i == node ? 1u : 0u;
+      if (start >= m) {
+        if (lane == 0) a.out_deg[node] = 0;
+        continue;
+      }
+      if (lane == 0) {
+        pid[0] = pool[start].i;
+        pd[0] = pool[start].d;
+      }
+      np = 1;
+      ex = start + 1;
+      end = min(m, a.maxc);
+      __syncwarp();
+    }
+    bool done = np >= a.R;
+    while (!done && ex < end) {
+      const uint32_t cnt = min(32u, end - ex);
+      DI cand = lane < (int)cnt ? pool[ex + lane] : DI{0.f, 0u};
+      // against the rows picked before this batch
+      bool s1 = false;
+      if (lane < (int)cnt) {
+        for (uint32_t j = 0; j < np && !s1; j++) {
+          if (NSG && pid[j] == cand.i) s1 = true;
+          else {
+            float dd = l2g(a.base, a.d, pid[j], cand.i);
+            s1 = NSG ? (dd < cand.d) : (__fmul_rn(a.alpha, dd) < cand.d);
+          }
+        }
+      }
+      // which earlier batch members would occlude this one
+      uint32_t occl = 0;
+      for (int b = 0; b < (int)cnt; b++) {
+        const uint32_t bid = __shfl_sync(FULL, cand.i, b);
+        if (b < lane && lane < (int)cnt) {
+          bool hit;
+          if (NSG && bid == cand.i) hit = true;
+          else {
+            float dd = l2g(a.base, a.d, bid, cand.i);
+            hit = NSG ? (dd < cand.d) : (__fmul_rn(a.alpha, dd) < cand.d);
+          }
+          if (hit) occl |= 1u << b;
+        }
+      }
+      // the sequential walk of the reference over this batch
+      uint32_t pm = 0;
+      uint32_t stop = cnt;
+      for (int b = 0; b < (int)cnt; b++) {
+        const bool sb = __shfl_sync(FULL, s1, b);
+        const uint32_t ob = __shfl_sync(FULL, occl, b);
+        const DI cb = DI{__shfl_sync(FULL, cand.d, b), __shfl_sync(FULL, cand.i, b)};
+        const bool skip = sb || (ob & pm);
+        if (!skip) {
+          pm |= 1u << b;
+          if (lane == 0) {
+            pid[np] = cb.i;
+            pd[np] = cb.d;
+          }
+          np++;
+          if (np == a.R) {
+            stop = b + 1;
+            done = true;
+            break;
+          }
+        } else if (!NSG) {
+          if (lane == 0) heap[nskip] = HeapItem{cb.d, cb};
+          nskip++;
+        }
+      }
+      __syncwarp();
+      ex += stop;
+    }
+    if (!NSG && np < a.R && nskip > 0) {
+      // refill from the skipped min-heap (component_prune.cpp:276-279)
+      if (lane == 0) {
+        for (uint32_t k = 1; k <= nskip; k++) stl::push_heap(heap, (int)k, HeapItemLess());
+        uint32_t hs = nskip;
+        while (np < a.R && hs > 0) {
+          pid[np] = heap[0].data.i;
+          pd[np] = heap[0].data.d;
+          np++;
+          stl::pop_heap(heap, (int)hs, HeapItemLess());
+          hs--;
+        }
+      }
+      np = __shfl_sync(FULL, np, 0);
+      __syncwarp();
+    }
+    for (uint32_t j = lane; j < np; j += 32) {
+      oid[j] = pid[j];
+      od[j] = pd[j];
+    }
+    if (lane == 0) a.out_deg[node] = np;
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------- InterInsert
+struct IIArgs {
+  const float *base;
+  uint32_t d, n, R;
+  float alpha;
+  int vamana;
+  const uint32_t *p_ids;   // pruned rows (width R)
+  const float *p_dist;
+  const uint32_t *p_deg;
+  uint32_t *s_ids;         // rows at each node's turn (width R)
+  float *s_dist;
+  uint32_t *s_deg;
+  uint32_t *f_ids;         // final rows (width R)
+  float *f_dist;
+  uint32_t *f_deg;
+  const uint32_t *nodes;   // nodes of this launch
+  uint32_t nn;
+  const unsigned long long *req;  // per target: (sender << 32 | index) sorted
+  const uint32_t *req_off, *req_cnt;
+  int *status;
+};
+
+constexpr int II_WARPS = 4;
+constexpr int II_SLOTS = LINK_MAX_R + 1;
+
+struct Ent3 {
+  float d;
+  uint32_t i;
+  uint32_t slot;
+};
+struct Ent3Less {
+  __device__ bool operator()(const Ent3 &a, const Ent3 &b) const { return a.d < b.d; }
+};
+struct HeapIdx {  // MinHeap item of the re-prune: key and temp index
+  float key;
+  uint32_t k;
+};
+struct HeapIdxLess {
+  __device__ bool operator()(const HeapIdx &a, const HeapIdx &b) const { return a.key > b.key; }
+};
+
+struct IIWarp {
+  Ent3 row[II_SLOTS];
+  Ent3 tmp[II_SLOTS];
+  uint32_t sid[II_SLOTS];     // id held by each slot
+  float D[II_SLOTS][II_SLOTS];  // pairwise distances of slot vectors
+  uint32_t res[II_SLOTS];
+  HeapIdx heap[II_SLOTS];
+};
+
+// applies "insert `s` (distance dist, sender index i) into this row" exactly
+// as InterInsert does to des_pool (component_refine.cpp:484-540 / 884-949)
+__device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t &rs, bool &dvalid, uint32_t s, float dist, uint32_t i,
+                         int lane) {
+  bool dup = false;
+  for (uint32_t j = lane; j < rs; j += 32) dup |= w.row[j].i == s;
+  if (__any_sync(FULL, dup)) return;
+  const uint32_t R = a.R;
+  if (rs + 1 <= R) {  // room: append
+    if (lane == 0) w.row[rs] = Ent3{dist, s, INVALID};
+    rs++;
+    dvalid = false;  // slots assigned lazily at the next re-prune
+    __syncwarp();
+    return;
+  }
+  // re-prune needs the pairwise distances of row + s
+  if (!dvalid) {
+    // (re)assign slots 0..rs-1 to the row and fill the whole matrix
+    for (uint32_t j = lane; j < rs; j += 32) {
+      w.row[j].slot = j;
+      w.sid[j] = w.row[j].i;
+    }
+    __syncwarp();
+    for (uint32_t p = lane; p < rs * rs; p += 32) {
+      uint32_t x = p / rs, y = p % rs;
+      if (x < y) {
+        float dd = l2g(a.base, a.d, w.sid[x], w.sid[y]);
+        w.D[x][y] = dd;
+        w.D[y][x] = dd;
+      }
+    }
+    dvalid = true;
+    __syncwarp();
+  }
+  // a free slot for s (the row uses rs <= R of R + 1 slots)
+  unsigned long long used = 0;
+  for (uint32_t j = 0; j < rs; j++) used |= 1ull << w.row[j].slot;
+  uint32_t f = __ffsll(~used) - 1;
+  if (lane == 0) w.sid[f] = s;
+  __syncwarp();
+  for (uint32_t j = lane; j < rs; j += 32) {
+    float dd = l2g(a.base, a.d, w.row[j].i, s);
+    w.D[f][w.row[j].slot] = dd;
+    w.D[w.row[j].slot][f] = dd;
+  }
+  const uint32_t T = rs + 1;
+  for (uint32_t j = lane; j < rs; j += 32) w.tmp[j] = w.row[j];
+  if (lane == 0) w.tmp[rs] = Ent3{dist, s, f};
+  __syncwarp();
+  if (lane == 0) stl::sort(w.tmp, (int)T, Ent3Less());
+  __syncwarp();
+  uint32_t nres = 0;
+  if (a.vamana) {
+    const float cur = w.tmp[i].d;  // temp_pool[i]: the outer index (refine.cpp:907)
+    uint32_t nskip = 0;
+    for (int k = (int)T - 1; k >= 0; --k) {
+      const uint32_t ks = w.tmp[k].slot;
+      bool hit = false;
+      for (uint32_t j = lane; j < nres; j += 32) hit |= __fmul_rn(a.alpha, w.D[w.tmp[w.res[j]].slot][ks]) < cur;
+      const bool skip = __any_sync(FULL, hit);
+      if (!skip) {
+        if (lane == 0) w.res[nres] = (uint32_t)k;
+        nres++;
+      } else {
+        if (lane == 0) {
+          w.heap[nskip] = HeapIdx{cur, (uint32_t)k};
+          stl::push_heap(w.heap, (int)(nskip + 1), HeapIdxLess());
+        }
+        nskip++;
+      }
+      __syncwarp();
+      if (nres == R) break;
+    }
+    if (nres < R && nskip > 0) {
+      if (lane == 0) {
+        uint32_t hs = nskip;
+        while (nres < R && hs > 0) {
+          w.res[nres++] = w.heap[0].k;
+          stl::pop_heap(w.heap, (int)hs, HeapIdxLess());
+          hs--;
+        }
+      }
+      nres = __shfl_sync(FULL, nres, 0);
+      __syncwarp();
+    }
+  } else {
+    if (lane == 0) w.res[0] = 0;
+    nres = 1;
+    __syncwarp();
+    for (uint32_t st = 1; nres < R && st < T; st++) {
+      const Ent3 p = w.tmp[st];
+      bool occ = false;
+      for (uint32_t j = lane; j < nres; j += 32) {
+        const Ent3 r = w.tmp[w.res[j]];
+        occ |= (r.i == p.i) || (w.D[r.slot][p.slot] < p.d);
+      }
+      if (!__any_sync(FULL, occ)) {
+        if (lane == 0) w.res[nres] = st;
+        nres++;
+      }
+      __syncwarp();
+    }
+  }
+  // des_pool[t] = result[t] for t < result.size() (refine.cpp:527-530,
+  // 943-946).  Vamana results always hold R entries; an NSG result may be
+  // shorter and then, with no sentinel written, the old entries at positions
+  // result.size()..R-1 stay in the row.
+  for (uint32_t j = lane; j < nres; j += 32) w.row[j] = w.tmp[w.res[j]];
+  __syncwarp();
+  if (a.vamana) rs = nres;
+  __syncwarp();
+}
+
+__device__ void ii_load_row(IIWarp &w, const uint32_t *ids, const float *dist, uint32_t deg, int lane) {
+  for (uint32_t j = lane; j < deg; j += 32) w.row[j] = Ent3{dist[j], ids[j], INVALID};
+  __syncwarp();
+}
+
+// forward: each node of this level applies the insertions from lower ids
+// (senders m < n whose row at their turn lists n), then snapshots its row
+__global__ void __launch_bounds__(II_WARPS * 32) k_ii_forward(IIArgs a) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  IIWarp &w = reinterpret_cast<IIWarp *>(smem)[warp];
+  for (uint32_t t = blockIdx.x * II_WARPS + warp; t < a.nn; t += gridDim.x * II_WARPS) {
+    const uint32_t n = a.nodes[t];
+    uint32_t rs = a.p_deg[n];
+    ii_load_row(w, a.p_ids + (size_t)n * a.R, a.p_dist + (size_t)n * a.R, rs, lane);
+    bool dvalid = false;
+    const uint32_t off = a.req_off[n], cnt = a.req_cnt[n];
+    for (uint32_t r = 0; r < cnt; r++) {
+      const uint32_t m = (uint32_t)(a.req[off + r] >> 32);
+      // each position of n in m's row at m's turn sends one insertion
+      // (an NSG row can list an id twice), in position order
+      const uint32_t mdeg = a.s_deg[m];
+      for (uint32_t b = 0; b < mdeg; b += 32) {
+        const uint32_t j = b + lane;
+        unsigned hits = __ballot_sync(FULL, j < mdeg && a.s_ids[(size_t)m * a.R + j] == n);
+        while (hits) {
+          const uint32_t pos = b + __ffs(hits) - 1;
+          hits &= hits - 1;
+          ii_apply(a, w, rs, dvalid, m, a.s_dist[(size_t)m * a.R + pos], pos, lane);
+        }
+      }
+    }
+    for (uint32_t j = lane; j < rs; j += 32) {
+      a.s_ids[(size_t)n * a.R + j] = w.row[j].i;
+      a.s_dist[(size_t)n * a.R + j] = w.row[j].d;
+    }
+    if (lane == 0) a.s_deg[n] = rs;
+    __syncwarp();
+  }
+}
+
+// backward: every row applies the insertions from higher ids in id order
+__global__ void __launch_bounds__(II_WARPS * 32) k_ii_backward(IIArgs a) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  IIWarp &w = reinterpret_cast<IIWarp *>(smem)[warp];
+  for (uint32_t r = blockIdx.x * II_WARPS + warp; r < a.n; r += gridDim.x * II_WARPS) {
+    uint32_t rs = a.s_deg[r];
+    ii_load_row(w, a.s_ids + (size_t)r * a.R, a.s_dist + (size_t)r * a.R, rs, lane);
+    bool dvalid = false;
+    const uint32_t off = a.req_off[r], cnt = a.req_cnt[r];
+    for (uint32_t q = 0; q < cnt; q++) {
+      const unsigned long long key = a.req[off + q];
+      const uint32_t m = (uint32_t)(key >> 32), pos = (uint32_t)key;
+      ii_apply(a, w, rs, dvalid, m, a.s_dist[(size_t)m * a.R + pos], pos, lane);
+    }
+    for (uint32_t j = lane; j < rs; j += 32) {
+      a.f_ids[(size_t)r * a.R + j] = w.row[j].i;
+      a.f_dist[(size_t)r * a.R + j] = w.row[j].d;
+    }
+    if (lane == 0) a.f_deg[r] = rs;
+    __syncwarp();
+  }
+}
+
+// requests index: count edges m -> t of rows (ids, deg) with m < t (fwd) or m > t
+__global__ void k_req_count(uint32_t n, uint32_t R, const uint32_t *ids, const uint32_t *deg, int fwd, uint32_t *cnt) {
+  const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  for (uint32_t j = 0; j < deg[m]; j++) {
+    const uint32_t t = ids[(size_t)m * R + j];
+    if (t < n && (fwd ? m < t : m > t)) atomicAdd(&cnt[t], 1u);
+  }
+}
+__global__ void k_req_fill(uint32_t n, uint32_t R, const uint32_t *ids, const uint32_t *deg, int fwd,
+                           const uint32_t *off, uint32_t *cur, unsigned long long *req) {
+  const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  for (uint32_t j = 0; j < deg[m]; j++) {
+    const uint32_t t = ids[(size_t)m * R + j];
+    if (t < n && (fwd ? m < t : m > t))
+      req[off[t] + atomicAdd(&cur[t], 1u)] = ((unsigned long long)m << 32) | j;
+  }
+}
+
+// level(t) = max(level(t), level(m) + 1) over forward edges of the pruned rows
+__global__ void k_level_relax(uint32_t n, uint32_t R, const uint32_t *ids, const uint32_t *deg, uint32_t *level,
+                              uint32_t *changed) {
+  const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  const uint32_t lm = level[m];
+  for (uint32_t j = 0; j < deg[m]; j++) {
+    const uint32_t t = ids[(size_t)m * R + j];
+    if (t < n && m < t && level[t] < lm + 1) {
+      atomicMax(&level[t], lm + 1);
+      *changed = 1;
+    }
+  }
+}
+__global__ void k_level_count(uint32_t n, const uint32_t *level, uint32_t *lcnt) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) atomicAdd(&lcnt[level[i]], 1u);
+}
+__global__ void k_level_fill(uint32_t n, const uint32_t *level, const uint32_t *loff, uint32_t *lcur,
+                             uint32_t *order) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) order[loff[level[i]] + atomicAdd(&lcur[level[i]], 1u)] = i;
+}
+
+// ---------------------------------------------------------------- centroid
+// EntryCentroid's FP32 column sums in the reference's order (i ascending)
+__global__ void k_centroid(const float *base, uint32_t n, uint32_t d, float *center) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= d) return;
+  float acc = 0.f;
+  for (uint32_t i = 0; i < n; i++) acc = __fadd_rn(acc, base[(size_t)i * d + j]);
+  center[j] = __fdiv_rn(acc, (float)n);
+}
+
+__global__ void k_pair_l2(const float *base, uint32_t d, uint32_t a, uint32_t b, float *out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *out = l2g(base, d, a, b);
+}
+
+}  // namespace
+
+// ================================================================ host side
+namespace {
+
+int run_build_search(wv_ctx *c, const float *d_queries, uint32_t nq, const uint32_t *d_seeds, uint32_t seed_stride,
+                     uint32_t L, const uint32_t *gids, const uint32_t *gdeg, uint32_t gw, DI *vis, uint32_t *vcnt,
+                     uint32_t vcap, uint32_t *out_ids, uint32_t K, uint32_t vlimit = 0) {
+  if (vlimit == 0) vlimit = vcap;
+  const uint32_t cap = gw + 32;
+  int blocks = search_grid(c->d, L, cap, c->device);
+  WV_CHECK(c, blocks > 0, WV_ERR_LIMIT, "candidate search cannot run with d=%u L=%u width=%u", c->d, L, gw);
+  size_t slots = (size_t)blocks * search_warps_per_block();
+  size_t words = (c->n + 31) / 32;
+  if (slots > c->vis_slots || words != c->vis_words) {
+    c->visited.release();
+    c->touched.release();
+    WV_CUDA(c, c->visited.ensure(slots * words * 4));
+    WV_CUDA(c, c->touched.ensure(slots * words * 4));
+    WV_CUDA(c, cudaMemsetAsync(c->visited.p, 0, slots * words * 4, c->stream));
+    c->vis_slots = slots;
+    c->vis_words = words;
+  }
+  WV_CUDA(c, cudaMemsetAsync(c->misc.p, 0, 32, c->stream));
+  SearchArgs a{};
+  a.base = c->base.as<float>();
+  a.n = c->n;
+  a.d = c->d;
+  a.gids = gids;
+  a.gdeg = gdeg;
+  a.gw = gw;
+  a.queries = d_queries;
+  a.nq = nq;
+  a.seeds = d_seeds;
+  a.seed_stride = seed_stride;
+  a.L = L;
+  a.K = K;
+  a.Lmax = L;
+  a.out_ids = out_ids;
+  a.out_stride = K;
+  a.visited = c->visited.as<uint32_t>();
+  a.touched = c->touched.as<uint32_t>();
+  a.words = (uint32_t)words;
+  a.cap = cap;
+  a.next_query = c->d_next();
+  a.status = c->d_status();
+  a.vis = vis;
+  a.vcnt = vcnt;
+  a.vcap = vcap;
+  a.vlimit = vlimit;
+  int nb = (int)std::min<size_t>((size_t)blocks, ((size_t)nq + search_warps_per_block() - 1) / search_warps_per_block());
+  WV_CUDA(c, launch_search_exact(a, std::max(nb, 1), c->stream));
+  return WV_OK;
+}
+
+}  // namespace
+
+int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
+  WV_CHECK(c, c->n > 0 && c->fg_n == c->n, WV_ERR_STATE, "the link needs the base and a candidate graph");
+  WV_CHECK(c, p.R >= 1 && p.R <= LINK_MAX_R, WV_ERR_LIMIT, "R_refine=%u: this build supports 1..%u", p.R, LINK_MAX_R);
+  WV_CHECK(c, p.L >= 1 && p.L < c->n && p.L <= SEARCH_MAX_L, WV_ERR_ARG, "L_refine=%u out of range", p.L);
+  WV_CHECK(c, c->fg_w <= SEARCH_MAX_WIDTH, WV_ERR_LIMIT, "candidate graph width %u above %u", c->fg_w,
+           SEARCH_MAX_WIDTH);
+  WV_CHECK(c, c->d % 4 == 0, WV_ERR_LIMIT, "dimension %u is not a multiple of 4", c->d);
+  LinkStats local;
+  LinkStats &S = st ? *st : local;
+  S = LinkStats();
+  cudaError_t e = cudaSuccess;
+  const uint32_t n = c->n, R = p.R, gw = c->fg_w;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, c->stream);
+  // host copies of what the host-side draws need
+  std::vector<uint32_t> hdeg(n);
+  WV_CUDA(c, cudaMemcpyAsync(hdeg.data(), c->fg_deg.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  auto host_row = [&](uint32_t v, std::vector<uint32_t> &out) -> int {
+    out.resize(hdeg[v]);
+    if (hdeg[v])
+      WV_CUDA(c, cudaMemcpy(out.data(), c->fg_ids.as<uint32_t>() + (size_t)v * gw, hdeg[v] * 4, cudaMemcpyDeviceToHost));
+    return WV_OK;
+  };
+  float *center = c->buf<float>("center", c->d, &e);
+  uint32_t *seed1 = c->buf<uint32_t>("seed1", p.L, &e);
+  uint32_t *one = c->buf<uint32_t>("one", 4, &e);
+  WV_CUDA(c, e);
+  // ---- entry point (ComponentRefineEntryCentroid::EntryInner)
+  k_centroid<<<(c->d + 127) / 128, 128, 0, c->stream>>>(c->base.as<float>(), n, c->d, center);
+  WV_CUDA(c, cudaGetLastError());
+  uint32_t ep = (uint32_t)c->rnd.next() % n;
+  if (p.entry_L == 0) {
+    ep = 0;  // get_neighbors with L = 0 leaves retset[0] value-initialised
+  } else {
+    std::vector<uint32_t> row, sd(p.entry_L);
+    int rc = host_row(ep, row);
+    if (rc) return rc;
+    draw_seeds_row(c->rnd, p.entry_L, n, row.data(), (uint32_t)row.size(), sd.data());
+    WV_CUDA(c, cudaMemcpyAsync(seed1, sd.data(), p.entry_L * 4, cudaMemcpyHostToDevice, c->stream));
+    DI *v1 = c->buf<DI>("vis1", (size_t)n + p.entry_L + 64, &e);
+    WV_CUDA(c, e);
+    rc = run_build_search(c, center, 1, seed1, p.entry_L, p.entry_L, c->fg_ids.as<uint32_t>(),
+                          c->fg_deg.as<uint32_t>(), gw, v1, one + 1, n + p.entry_L + 64, one, 1);
+    if (rc) return rc;
+    WV_CUDA(c, cudaMemcpyAsync(&ep, one, 4, cudaMemcpyDeviceToHost, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  S.ep = ep;
+  // ---- candidates + prune, in chunks of nodes
+  uint32_t *p_ids = c->buf<uint32_t>("lk_pids", (size_t)n * R, &e);
+  float *p_dist = c->buf<float>("lk_pdist", (size_t)n * R, &e);
+  uint32_t *p_deg = c->buf<uint32_t>("lk_pdeg", n, &e);
+  WV_CUDA(c, e);
+  std::vector<uint32_t> ep_row;
+  {
+    int rc = host_row(ep, ep_row);
+    if (rc) return rc;
+  }
+  const bool shared_seeds = p.L <= ep_row.size();  // no rand() fill needed
+  uint32_t vcap = std::max<uint32_t>(2048, 8 * p.L) + gw;
+  const uint32_t CH = std::min<uint32_t>(n, 1u << 17);
+  std::vector<uint32_t> hseeds;
+  uint32_t *dseeds = c->buf<uint32_t>("lk_seeds", (size_t)(shared_seeds ? 1 : CH) * p.L, &e);
+  WV_CUDA(c, e);
+  if (shared_seeds)
+    WV_CUDA(c, cudaMemcpyAsync(dseeds, ep_row.data(), p.L * 4, cudaMemcpyHostToDevice, c->stream));
+  const int prune_blocks = c->sms * 8;
+  const size_t nwarps = (size_t)prune_blocks * PR_WARPS;
+  for (uint32_t n0 = 0; n0 < n; n0 += CH) {
+    const uint32_t cnt = std::min(CH, n - n0);
+    if (!shared_seeds) {
+      hseeds.resize((size_t)cnt * p.L);
+      for (uint32_t q = 0; q < cnt; q++) {
+        // the fill draws rand() % N until L ids are taken (candidate.cpp:25-31)
+        draw_seeds_row(c->rnd, p.L, n, ep_row.data(), (uint32_t)ep_row.size(), hseeds.data() + (size_t)q * p.L);
+      }
+      WV_CUDA(c, cudaMemcpyAsync(dseeds, hseeds.data(), (size_t)cnt * p.L * 4, cudaMemcpyHostToDevice, c->stream));
+    }
+    while (true) {
+      DI *vis = c->buf<DI>("lk_vis", (size_t)cnt * vcap, &e);
+      uint32_t *vcnt = c->buf<uint32_t>("lk_vcnt", cnt, &e);
+      int *gscr = c->buf<int>("lk_gscr", nwarps * (2 * (size_t)vcap + 256), &e);
+      HeapItem *hscr = c->buf<HeapItem>("lk_hscr", nwarps * (size_t)vcap, &e);
+      WV_CUDA(c, e);
+      int rc = run_build_search(c, c->base.as<float>() + (size_t)n0 * c->d, cnt, dseeds, shared_seeds ? 0 : p.L, p.L,
+                                c->fg_ids.as<uint32_t>(), c->fg_deg.as<uint32_t>(), gw, vis, vcnt, vcap, nullptr, 1,
+                                vcap - (p.nsg ? gw : 0));
+      if (rc) return rc;
+      int st0 = 0;
+      WV_CUDA(c, cudaMemcpyAsync(&st0, c->d_status(), 4, cudaMemcpyDeviceToHost, c->stream));
+      WV_CUDA(c, cudaStreamSynchronize(c->stream));
+      if (st0 == DEV_OVERFLOW) {  // a visit list outgrew vcap: redo the chunk with room
+        WV_CUDA(c, cudaMemsetAsync(c->d_status(), 0, 4, c->stream));
+        vcap = vcap * 2;
+        continue;
+      }
+      rc = check_device_status(c, "candidate search");
+      if (rc) return rc;
+      PruneArgs pa{};
+      pa.base = c->base.as<float>();
+      pa.d = c->d;
+      pa.n = n;
+      pa.vis = vis;
+      pa.vcnt = vcnt;
+      pa.vcap = vcap;
+      pa.n0 = n0;
+      pa.cnt = cnt;
+      pa.R = R;
+      pa.alpha = p.alpha;
+      pa.maxc = p.C;
+      pa.g_ids = c->fg_ids.as<uint32_t>();
+      pa.g_deg = c->fg_deg.as<uint32_t>();
+      pa.gw = gw;
+      pa.gscr = gscr;
+      pa.hscr = hscr;
+      pa.out_ids = p_ids;
+      pa.out_dist = p_dist;
+      pa.out_deg = p_deg;
+      pa.status = c->d_status();
+      if (p.nsg) k_prune<true><<<prune_blocks, PR_WARPS * 32, 0, c->stream>>>(pa);
+      else k_prune<false><<<prune_blocks, PR_WARPS * 32, 0, c->stream>>>(pa);
+      WV_CUDA(c, cudaGetLastError());
+      rc = check_device_status(c, "prune");
+      if (rc) return rc;
+      break;
+    }
+  }
+  // ---- InterInsert
+  uint32_t *level = c->buf<uint32_t>("lk_level", n, &e);
+  uint32_t *flag = c->buf<uint32_t>("lk_flag", 4, &e);
+  uint32_t *rcnt = c->buf<uint32_t>("lk_rcnt", n, &e);
+  uint32_t *roff = c->buf<uint32_t>("lk_roff", n + 1, &e);
+  uint32_t *rcur = c->buf<uint32_t>("lk_rcur", n, &e);
+  uint32_t *scan_tmp = c->buf<uint32_t>("lk_scan", scan_scratch_words((size_t)n + 1), &e);
+  unsigned long long *req = c->buf<unsigned long long>("lk_req", (size_t)n * R + 1, &e);
+  uint32_t *s_ids = c->buf<uint32_t>("lk_sids", (size_t)n * R, &e);
+  float *s_dist = c->buf<float>("lk_sdist", (size_t)n * R, &e);
+  uint32_t *s_deg = c->buf<uint32_t>("lk_sdeg", n, &e);
+  uint32_t *order = c->buf<uint32_t>("lk_order", n, &e);
+  WV_CUDA(c, e);
+  const int nb = (int)((n + 255) / 256);
+  WV_CUDA(c, cudaMemsetAsync(level, 0, (size_t)n * 4, c->stream));
+  uint32_t iters = 0;
+  while (true) {
+    WV_CUDA(c, cudaMemsetAsync(flag, 0, 4, c->stream));
+    k_level_relax<<<nb, 256, 0, c->stream>>>(n, R, p_ids, p_deg, level, flag);
+    uint32_t ch = 0;
+    WV_CUDA(c, cudaMemcpyAsync(&ch, flag, 4, cudaMemcpyDeviceToHost, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    iters++;
+    if (!ch) break;
+    WV_CHECK(c, iters <= n + 1, WV_ERR_DEVICE, "level relaxation did not converge");
+  }
+  std::vector<uint32_t> hlevel(n);
+  WV_CUDA(c, cudaMemcpyAsync(hlevel.data(), level, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  const uint32_t nlev = *std::max_element(hlevel.begin(), hlevel.end()) + 1;
+  S.levels = nlev;
+  uint32_t *lcnt = c->buf<uint32_t>("lk_lcnt", nlev + 1, &e);
+  uint32_t *loff = c->buf<uint32_t>("lk_loff", nlev + 1, &e);
+  uint32_t *lcur = c->buf<uint32_t>("lk_lcur", nlev + 1, &e);
+  uint32_t *scan_l = c->buf<uint32_t>("lk_scanl", scan_scratch_words(nlev + 1), &e);
+  WV_CUDA(c, e);
+  WV_CUDA(c, cudaMemsetAsync(lcnt, 0, (size_t)(nlev + 1) * 4, c->stream));
+  WV_CUDA(c, cudaMemsetAsync(lcur, 0, (size_t)(nlev + 1) * 4, c->stream));
+  k_level_count<<<nb, 256, 0, c->stream>>>(n, level, lcnt);
+  WV_CUDA(c, exclusive_scan_u32(lcnt, loff, nlev + 1, scan_l, c->stream));
+  k_level_fill<<<nb, 256, 0, c->stream>>>(n, level, loff, lcur, order);
+  std::vector<uint32_t> hloff(nlev + 1);
+  WV_CUDA(c, cudaMemcpyAsync(hloff.data(), loff, (size_t)(nlev + 1) * 4, cudaMemcpyDeviceToHost, c->stream));
+  // forward request lists from the pruned rows, sorted by sender
+  WV_CUDA(c, cudaMemsetAsync(rcnt, 0, (size_t)n * 4, c->stream));
+  WV_CUDA(c, cudaMemsetAsync(rcur, 0, (size_t)n * 4, c->stream));
+  k_req_count<<<nb, 256, 0, c->stream>>>(n, R, p_ids, p_deg, 1, rcnt);
+  WV_CUDA(c, exclusive_scan_u32(rcnt, roff, n, scan_tmp, c->stream));
+  k_req_fill<<<nb, 256, 0, c->stream>>>(n, R, p_ids, p_deg, 1, roff, rcur, req);
+  int rc = segsort_u64(c, req, roff, rcnt, n);
+  if (rc) return rc;
+  IIArgs ia{};
+  ia.base = c->base.as<float>();
+  ia.d = c->d;
+  ia.n = n;
+  ia.R = R;
+  ia.alpha = p.alpha;
+  ia.vamana = !p.nsg;
+  ia.p_ids = p_ids;
+  ia.p_dist = p_dist;
+  ia.p_deg = p_deg;
+  ia.s_ids = s_ids;
+  ia.s_dist = s_dist;
+  ia.s_deg = s_deg;
+  ia.req = req;
+  ia.req_off = roff;
+  ia.req_cnt = rcnt;
+  ia.status = c->d_status();
+  const size_t ii_smem = II_WARPS * sizeof(IIWarp);
+  WV_CUDA(c, cudaFuncSetAttribute(k_ii_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ii_smem));
+  WV_CUDA(c, cudaFuncSetAttribute(k_ii_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ii_smem));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (uint32_t t = 0; t < nlev; t++) {
+    const uint32_t cnt = hloff[t + 1] - hloff[t];
+    if (!cnt) continue;
+    ia.nodes = order + hloff[t];
+    ia.nn = cnt;
+    const int blocks = (int)std::min<uint32_t>((cnt + II_WARPS - 1) / II_WARPS, (uint32_t)c->sms * 16);
+    k_ii_forward<<<blocks, II_WARPS * 32, ii_smem, c->stream>>>(ia);
+  }
+  WV_CUDA(c, cudaGetLastError());
+  // backward request lists from the snapshots, sorted by sender
+  WV_CUDA(c, cudaMemsetAsync(rcnt, 0, (size_t)n * 4, c->stream));
+  WV_CUDA(c, cudaMemsetAsync(rcur, 0, (size_t)n * 4, c->stream));
+  k_req_count<<<nb, 256, 0, c->stream>>>(n, R, s_ids, s_deg, 0, rcnt);
+  WV_CUDA(c, exclusive_scan_u32(rcnt, roff, n, scan_tmp, c->stream));
+  k_req_fill<<<nb, 256, 0, c->stream>>>(n, R, s_ids, s_deg, 0, roff, rcur, req);
+  rc = segsort_u64(c, req, roff, rcnt, n);
+  if (rc) return rc;
+  // final rows (width R) replace the build graph
+  WV_CUDA(c, c->fg_ids.ensure((size_t)n * R * 4));
+  WV_CUDA(c, c->fg_dist.ensure((size_t)n * R * 4));
+  WV_CUDA(c, c->fg_deg.ensure((size_t)n * 4));
+  ia.f_ids = c->fg_ids.as<uint32_t>();
+  ia.f_dist = c->fg_dist.as<float>();
+  ia.f_deg = c->fg_deg.as<uint32_t>();
+  k_ii_backward<<<c->sms * 16, II_WARPS * 32, ii_smem, c->stream>>>(ia);
+  WV_CUDA(c, cudaGetLastError());
+  rc = check_device_status(c, "inter-insert");
+  if (rc) return rc;
+  c->fg_w = R;
+  c->fg_ep = ep;
+  c->fg_has_ep = true;
+  cudaEventRecord(e1, c->stream);
+  cudaEventSynchronize(e1);
+  cudaEventElapsedTime(&S.ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return WV_OK;
+}
+
+int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
+  // ComponentConnNSGDFS::tree_grow (component_conn.cpp:14-28): host DFS over
+  // the graph; each unreached node is linked from the nearest reached node a
+  // greedy search finds (GPU), or a random reached node.  The searches read
+  // the graph with the edges added so far, so each new edge is written into
+  // the device rows at once (rows carry spare width for them).
+  const uint32_t n = c->n, ep = c->fg_ep;
+  uint32_t w = c->fg_w;
+  std::vector<uint32_t> deg(n), ids((size_t)n * w);
+  std::vector<float> dist((size_t)n * w);
+  WV_CUDA(c, cudaMemcpyAsync(deg.data(), c->fg_deg.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaMemcpyAsync(ids.data(), c->fg_ids.p, (size_t)n * w * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaMemcpyAsync(dist.data(), c->fg_dist.p, (size_t)n * w * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  // re-lays rows out with width nw (host arrays and device copy)
+  auto relayout = [&](uint32_t nw) -> int {
+    std::vector<uint32_t> i2((size_t)n * nw, 0);
+    std::vector<float> d2((size_t)n * nw, 0.f);
+    for (uint32_t v = 0; v < n; v++)
+      for (uint32_t j = 0; j < deg[v]; j++) {
+        i2[(size_t)v * nw + j] = ids[(size_t)v * w + j];
+        d2[(size_t)v * nw + j] = dist[(size_t)v * w + j];
+      }
+    ids.swap(i2);
+    dist.swap(d2);
+    w = nw;
+    WV_CUDA(c, c->fg_ids.ensure((size_t)n * w * 4));
+    WV_CUDA(c, c->fg_dist.ensure((size_t)n * w * 4));
+    WV_CUDA(c, cudaMemcpyAsync(c->fg_ids.p, ids.data(), (size_t)n * w * 4, cudaMemcpyHostToDevice, c->stream));
+    WV_CUDA(c, cudaMemcpyAsync(c->fg_dist.p, dist.data(), (size_t)n * w * 4, cudaMemcpyHostToDevice, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->fg_w = w;
+    return WV_OK;
+  };
+  std::vector<char> flag(n, 0);
+  uint32_t root = ep, cnt = 0;
+  *added = 0;
+  cudaError_t e = cudaSuccess;
+  float *dd = c->buf<float>("conn_d", 4, &e);
+  uint32_t *dseed = c->buf<uint32_t>("conn_seed", L_refine, &e);
+  uint32_t *one = c->buf<uint32_t>("conn_one", 4, &e);
+  DI *vis = c->buf<DI>("conn_vis", (size_t)n + L_refine + 64, &e);
+  WV_CUDA(c, e);
+  std::vector<DI> hv;
+  bool widened = false;
+  while (cnt < n) {
+    std::vector<uint32_t> st;
+    uint32_t tmp = root;
+    st.push_back(root);
+    if (!flag[root]) cnt++;
+    flag[root] = 1;
+    while (!st.empty()) {
+      uint32_t next = n + 1;
+      for (uint32_t j = 0; j < deg[tmp]; j++)
+        if (!flag[ids[(size_t)tmp * w + j]]) {
+          next = ids[(size_t)tmp * w + j];
+          break;
+        }
+      if (next == n + 1) {
+        st.pop_back();
+        if (st.empty()) break;
+        tmp = st.back();
+        continue;
+      }
+      tmp = next;
+      flag[tmp] = 1;
+      st.push_back(tmp);
+      cnt++;
+    }
+    if (cnt >= n) break;
+    uint32_t id = n;
+    for (uint32_t i = 0; i < n; i++)
+      if (!flag[i]) {
+        id = i;
+        break;
+      }
+    if (id == n) break;
+    if (!widened) {  // spare width for the edges this pass adds
+      int rc = relayout(w + 16);
+      if (rc) return rc;
+      widened = true;
+    }
+    // get_neighbors(base[id]) from ep's row (component_conn.cpp:94-160)
+    std::vector<uint32_t> sd(L_refine);
+    draw_seeds_row(c->rnd, L_refine, n, ids.data() + (size_t)ep * w, deg[ep], sd.data());
+    WV_CUDA(c, cudaMemcpyAsync(dseed, sd.data(), L_refine * 4, cudaMemcpyHostToDevice, c->stream));
+    int rc = run_build_search(c, c->base.as<float>() + (size_t)id * c->d, 1, dseed, L_refine, L_refine,
+                              c->fg_ids.as<uint32_t>(), c->fg_deg.as<uint32_t>(), w, vis, one + 1,
+                              n + L_refine + 64, one, 1);
+    if (rc) return rc;
+    uint32_t nv = 0;
+    WV_CUDA(c, cudaMemcpyAsync(&nv, one + 1, 4, cudaMemcpyDeviceToHost, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    rc = check_device_status(c, "conn search");
+    if (rc) return rc;
+    // fullset = the expansion visits (the seeds are not part of it)
+    hv.resize(nv > L_refine ? nv - L_refine : 0);
+    if (!hv.empty())
+      WV_CUDA(c, cudaMemcpy(hv.data(), vis + L_refine, hv.size() * sizeof(DI), cudaMemcpyDeviceToHost));
+    stl::sort(hv.data(), (int)hv.size(), DILess());
+    bool found = false;
+    for (auto &x : hv)
+      if (flag[x.i]) {
+        root = x.i;
+        found = true;
+        break;
+      }
+    if (!found) {
+      while (true) {
+        uint32_t rid = (uint32_t)c->rnd.next() % n;
+        if (flag[rid]) {
+          root = rid;
+          break;
+        }
+      }
+    }
+    k_pair_l2<<<1, 32, 0, c->stream>>>(c->base.as<float>(), c->d, root, id, dd);
+    float h = 0;
+    WV_CUDA(c, cudaMemcpyAsync(&h, dd, 4, cudaMemcpyDeviceToHost, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (deg[root] == w) {
+      rc = relayout(w + 16);
+      if (rc) return rc;
+    }
+    const uint32_t pos = deg[root]++;
+    ids[(size_t)root * w + pos] = id;
+    dist[(size_t)root * w + pos] = h;
+    WV_CUDA(c, cudaMemcpyAsync(c->fg_ids.as<uint32_t>() + (size_t)root * w + pos, &id, 4, cudaMemcpyHostToDevice,
+                               c->stream));
+    WV_CUDA(c, cudaMemcpyAsync(c->fg_dist.as<float>() + (size_t)root * w + pos, &h, 4, cudaMemcpyHostToDevice,
+                               c->stream));
+    WV_CUDA(c, cudaMemcpyAsync(c->fg_deg.as<uint32_t>() + root, &deg[root], 4, cudaMemcpyHostToDevice, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    (*added)++;
+  }
+  if (widened) {  // trim to the widest row
+    uint32_t nw = 1;
+    for (uint32_t v = 0; v < n; v++) nw = std::max(nw, deg[v]);
+    if (nw != w) {
+      int rc = relayout(nw);
+      if (rc) return rc;
+    }
+  }
+  return WV_OK;
+}
+
+}  // namespace wv

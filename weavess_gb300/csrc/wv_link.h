@@ -1,0 +1,29 @@
+// Vamana / NSG link on the GPU (REFINE_VAMANA, REFINE_NSG).
+#pragma once
+#include <cstdint>
+
+#include "wv_ctx.h"
+
+namespace wv {
+
+struct LinkParams {
+  uint32_t L;        // L_refine: beam of the candidate searches
+  uint32_t R;        // R_refine: row width
+  uint32_t C;        // C_refine: candidates examined by the NSG prune
+  float alpha;       // Vamana occlusion factor (ignored by NSG)
+  uint32_t entry_L;  // the index's L_refine member read by the entry search (0: ep_ = 0)
+  bool nsg;          // NSG prune / re-prune, else Vamana
+};
+
+struct LinkStats {
+  uint32_t ep = 0;
+  uint32_t levels = 0;  // InterInsert dependency levels
+  float ms = 0;
+};
+
+// Link on ctx->fg_* (candidate graph) -> ctx->fg_* (rows of width R, ep set)
+int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st);
+// ComponentConnNSGDFS on ctx->fg_* (may widen the rows)
+int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added);
+
+}  // namespace wv

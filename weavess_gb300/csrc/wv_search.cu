@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
       if (lane < cnt) {
         s.pa_d[b + lane] = dist;
         s.pa_i[b + lane] = id;
-        if (BUILD && nvis + lane < a.vcap) vis_out[nvis + lane] = DI{dist, id};
+        if (BUILD && nvis + lane < a.vlimit) vis_out[nvis + lane] = DI{dist, id};
       }
       nvis += cnt;
     }
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
         float dist = warp_l2_rows(a.base, a.d, my, cnt, s.qv, s.stage, lane);
         dcount += cnt;
         if (BUILD) {
-          if (lane < cnt && nvis + lane < a.vcap) vis_out[nvis + lane] = DI{dist, my};
+          if (lane < cnt && nvis + lane < a.vlimit) vis_out[nvis + lane] = DI{dist, my};
           nvis += cnt;
         }
         bool acc = false;
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
     if (BUILD) {
       if (lane == 0) {
         a.vcnt[q] = nvis;
-        if (nvis > a.vcap) set_err(a.status, DEV_OVERFLOW);
+        if (nvis > a.vlimit) set_err(a.status, DEV_OVERFLOW);
       }
       if (a.out_ids)
         for (int i = lane; i < K; i += 32) {

@@ -34,7 +34,8 @@ struct SearchArgs {
   // candidate-search (build) mode: visit lists, vcap entries per query
   ::wv::DI *vis;
   uint32_t *vcnt;
-  uint32_t vcap;
+  uint32_t vcap;    // stride between queries' visit lists
+  uint32_t vlimit;  // entries recorded per query (<= vcap)
 };
 
 constexpr uint32_t SEARCH_MAX_WIDTH = 256;  // graph row width the kernel accepts

@@ -101,6 +101,16 @@ class Context:
         self._check(self.L.wv_nnd_refine(self.h, S, K, L, ITER, R, C.byref(st)))
         return st.as_dict()
 
+    def vamana_refine(self, L_refine: int, R_refine: int, alpha: float, entry_L: int = 0):
+        st = _lib.BuildStats()
+        self._check(self.L.wv_vamana_refine(self.h, L_refine, R_refine, alpha, entry_L, C.byref(st)))
+        return st.as_dict()
+
+    def nsg_refine(self, L_refine: int, R_refine: int, C_refine: int):
+        st = _lib.BuildStats()
+        self._check(self.L.wv_nsg_refine(self.h, L_refine, R_refine, C_refine, C.byref(st)))
+        return st.as_dict()
+
     # -- search (IndexBuilder::search, L_SEARCH_ASSIGN)
     def search(self, queries, L: int, K: int = 10, entry="rand", return_dist=False):
         q = _f32(queries)
