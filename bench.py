@@ -117,8 +117,7 @@ def build_index(ctx, base, cfg):
     st0 = ctx.init_random(cfg["S"])
     st1 = ctx.nnd_refine(cfg["S"], cfg["K"], cfg["L"], cfg["ITER"], cfg["R"])
     stages = {"init_random": st0, "nndescent": st1}
-    if hasattr(ctx, "vamana_refine"):
-        stages["vamana"] = ctx.vamana_refine(cfg["L_refine"], cfg["R_refine"], cfg["alpha"])
+    stages["vamana"] = ctx.vamana_refine(cfg["L_refine"], cfg["R_refine"], cfg["alpha"], 0)
     ctx.load_built_graph()
     torch.cuda.synchronize()
     return time.time() - t0, stages
@@ -144,7 +143,7 @@ def run_ours(args):
     from weavess_gb300.groundtruth import knn_fp64
     cfg = dict(CFG)
     if args.small:
-        cfg.update(n=100_000, centers=64, nq=1000, S=10, K=20, L=40, ITER=8, R=100, R_refine=32)
+        cfg.update(n=100_000, centers=64, nq=1000, S=10, K=32, L=40, ITER=8, R=100, R_refine=32, L_refine=32)
     dev = torch.device("cuda:0")
     torch.cuda.set_device(dev)
     base, query = make_data(cfg)
