@@ -145,6 +145,19 @@ int wv_search_batch(wv_ctx *ctx, const float *queries, uint32_t nq, int entry, c
 int wv_search_device(wv_ctx *ctx, const float *d_queries, uint32_t nq, uint32_t L, uint32_t K,
                      const uint32_t *d_seeds, uint32_t *d_out_ids, float *d_out_dist, wv_counters *counters);
 
+/* Low-precision candidate distances (not in the reference).  Builds a copy of
+ * the uploaded base in bf16, or in fp8 e4m3 with one FP32 scale per row
+ * (max |x| / 448), and makes every later search compute candidate distances
+ * from it (FP32 accumulation), then re-score the first `rerank` entries of
+ * each final pool exactly in FP32 (0 = the whole pool) and re-sort them before
+ * the top K are returned.  WV_STORE_FP32 restores the plain form. */
+typedef enum { WV_STORE_FP32 = 0, WV_STORE_BF16 = 1, WV_STORE_FP8 = 2 } wv_storage;
+int wv_set_search_precision(wv_ctx *ctx, int storage, uint32_t rerank);
+/* Candidate distances of the current precision for nq host queries against
+ * m base ids each (ids nq x m): out nq x m (to measure the error). */
+int wv_candidate_distances(wv_ctx *ctx, const float *queries, uint32_t nq, const uint32_t *ids, uint32_t m,
+                           float *out);
+
 /* The seed ids SearchEntryInner would draw for nq queries (host nq x L),
  * consuming the context's rand stream exactly as the reference does. */
 int wv_draw_seeds(wv_ctx *ctx, uint32_t nq, int entry, uint32_t L, uint32_t *seeds);

@@ -81,6 +81,8 @@ def load(build_if_needed: bool = True):
                                 C.POINTER(BuildStats)]
     L.wv_vamana_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, C.POINTER(BuildStats)]
     L.wv_nsg_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(BuildStats)]
+    L.wv_set_search_precision.argtypes = [vp, C.c_int, C.c_uint32]
+    L.wv_candidate_distances.argtypes = [vp, f32p, C.c_uint32, u32p, C.c_uint32, f32p]
     L.wv_debug_sort.argtypes = [vp, f32p, u32p, u32p, C.c_uint32, C.c_int]
     L.wv_search_noalloc.argtypes = [vp, C.c_uint32, C.c_uint32, vp, vp, C.c_uint32, vp, C.c_uint32, vp, C.c_uint32,
                                     C.c_uint32, vp, vp, vp]

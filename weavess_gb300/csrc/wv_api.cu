@@ -27,6 +27,16 @@ int check_device_status(wv_ctx *c, const char *what) {
 
 namespace {
 
+__global__ void k_check_int(const float *x, size_t count, int *ok) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+    const float v = x[i];
+    if (!(v >= 0.f && v <= 255.f && v == rintf(v))) {
+      *ok = 0;
+      return;
+    }
+  }
+}
+
 int ensure_search_scratch(wv_ctx *c, uint32_t Lmax) {
   const uint32_t cap = c->gw + 32;
   int blocks = search_grid(c->d, Lmax, cap, c->device);
@@ -79,6 +89,11 @@ int run_search(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t *d_seeds
   a.cap = c->gw + 32;
   a.next_query = c->d_next();
   a.status = c->d_status();
+  a.int_exact = c->base_int;
+  a.storage = c->storage;
+  a.qbase = c->qbase.p;
+  a.qscale = c->qscale.as<float>();
+  a.rerank = c->rerank == 0 ? Lmax : c->rerank;
   int nb = std::min<long>(blocks, ((long)nq + search_warps_per_block() - 1) / search_warps_per_block());
   if (nb < 1) nb = 1;
   WV_CUDA(c, launch_search_exact(a, nb, c->stream));
@@ -150,7 +165,7 @@ int wv_ctx_destroy(wv_ctx *c) {
   cudaStreamSynchronize(c->stream);
   for (DevBuf *b : {&c->base, &c->gids, &c->gdeg, &c->visited, &c->touched, &c->misc, &c->q_buf, &c->seed_buf,
                     &c->out_ids_buf, &c->out_dist_buf, &c->lq_buf, &c->kq_buf, &c->fg_ids, &c->fg_dist,
-                    &c->fg_deg})
+                    &c->fg_deg, &c->qbase, &c->qscale})
     b->release();
   c->release_work();
   cudaStreamDestroy(c->own_stream);
@@ -195,8 +210,17 @@ int wv_upload_base(wv_ctx *c, const float *base, uint32_t n, uint32_t d) {
   WV_CUDA(c, cudaMemcpyAsync(c->base.p, base, (size_t)n * d * 4, cudaMemcpyHostToDevice, c->stream));
   WV_CUDA(c, cudaStreamSynchronize(c->stream));
   if (c->n != n) c->gn = 0;  // the old graph no longer matches
+  c->storage = 0;            // a low-precision copy no longer matches
   c->n = n;
   c->d = d;
+  int *ok = c->d_status() + 4;
+  int one = 1, hok = 0;
+  WV_CUDA(c, cudaMemcpyAsync(ok, &one, 4, cudaMemcpyHostToDevice, c->stream));
+  k_check_int<<<c->sms * 8, 256, 0, c->stream>>>(c->base.as<float>(), (size_t)n * d, ok);
+  WV_CUDA(c, cudaGetLastError());
+  WV_CUDA(c, cudaMemcpyAsync(&hok, ok, 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->base_int = hok == 1;
   return WV_OK;
 }
 

@@ -52,6 +52,11 @@ struct wv_ctx {
   // base vectors
   wv::DevBuf base;
   uint32_t n = 0, d = 0;
+  bool base_int = false;  // every value an integer in [0, 255]
+  // low-precision copy of the base for candidate distances
+  int storage = 0;
+  uint32_t rerank = 0;
+  wv::DevBuf qbase, qscale;
 
   // search graph (load_graph_)
   wv::DevBuf gids, gdeg;

@@ -274,63 +274,120 @@ struct HeapIdxLess {
   __device__ bool operator()(const HeapIdx &a, const HeapIdx &b) const { return a.key > b.key; }
 };
 
+// per-warp state: the row (with the slot holding each entry's vector), the
+// re-prune scratch, and -- in the dynamic tail -- the pairwise distances of
+// the slot vectors (S x S, S = R + 1) and the vectors themselves (S rows)
 struct IIWarp {
   Ent3 row[II_SLOTS];
   Ent3 tmp[II_SLOTS];
-  uint32_t sid[II_SLOTS];     // id held by each slot
-  float D[II_SLOTS][II_SLOTS];  // pairwise distances of slot vectors
+  uint32_t sid[II_SLOTS];  // id held by each slot
   uint32_t res[II_SLOTS];
   HeapIdx heap[II_SLOTS];
+  float *D;                // S x S
+  float *V;                // S x vs floats, or null: distances from global memory
 };
+
+__host__ __device__ inline size_t ii_warp_bytes(uint32_t R, uint32_t vs) {
+  const size_t S = R + 1;
+  return ((sizeof(IIWarp) + 15) & ~size_t(15)) + ((S * S * 4 + 15) & ~size_t(15)) + S * vs * 4;
+}
+
+__device__ inline IIWarp &ii_carve(uint8_t *smem, int warp, uint32_t R, uint32_t vs) {
+  uint8_t *p = smem + (size_t)warp * ii_warp_bytes(R, vs);
+  IIWarp &w = *reinterpret_cast<IIWarp *>(p);
+  p += (sizeof(IIWarp) + 15) & ~size_t(15);
+  w.D = reinterpret_cast<float *>(p);
+  p += ((size_t)(R + 1) * (R + 1) * 4 + 15) & ~size_t(15);
+  w.V = vs ? reinterpret_cast<float *>(p) : nullptr;
+  return w;
+}
+
+// copies base row `id` into vector slot f (one warp, 16-byte pieces)
+__device__ __forceinline__ void ii_stage(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t f, uint32_t id, int lane) {
+  if (!w.V) return;
+  const float4 *src = reinterpret_cast<const float4 *>(a.base + (size_t)id * a.d);
+  float4 *dst = reinterpret_cast<float4 *>(w.V + (size_t)f * vs);
+  for (uint32_t k = lane; k < (a.d >> 2); k += 32) dst[k] = __ldg(src + k);
+}
+
+// exact-order distance between the vectors of slots x and y
+__device__ __forceinline__ float ii_dist(const IIArgs &a, const IIWarp &w, uint32_t vs, uint32_t x, uint32_t y) {
+  if (!w.V) return l2g(a.base, a.d, w.sid[x], w.sid[y]);
+  const float4 *p = reinterpret_cast<const float4 *>(w.V + (size_t)x * vs);
+  const float4 *q = reinterpret_cast<const float4 *>(w.V + (size_t)y * vs);
+  float acc = 0.f;
+  const uint32_t d4 = a.d >> 2;
+#pragma unroll 4
+  for (uint32_t g = 0; g < d4; g++) acc = __fadd_rn(acc, group4(p[g], q[g]));
+  return acc;
+}
+
+// gives row entry j (slot INVALID) a free slot, its vector and its distance
+// column to the other slotted entries (dvalid rows only)
+__device__ void ii_slot_entry(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t rs, uint32_t j, int lane) {
+  const uint32_t S = a.R + 1;
+  unsigned long long used = 0;
+  for (uint32_t t = 0; t < rs; t++)
+    if (t != j) used |= 1ull << w.row[t].slot;
+  const uint32_t f = __ffsll(~used) - 1;
+  if (lane == 0) {
+    w.row[j].slot = f;
+    w.sid[f] = w.row[j].i;
+  }
+  __syncwarp();
+  ii_stage(a, w, vs, f, w.row[j].i, lane);
+  __syncwarp();
+  for (uint32_t t = lane; t < rs; t += 32) {
+    if (t == j) continue;
+    const uint32_t o = w.row[t].slot;
+    const float dd = ii_dist(a, w, vs, o, f);
+    w.D[f * S + o] = dd;
+    w.D[o * S + f] = dd;
+  }
+  __syncwarp();
+}
 
 // applies "insert `s` (distance dist, sender index i) into this row" exactly
 // as InterInsert does to des_pool (component_refine.cpp:484-540 / 884-949)
-__device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t &rs, bool &dvalid, uint32_t s, float dist, uint32_t i,
-                         int lane) {
+__device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t &rs, bool &dvalid, uint32_t s, float dist,
+                         uint32_t i, int lane) {
   bool dup = false;
   for (uint32_t j = lane; j < rs; j += 32) dup |= w.row[j].i == s;
   if (__any_sync(FULL, dup)) return;
-  const uint32_t R = a.R;
-  if (rs + 1 <= R) {  // room: append
+  const uint32_t R = a.R, S = R + 1;
+  if (rs + 1 <= R) {  // room: append at the sentinel
     if (lane == 0) w.row[rs] = Ent3{dist, s, INVALID};
-    rs++;
-    dvalid = false;  // slots assigned lazily at the next re-prune
     __syncwarp();
+    if (dvalid) ii_slot_entry(a, w, vs, rs + 1, rs, lane);
+    rs++;
     return;
   }
-  // re-prune needs the pairwise distances of row + s
+  // a re-prune needs the pairwise distances of row + s
   if (!dvalid) {
-    // (re)assign slots 0..rs-1 to the row and fill the whole matrix
     for (uint32_t j = lane; j < rs; j += 32) {
       w.row[j].slot = j;
       w.sid[j] = w.row[j].i;
     }
     __syncwarp();
+    for (uint32_t j = 0; j < rs; j++) ii_stage(a, w, vs, j, w.row[j].i, lane);
+    __syncwarp();
     for (uint32_t p = lane; p < rs * rs; p += 32) {
-      uint32_t x = p / rs, y = p % rs;
+      const uint32_t x = p / rs, y = p % rs;
       if (x < y) {
-        float dd = l2g(a.base, a.d, w.sid[x], w.sid[y]);
-        w.D[x][y] = dd;
-        w.D[y][x] = dd;
+        const float dd = ii_dist(a, w, vs, x, y);
+        w.D[x * S + y] = dd;
+        w.D[y * S + x] = dd;
       }
     }
     dvalid = true;
     __syncwarp();
   }
-  // a free slot for s (the row uses rs <= R of R + 1 slots)
-  unsigned long long used = 0;
-  for (uint32_t j = 0; j < rs; j++) used |= 1ull << w.row[j].slot;
-  uint32_t f = __ffsll(~used) - 1;
-  if (lane == 0) w.sid[f] = s;
+  // s takes the free slot (the row holds at most R of the R + 1 slots)
+  if (lane == 0) w.row[rs] = Ent3{dist, s, INVALID};
   __syncwarp();
-  for (uint32_t j = lane; j < rs; j += 32) {
-    float dd = l2g(a.base, a.d, w.row[j].i, s);
-    w.D[f][w.row[j].slot] = dd;
-    w.D[w.row[j].slot][f] = dd;
-  }
+  ii_slot_entry(a, w, vs, rs + 1, rs, lane);
   const uint32_t T = rs + 1;
-  for (uint32_t j = lane; j < rs; j += 32) w.tmp[j] = w.row[j];
-  if (lane == 0) w.tmp[rs] = Ent3{dist, s, f};
+  for (uint32_t j = lane; j < T; j += 32) w.tmp[j] = w.row[j];
   __syncwarp();
   if (lane == 0) stl::sort(w.tmp, (int)T, Ent3Less());
   __syncwarp();
@@ -341,7 +398,7 @@ __device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t &rs, bool &dvalid,
     for (int k = (int)T - 1; k >= 0; --k) {
       const uint32_t ks = w.tmp[k].slot;
       bool hit = false;
-      for (uint32_t j = lane; j < nres; j += 32) hit |= __fmul_rn(a.alpha, w.D[w.tmp[w.res[j]].slot][ks]) < cur;
+      for (uint32_t j = lane; j < nres; j += 32) hit |= __fmul_rn(a.alpha, w.D[w.tmp[w.res[j]].slot * S + ks]) < cur;
       const bool skip = __any_sync(FULL, hit);
       if (!skip) {
         if (lane == 0) w.res[nres] = (uint32_t)k;
@@ -377,7 +434,7 @@ __device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t &rs, bool &dvalid,
       bool occ = false;
       for (uint32_t j = lane; j < nres; j += 32) {
         const Ent3 r = w.tmp[w.res[j]];
-        occ |= (r.i == p.i) || (w.D[r.slot][p.slot] < p.d);
+        occ |= (r.i == p.i) || (w.D[r.slot * S + p.slot] < p.d);
       }
       if (!__any_sync(FULL, occ)) {
         if (lane == 0) w.res[nres] = st;
@@ -403,10 +460,10 @@ __device__ void ii_load_row(IIWarp &w, const uint32_t *ids, const float *dist, u
 
 // forward: each node of this level applies the insertions from lower ids
 // (senders m < n whose row at their turn lists n), then snapshots its row
-__global__ void __launch_bounds__(II_WARPS * 32) k_ii_forward(IIArgs a) {
+__global__ void __launch_bounds__(II_WARPS * 32) k_ii_forward(IIArgs a, uint32_t vs) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  IIWarp &w = reinterpret_cast<IIWarp *>(smem)[warp];
+  IIWarp &w = ii_carve(smem, warp, a.R, vs);
   for (uint32_t t = blockIdx.x * II_WARPS + warp; t < a.nn; t += gridDim.x * II_WARPS) {
     const uint32_t n = a.nodes[t];
     uint32_t rs = a.p_deg[n];
@@ -424,7 +481,7 @@ __global__ void __launch_bounds__(II_WARPS * 32) k_ii_forward(IIArgs a) {
         while (hits) {
           const uint32_t pos = b + __ffs(hits) - 1;
           hits &= hits - 1;
-          ii_apply(a, w, rs, dvalid, m, a.s_dist[(size_t)m * a.R + pos], pos, lane);
+          ii_apply(a, w, vs, rs, dvalid, m, a.s_dist[(size_t)m * a.R + pos], pos, lane);
         }
       }
     }
@@ -438,10 +495,10 @@ __global__ void __launch_bounds__(II_WARPS * 32) k_ii_forward(IIArgs a) {
 }
 
 // backward: every row applies the insertions from higher ids in id order
-__global__ void __launch_bounds__(II_WARPS * 32) k_ii_backward(IIArgs a) {
+__global__ void __launch_bounds__(II_WARPS * 32) k_ii_backward(IIArgs a, uint32_t vs) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  IIWarp &w = reinterpret_cast<IIWarp *>(smem)[warp];
+  IIWarp &w = ii_carve(smem, warp, a.R, vs);
   for (uint32_t r = blockIdx.x * II_WARPS + warp; r < a.n; r += gridDim.x * II_WARPS) {
     uint32_t rs = a.s_deg[r];
     ii_load_row(w, a.s_ids + (size_t)r * a.R, a.s_dist + (size_t)r * a.R, rs, lane);
@@ -450,7 +507,7 @@ __global__ void __launch_bounds__(II_WARPS * 32) k_ii_backward(IIArgs a) {
     for (uint32_t q = 0; q < cnt; q++) {
       const unsigned long long key = a.req[off + q];
       const uint32_t m = (uint32_t)(key >> 32), pos = (uint32_t)key;
-      ii_apply(a, w, rs, dvalid, m, a.s_dist[(size_t)m * a.R + pos], pos, lane);
+      ii_apply(a, w, vs, rs, dvalid, m, a.s_dist[(size_t)m * a.R + pos], pos, lane);
     }
     for (uint32_t j = lane; j < rs; j += 32) {
       a.f_ids[(size_t)r * a.R + j] = w.row[j].i;
@@ -569,6 +626,7 @@ int run_build_search(wv_ctx *c, const float *d_queries, uint32_t nq, const uint3
   a.vcnt = vcnt;
   a.vcap = vcap;
   a.vlimit = vlimit;
+  a.int_exact = c->base_int;
   int nb = (int)std::min<size_t>((size_t)blocks, ((size_t)nq + search_warps_per_block() - 1) / search_warps_per_block());
   WV_CUDA(c, launch_search_exact(a, std::max(nb, 1), c->stream));
   return WV_OK;
@@ -774,7 +832,10 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
   ia.req_off = roff;
   ia.req_cnt = rcnt;
   ia.status = c->d_status();
-  const size_t ii_smem = II_WARPS * sizeof(IIWarp);
+  // row vectors in shared memory when they fit, else read from global memory
+  uint32_t vs = ((c->d + 3) & ~3u) + 4;
+  if (II_WARPS * ii_warp_bytes(R, vs) > 200 * 1024) vs = 0;
+  const size_t ii_smem = II_WARPS * ii_warp_bytes(R, vs);
   WV_CUDA(c, cudaFuncSetAttribute(k_ii_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ii_smem));
   WV_CUDA(c, cudaFuncSetAttribute(k_ii_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ii_smem));
   WV_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -784,7 +845,7 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
     ia.nodes = order + hloff[t];
     ia.nn = cnt;
     const int blocks = (int)std::min<uint32_t>((cnt + II_WARPS - 1) / II_WARPS, (uint32_t)c->sms * 16);
-    k_ii_forward<<<blocks, II_WARPS * 32, ii_smem, c->stream>>>(ia);
+    k_ii_forward<<<blocks, II_WARPS * 32, ii_smem, c->stream>>>(ia, vs);
   }
   WV_CUDA(c, cudaGetLastError());
   // backward request lists from the snapshots, sorted by sender
@@ -802,7 +863,7 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
   ia.f_ids = c->fg_ids.as<uint32_t>();
   ia.f_dist = c->fg_dist.as<float>();
   ia.f_deg = c->fg_deg.as<uint32_t>();
-  k_ii_backward<<<c->sms * 16, II_WARPS * 32, ii_smem, c->stream>>>(ia);
+  k_ii_backward<<<c->sms * 16, II_WARPS * 32, ii_smem, c->stream>>>(ia, vs);
   WV_CUDA(c, cudaGetLastError());
   rc = check_device_status(c, "inter-insert");
   if (rc) return rc;

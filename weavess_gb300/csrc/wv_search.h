@@ -36,6 +36,17 @@ struct SearchArgs {
   uint32_t *vcnt;
   uint32_t vcap;    // stride between queries' visit lists
   uint32_t vlimit;  // entries recorded per query (<= vcap)
+  // every base value is an integer in [0, 255]: queries that are too get
+  // their distances by a warp reduction (exact in any order)
+  int int_exact;
+  // candidate distances from a low-precision copy of the base (0: the FP32
+  // base; 1: bf16 rows; 2: fp8 e4m3 rows with a per-row FP32 scale), FP32
+  // accumulation; the first `rerank` pool entries are then re-scored exactly
+  // in FP32 and re-sorted before the top K are written
+  int storage;
+  const void *qbase;
+  const float *qscale;
+  uint32_t rerank;
 };
 
 constexpr uint32_t SEARCH_MAX_WIDTH = 256;  // graph row width the kernel accepts

@@ -140,6 +140,20 @@ class Context:
         self._check(self.L.wv_search_batch(self.h, q, nq, ENTRY[entry], L, K, stride, out, None, C.byref(cnt)))
         return out, int(cnt.dist_count), int(cnt.hop_count)
 
+    STORAGE = {"fp32": 0, "bf16": 1, "fp8": 2}
+
+    def set_precision(self, storage: str = "fp32", rerank: int = 0):
+        """Candidate distances from a bf16 / fp8 copy of the base, exact FP32
+        rerank of the first `rerank` pool entries (0 = whole pool)."""
+        self._check(self.L.wv_set_search_precision(self.h, self.STORAGE[storage], rerank))
+
+    def candidate_distances(self, queries, ids):
+        q = _f32(queries)
+        ids = _u32(ids)
+        out = np.zeros(ids.shape, np.float32)
+        self._check(self.L.wv_candidate_distances(self.h, q, q.shape[0], ids, ids.shape[1], out))
+        return out
+
     def draw_seeds(self, nq: int, L: int, entry="rand"):
         out = np.zeros((nq, L), np.uint32)
         self._check(self.L.wv_draw_seeds(self.h, nq, ENTRY[entry], L, out))
