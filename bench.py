@@ -37,7 +37,8 @@ from weavess_gb300 import datasets as ds  # noqa: E402
 
 CFG = dict(n=1_000_000, d=128, centers=256, nq=10_000, seed=7, S=20, K=64, L=80, ITER=8, R=100,
            R_refine=32, L_refine=64, C_refine=500, k=10, target_recall=0.95,
-           L_grid=[10, 16, 20, 24, 32, 40, 48, 64, 80, 96, 128, 160, 192, 224, 256, 300])
+           L_grid=[16, 24, 32, 48, 64, 96, 128, 160, 192, 256, 320, 384, 448, 512, 640, 768, 896, 1024, 1280,
+                   1536])
 METRIC = "QPS at recall@10>=0.95 (plain FP32 greedy search, 1M x 128)"
 
 
@@ -147,6 +148,8 @@ def run_ours(args):
     cfg = dict(CFG)
     if args.small:
         cfg.update(n=100_000, centers=64, nq=1000, S=10, K=32, L=40, ITER=8, R=100, R_refine=32, L_refine=32)
+    if args.nq:
+        cfg["nq"] = args.nq
     dev = torch.device("cuda:0")
     torch.cuda.set_device(dev)
     base, query = make_data(cfg)
@@ -301,6 +304,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="N=1e5 configuration (quick check)")
+    ap.add_argument("--nq", type=int, default=0, help="override the number of queries")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
