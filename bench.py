@@ -37,9 +37,10 @@ from weavess_gb300 import datasets as ds  # noqa: E402
 
 CFG = dict(n=1_000_000, d=128, centers=256, nq=10_000, seed=7, S=20, K=64, L=80, ITER=8, R=100,
            R_refine=32, L_refine=64, C_refine=500, k=10, target_recall=0.95,
+           n_train=200_000, n_val=2000, clusters=64, L_trace=512, epochs=6,
            L_grid=[16, 24, 32, 48, 64, 96, 128, 160, 192, 256, 320, 384, 448, 512, 640, 768, 896, 1024, 1280,
                    1536])
-METRIC = "QPS at recall@10>=0.95 (plain FP32 greedy search, 1M x 128)"
+METRIC = "QPS at recall@10>=0.95 (learned+BF16 vs plain FP32, 1 GB300); build sec"
 
 
 def log(*a):
@@ -141,13 +142,80 @@ def cpu_search_qps(base, query, g_ids, g_deg, L, threads, sample):
     return sample / dt, dt, res
 
 
+def run_learned(ctx, cfg, base, query, gt, args, dev, stream, flush):
+    """Learned entry point and beam width (trained on plain-search traces of
+    queries disjoint from the evaluation set), bf16 candidate distances with an
+    exact FP32 rerank.  The beam margin is calibrated to recall@10 >= target on
+    held-out validation queries (exact ground truth), then the evaluation
+    queries are timed like the plain search."""
+    import torch
+    from weavess_gb300.groundtruth import knn_fp64
+    nt, nval = cfg["n_train"], cfg["n_val"]
+    _, tq = ds.int_mixture(0, cfg["d"], cfg["centers"], seed=cfg["seed"], n_query=nt + nval, query_stream=3)
+    train, val = tq[:nt], tq[nt:]
+    t = time.time()
+    rep = ctx.learn_fit(train, clusters=cfg["clusters"], L_trace=cfg["L_trace"], L_max=cfg["L_trace"],
+                        list_len=cfg["L_trace"], epochs=cfg["epochs"], batch=1024)
+    fit_s = time.time() - t
+    log(f"learn_fit {fit_s:.1f}s {rep}")
+    gtv = knn_fp64(base, val, 10)
+    ctx.set_precision("bf16", rerank=0)
+    margin = rep["margin"]
+    chosen = None
+    for m in [margin * f for f in (1.0, 1.25, 1.5, 2.0, 2.5, 3.0, 4.0, 6.0, 8.0)]:
+        ctx.learn_set_margin(m)
+        ctx.srand(4321)
+        rv, _, _ = ctx.search_learned(val, cfg["k"])
+        r = recall(rv, gtv, cfg["k"])
+        log(f"margin {m:.2f} val recall {r:.4f}")
+        chosen = m
+        if r >= cfg["target_recall"] + 0.005:
+            break
+    ctx.learn_set_margin(chosen)
+    nq, K = query.shape[0], cfg["k"]
+    ctx.srand(777)
+    pseeds = ctx.draw_seeds(nq, cfg["L_trace"], "rand")
+    dq = torch.from_numpy(query).to(dev)
+    dps = torch.from_numpy(pseeds.astype(np.int32)).to(dev)
+    dout = torch.empty((nq, K), dtype=torch.int32, device=dev)
+    counters = None
+    for _ in range(args.warmup):
+        counters = ctx.search_learned_device(dq.data_ptr(), nq, K, dps.data_ptr(), dout.data_ptr(), counters=True)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        ctx.search_learned_device(dq.data_ptr(), nq, K, dps.data_ptr(), dout.data_ptr())
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    res = dout.cpu().numpy().astype(np.uint32)
+    r_test = recall(res, gt, K)
+    # e2e through the public host-buffer call
+    qpin = torch.from_numpy(query).pin_memory().numpy()
+    ctx.search_learned(qpin, K)
+    e2e_t = []
+    Ls = None
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, _, _, Ls = ctx.search_learned(qpin, K, return_L=True)
+        e2e_t.append(time.perf_counter() - t0)
+    ctx.set_precision("fp32")
+    dc, hc = counters
+    return {"qps": nq / (ms / 1e3), "ms": ms, "recall@10": r_test, "e2e_qps": nq / float(np.mean(e2e_t)),
+            "margin": chosen, "mean_L": float(Ls.mean()), "fit_s": fit_s, "report": rep, "dist_count": dc,
+            "hop_count": hc, "n_train": nt}
+
+
 def run_ours(args):
     import torch
     from weavess_gb300 import Context
     from weavess_gb300.groundtruth import knn_fp64
     cfg = dict(CFG)
     if args.small:
-        cfg.update(n=100_000, centers=64, nq=1000, S=10, K=32, L=40, ITER=8, R=100, R_refine=32, L_refine=32)
+        cfg.update(n=100_000, centers=64, nq=1000, S=10, K=32, L=40, ITER=8, R=100, R_refine=32, L_refine=32,
+                   n_train=40_000, clusters=32, L_trace=256)
     if args.nq:
         cfg["nq"] = args.nq
     dev = torch.device("cuda:0")
@@ -220,31 +288,59 @@ def run_ours(args):
         out, _, _ = ctx.search(qpin, Lsel, K, entry="rand")
         e2e_t.append(time.perf_counter() - t0)
     e2e_qps = nq / float(np.mean(e2e_t))
+    # ---- learned entry / beam + bf16 candidate distances
+    learned = None
+    if not args.no_learned:
+        learned = run_learned(ctx, cfg, base, query, gt, args, dev, stream, flush)
     # ---- CPU baseline: the oracle on the host cores, bounded sample
     threads = os.cpu_count() or 1
     sample = 2000 if not args.small else 1000
     cpu_qps, cpu_dt, _ = cpu_search_qps(base, query, g_ids, g_deg, Lsel, threads, sample)
+    plain = {"qps": round(value, 1), "ms_per_step": round(ms, 4), "L_search": Lsel, "recall@10": round(r_dev, 4),
+             "recall_sweep": sweep, "e2e_qps": round(e2e_qps, 1), "dist_count": dc, "hop_count": hc}
+    if learned is not None:
+        head_qps, head_ms, head_e2e = learned["qps"], learned["ms"], learned["e2e_qps"]
+        ldc, lhc = learned["dist_count"], learned["hop_count"]
+        # bf16 candidate rows (2d bytes), graph rows, query rows
+        alg = ldc * d * 2 + lhc * (avg_deg * 4 + 4) + nq * d * 4
+        l_achieved = alg / (head_ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": round(l_achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(l_achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
+                "alg_bytes_per_launch": int(alg), "dist_count": ldc, "hop_count": lhc,
+                "kernel": "k_search (learned seeds, per-query L, bf16 candidate rows)"}
+        h2d = nq * d * 4 + nq * cfg["L_trace"] * 4
+        launches = args.steps * 5  # 3 GEMMs + the seed kernel + the search per step
+    else:
+        head_qps, head_ms, head_e2e = value, ms, e2e_qps
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
+                "alg_bytes_per_launch": int(alg_bytes), "dist_count": dc, "hop_count": hc, "kernel": "k_search"}
+        h2d = nq * d * 4 + nq * Lsel * 4
+        launches = args.steps
     line = {
-        "metric": METRIC, "value": round(value, 1), "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded integer Gaussian mixture)",
+        "metric": METRIC, "value": round(head_qps, 1), "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(head_ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 candidates, f32 rerank" if learned else "f32",
+        "data": "synthetic (seeded integer Gaussian mixture)",
         "config": {"workload": f"{cfg['n']}x{cfg['d']} int-mixture({cfg['centers']}), {nq} queries, top-{K}, "
                                f"KGraph NN-Descent S={cfg['S']} K={cfg['K']} L={cfg['L']} ITER={cfg['ITER']} "
                                f"R={cfg['R']} -> NSG R={cfg['R_refine']} L_refine={cfg['L_refine']} "
                                f"C_refine={cfg['C_refine']}",
-                   "entry": "SEARCH_ENTRY_RAND", "L_search": Lsel, "recall@10": round(r_dev, 4),
-                   "recall_sweep": sweep, "l2": "flushed (256 MB write) between steps; base 512 MB > L2",
+                   "headline": "learned entry + beam, bf16 candidates" if learned else "plain FP32",
+                   "learned": ({k: (round(v, 4) if isinstance(v, float) else v) for k, v in learned.items()}
+                               if learned else None),
+                   "plain_fp32": plain,
+                   "speedup_vs_plain": round(head_qps / value, 3) if learned else 1.0,
+                   "l2": "flushed (256 MB write) between steps; base 512 MB > L2",
                    "build_s": round(build_s, 3),
                    "build_stages": {k: {kk: (round(vv, 2) if isinstance(vv, float) else vv) for kk, vv in v.items()}
                                     for k, v in stages.items()}},
-        "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": nq * d * 4 + nq * Lsel * 4,
+        "e2e": {"value": round(head_e2e, 1), "unit": "queries/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": nq * K * 4},
-        "gpu_launches": args.steps,
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
-                     "alg_bytes_per_launch": int(alg_bytes), "dist_count": dc, "hop_count": hc},
+        "gpu_launches": launches,
+        "roofline": roof,
         "cpu_baseline": {"value": round(cpu_qps, 1), "unit": "queries/s", "cores": threads, "kind": "port",
-                         "sample": f"first {sample} queries, same graph and L, oracle OpenMP search "
+                         "sample": f"first {sample} queries, same graph, plain search at L={Lsel}, oracle OpenMP "
                                    f"({cpu_dt:.2f}s)"},
         "clocks": clk.summary(),
     }
@@ -305,6 +401,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="N=1e5 configuration (quick check)")
     ap.add_argument("--nq", type=int, default=0, help="override the number of queries")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned + bf16 leg")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

@@ -158,6 +158,49 @@ int wv_set_search_precision(wv_ctx *ctx, int storage, uint32_t rerank);
 int wv_candidate_distances(wv_ctx *ctx, const float *queries, uint32_t nq, const uint32_t *ids, uint32_t m,
                            float *out);
 
+/* ---- learned entry point and beam width (not in the reference) ----------- */
+/* A small MLP (d -> 256 -> 256 -> `clusters` entry logits + 1 beam
+ * regressor, BF16 with FP32 accumulation) trained on the GPU by this
+ * library's own forward / backward kernels, on traces of the plain search:
+ * the cluster (k-means on the base) of each training query's plain answer is
+ * its entry label, and the smallest beam whose cluster-seeded answer keeps 9
+ * of the 10 plain ids its beam label.  The beam margin is calibrated on 10%
+ * of the training queries held out, to keep `target_agreement` of the plain
+ * answers.  Needs the base and the search graph. */
+typedef struct {
+  uint32_t clusters, kmeans_iters, list_len, L_trace, epochs, batch;
+  float lr, lam;
+  uint32_t L_min, L_max;
+  float target_agreement, fallback_p;
+  uint32_t seed;
+} wv_learn_params;
+typedef struct {
+  float loss_ce, loss_mse, margin, val_agreement, ms, mean_label_L;
+  uint32_t steps, labelled;
+} wv_learn_report;
+void wv_learn_default_params(wv_learn_params *p);
+int wv_learn_fit(wv_ctx *ctx, const float *train_queries, uint32_t nt, const wv_learn_params *p,
+                 wv_learn_report *report);
+/* Learned search: entry cluster(s) and beam per query from the model, the
+ * plain random-entry search (beam L_trace) for queries below fallback_p, all
+ * queries in one mixed-beam launch.  out_L (nullable): the beam each query
+ * used. */
+int wv_search_learned(wv_ctx *ctx, const float *queries, uint32_t nq, uint32_t K, uint32_t *out_ids, float *out_dist,
+                      wv_counters *counters, uint32_t *out_L);
+/* Same with device buffers; d_plain_seeds (nq x L_trace, drawn with
+ * wv_draw_seeds at L_trace) serve the fallback and fill short lists. */
+int wv_search_learned_device(wv_ctx *ctx, const float *d_queries, uint32_t nq, uint32_t K,
+                             const uint32_t *d_plain_seeds, uint32_t *d_out_ids, float *d_out_dist,
+                             wv_counters *counters);
+/* Overrides the calibrated beam margin (beam = margin * 2^regressor). */
+int wv_learn_set_margin(wv_ctx *ctx, float margin);
+/* Loss (ce, mse) and gradients of one batch for given parameters, for the
+ * gradient check; parameters packed as W1 (d x 256), b1, W2 (256 x 256), b2,
+ * W3 (256 x (clusters + 1)), b3.  Overwrites (and unsets) a trained model. */
+int wv_learn_param_count(uint32_t d, uint32_t clusters, unsigned long long *count);
+int wv_learn_grad(wv_ctx *ctx, const float *x, const uint32_t *y_cluster, const float *y_log2L, uint32_t B,
+                  uint32_t clusters, const float *params, float lam, float *grad, float *loss);
+
 /* The seed ids SearchEntryInner would draw for nq queries (host nq x L),
  * consuming the context's rand stream exactly as the reference does. */
 int wv_draw_seeds(wv_ctx *ctx, uint32_t nq, int entry, uint32_t L, uint32_t *seeds);

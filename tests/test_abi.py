@@ -21,3 +21,11 @@ def test_ctx_create_without_gpu_fails_cleanly():
     lib = _lib.load()
     h = ctypes.c_void_p()
     assert lib.wv_ctx_create(ctypes.byref(h), 0) != 0
+
+
+def test_library_has_no_unresolved_own_symbols():
+    import subprocess
+    path = build.build()
+    out = subprocess.run(["nm", "-D", "--undefined-only", path], capture_output=True, text=True).stdout
+    own = [l.split()[-1] for l in out.splitlines() if "wv" in l.split()[-1].lower() or "learn" in l]
+    assert not own, own

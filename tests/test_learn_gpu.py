@@ -1,0 +1,132 @@
+"""Learned entry / beam MLP: GPU gradients against an FP64 numpy restatement
+(same bf16 rounding points), and the gain of the learned search over the
+plain search at equal recall."""
+import numpy as np
+import pytest
+
+from weavess_gb300 import datasets as ds
+
+pytestmark = pytest.mark.gpu
+
+HID = 256
+
+
+def bf16(x):
+    """Round float32 to bfloat16 (nearest even), returned as float64."""
+    u = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def unpack(p, d, C):
+    o = 0
+    out = {}
+    for name, shape in (("W1", (d, HID)), ("b1", (HID,)), ("W2", (HID, HID)), ("b2", (HID,)),
+                        ("W3", (HID, C + 1)), ("b3", (C + 1,))):
+        n = int(np.prod(shape))
+        out[name] = p[o:o + n].reshape(shape).astype(np.float64)
+        o += n
+    return out
+
+
+def reference_grad(x, yc, yr, C, p, lam, rounding=True):
+    """FP64 forward/backward of the MLP; with `rounding`, operands rounded to
+    bf16 where the GPU rounds them."""
+    r = bf16 if rounding else (lambda v: np.asarray(v, np.float64))
+    d = x.shape[1]
+    P = unpack(p, d, C)
+    B = x.shape[0]
+    X = r(x)
+    H1 = np.maximum(X @ r(P["W1"]) + P["b1"], 0)
+    H1b = r(H1)
+    H2 = np.maximum(H1b @ r(P["W2"]) + P["b2"], 0)
+    H2b = r(H2)
+    O = H2b @ r(P["W3"]) + P["b3"]
+    z = O[:, :C] - O[:, :C].max(1, keepdims=True)
+    pr = np.exp(z) / np.exp(z).sum(1, keepdims=True)
+    ce = -np.log(pr[np.arange(B), yc]).mean()
+    mse = ((O[:, C] - yr) ** 2).mean()
+    dO = np.zeros_like(O)
+    dO[:, :C] = pr
+    dO[np.arange(B), yc] -= 1
+    dO[:, :C] /= B
+    dO[:, C] = 2 * lam * (O[:, C] - yr) / B
+    dOb = r(dO)
+    g = {"W3": H2b.T @ dOb, "b3": dO.sum(0)}
+    dZ2 = (dOb @ r(P["W3"]).T) * (H2 > 0)
+    dZ2b = r(dZ2)
+    g["W2"], g["b2"] = H1b.T @ dZ2b, dZ2.sum(0)
+    dZ1 = (dZ2b @ r(P["W2"]).T) * (H1 > 0)
+    dZ1b = r(dZ1)
+    g["W1"], g["b1"] = X.T @ dZ1b, dZ1.sum(0)
+    flat = np.concatenate([g[k].reshape(-1) for k in ("W1", "b1", "W2", "b2", "W3", "b3")])
+    return flat, ce, mse
+
+
+def test_reference_gradient_is_the_derivative():
+    """The FP64 restatement itself, without rounding, against central differences."""
+    rng = np.random.default_rng(0)
+    d, C, B = 6, 5, 7
+    n = d * HID + HID + HID * HID + HID + HID * (C + 1) + C + 1
+    p = rng.normal(0, 0.1, n)
+    x = rng.normal(size=(B, d))
+    yc = rng.integers(0, C, B)
+    yr = rng.normal(3, 1, B)
+    g, _, _ = reference_grad(x, yc, yr, C, p, 0.5, rounding=False)
+    idx = rng.choice(n, 40, replace=False)
+    for i in idx:
+        e = np.zeros(n)
+        e[i] = 1e-6
+        f = lambda q: sum(reference_grad(x, yc, yr, C, q, 0.5, rounding=False)[1:3][j] * (1, 0.5)[j] for j in (0, 1))
+        num = (f(p + e) - f(p - e)) / 2e-6
+        assert abs(num - g[i]) <= 1e-6 + 1e-4 * abs(num), (i, num, g[i])
+
+
+def test_gpu_gradients_match_fp64_oracle():
+    from weavess_gb300 import Context
+    import ctypes
+    d, C, B = 32, 12, 96
+    ctx = Context(0)
+    ctx.upload_base(np.zeros((64, d), np.float32))
+    cnt = ctypes.c_ulonglong()
+    assert ctx.L.wv_learn_param_count(d, C, ctypes.byref(cnt)) == 0
+    rng = np.random.default_rng(1)
+    p = rng.normal(0, 0.08, cnt.value).astype(np.float32)
+    x = rng.normal(size=(B, d)).astype(np.float32)
+    yc = rng.integers(0, C, B).astype(np.uint32)
+    yr = rng.normal(5, 1, B).astype(np.float32)
+    g, loss = ctx.learn_grad(x, yc, yr, C, p, lam=0.5)
+    ref, ce, mse = reference_grad(x, yc, yr, C, p.astype(np.float64), 0.5)
+    assert abs(loss[0] - ce) <= 1e-4 * max(1, abs(ce))
+    assert abs(loss[1] - mse) <= 1e-4 * max(1, abs(mse))
+    # FP32 accumulation vs FP64 on identical bf16 operands
+    err = np.abs(g - ref)
+    assert np.all(err <= 2e-4 * np.abs(ref).max() + 1e-3 * np.abs(ref)), err.max()
+
+
+def test_learned_search_beats_plain_at_equal_recall():
+    from weavess_gb300 import Context
+    base, query = ds.int_mixture(40000, 64, 48, seed=41, n_query=600)
+    _, train = ds.int_mixture(40000, 64, 48, seed=41, n_query=12600)
+    train = train[600:]  # queries of the same mixture, disjoint from the test set
+    gt = ds.groundtruth_fp64(base, query, 10)
+    ctx = Context(0)
+    ctx.upload_base(base)
+    ctx.srand(1)
+    ctx.init_random(12)
+    ctx.nnd_refine(12, 32, 48, 6, 64)
+    ctx.nsg_refine(48, 24, 300)
+    ctx.load_built_graph()
+    rep = ctx.learn_fit(train, clusters=48, L_trace=256, L_max=256, epochs=8, batch=512)
+    res, dc_l, _, Ls = ctx.search_learned(query, 10, return_L=True)
+    r_l = ds.recall_at(res, gt)
+    # the plain search at the smallest beam reaching the same recall
+    dc_p = None
+    for L in (16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024):
+        ctx.srand(9)
+        rp, dc, _ = ctx.search(query, L, 10)
+        if ds.recall_at(rp, gt) >= r_l:
+            dc_p = dc
+            break
+    assert r_l >= 0.9, (r_l, rep)
+    assert dc_p is None or dc_p > 1.3 * dc_l, (dc_p, dc_l, r_l, rep, float(Ls.mean()))

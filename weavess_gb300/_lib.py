@@ -30,6 +30,22 @@ class Counters(C.Structure):
     _fields_ = [("dist_count", C.c_ulonglong), ("hop_count", C.c_ulonglong)]
 
 
+class LearnParams(C.Structure):
+    _fields_ = [("clusters", C.c_uint32), ("kmeans_iters", C.c_uint32), ("list_len", C.c_uint32),
+                ("L_trace", C.c_uint32), ("epochs", C.c_uint32), ("batch", C.c_uint32), ("lr", C.c_float),
+                ("lam", C.c_float), ("L_min", C.c_uint32), ("L_max", C.c_uint32), ("target_agreement", C.c_float),
+                ("fallback_p", C.c_float), ("seed", C.c_uint32)]
+
+
+class LearnReport(C.Structure):
+    _fields_ = [("loss_ce", C.c_float), ("loss_mse", C.c_float), ("margin", C.c_float),
+                ("val_agreement", C.c_float), ("ms", C.c_float), ("mean_label_L", C.c_float),
+                ("steps", C.c_uint32), ("labelled", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class BuildStats(C.Structure):
     _fields_ = [("rand_draws", C.c_ulonglong), ("offers", C.c_ulonglong), ("pairs", C.c_ulonglong),
                 ("chunks", C.c_uint), ("ms_join", C.c_float), ("ms_update", C.c_float), ("ms_total", C.c_float),
@@ -83,6 +99,14 @@ def load(build_if_needed: bool = True):
     L.wv_nsg_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(BuildStats)]
     L.wv_set_search_precision.argtypes = [vp, C.c_int, C.c_uint32]
     L.wv_candidate_distances.argtypes = [vp, f32p, C.c_uint32, u32p, C.c_uint32, f32p]
+    L.wv_learn_default_params.argtypes = [C.POINTER(LearnParams)]
+    L.wv_learn_default_params.restype = None
+    L.wv_learn_fit.argtypes = [vp, f32p, C.c_uint32, C.POINTER(LearnParams), C.POINTER(LearnReport)]
+    L.wv_search_learned.argtypes = [vp, f32p, C.c_uint32, C.c_uint32, u32p, vp, C.POINTER(Counters), vp]
+    L.wv_search_learned_device.argtypes = [vp, vp, C.c_uint32, C.c_uint32, vp, vp, vp, C.POINTER(Counters)]
+    L.wv_learn_set_margin.argtypes = [vp, C.c_float]
+    L.wv_learn_param_count.argtypes = [C.c_uint32, C.c_uint32, C.POINTER(C.c_ulonglong)]
+    L.wv_learn_grad.argtypes = [vp, f32p, u32p, f32p, C.c_uint32, C.c_uint32, f32p, C.c_float, f32p, f32p]
     L.wv_debug_sort.argtypes = [vp, f32p, u32p, u32p, C.c_uint32, C.c_int]
     L.wv_search_noalloc.argtypes = [vp, C.c_uint32, C.c_uint32, vp, vp, C.c_uint32, vp, C.c_uint32, vp, C.c_uint32,
                                     C.c_uint32, vp, vp, vp]

@@ -3,6 +3,7 @@
 #include <cstring>
 
 #include "wv_ctx.h"
+#include "wv_learn.h"
 #include "wv_search.h"
 
 using namespace wv;
@@ -56,8 +57,10 @@ int ensure_search_scratch(wv_ctx *c, uint32_t Lmax) {
   return blocks;
 }
 
+}  // namespace
+
 // runs the kernel on device-resident queries / seeds / outputs
-int run_search(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t *d_seeds, uint32_t seed_stride,
+int wv::run_search_device(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t *d_seeds, uint32_t seed_stride,
                const uint32_t *d_L, const uint32_t *d_K, uint32_t L, uint32_t K, uint32_t Lmax, uint32_t *d_out,
                float *d_dist, uint32_t out_stride, wv_counters *counters) {
   int blocks = ensure_search_scratch(c, Lmax);
@@ -106,6 +109,8 @@ int run_search(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t *d_seeds
   }
   return check_device_status(c, "search");
 }
+
+namespace {
 
 int check_search_args(wv_ctx *c, uint32_t nq, uint32_t L, uint32_t K) {
   WV_CHECK(c, c->n > 0, WV_ERR_STATE, "no base uploaded");
@@ -168,6 +173,7 @@ int wv_ctx_destroy(wv_ctx *c) {
                     &c->fg_deg, &c->qbase, &c->qscale})
     b->release();
   c->release_work();
+  learn_free(c);
   cudaStreamDestroy(c->own_stream);
   delete c;
   return WV_OK;
@@ -275,7 +281,7 @@ int wv_search(wv_ctx *c, const float *queries, uint32_t nq, int entry, uint32_t 
   if (out_dist) WV_CUDA(c, c->out_dist_buf.ensure((size_t)nq * K * 4));
   WV_CUDA(c, cudaMemcpyAsync(c->q_buf.p, queries, (size_t)nq * c->d * 4, cudaMemcpyHostToDevice, c->stream));
   WV_CUDA(c, cudaMemcpyAsync(c->seed_buf.p, seeds, (size_t)nq * L * 4, cudaMemcpyHostToDevice, c->stream));
-  rc = run_search(c, c->q_buf.as<float>(), nq, c->seed_buf.as<uint32_t>(), L, nullptr, nullptr, L, K, L,
+  rc = run_search_device(c, c->q_buf.as<float>(), nq, c->seed_buf.as<uint32_t>(), L, nullptr, nullptr, L, K, L,
                   c->out_ids_buf.as<uint32_t>(), out_dist ? c->out_dist_buf.as<float>() : nullptr, K, counters);
   if (rc) return rc;
   WV_CUDA(c, cudaMemcpyAsync(out_ids, c->out_ids_buf.p, (size_t)nq * K * 4, cudaMemcpyDeviceToHost, c->stream));
@@ -317,7 +323,7 @@ int wv_search_batch(wv_ctx *c, const float *queries, uint32_t nq, int entry, con
   WV_CUDA(c, cudaMemcpyAsync(c->seed_buf.p, hs.data(), hs.size() * 4, cudaMemcpyHostToDevice, c->stream));
   WV_CUDA(c, cudaMemcpyAsync(c->lq_buf.p, L, (size_t)nq * 4, cudaMemcpyHostToDevice, c->stream));
   WV_CUDA(c, cudaMemcpyAsync(c->kq_buf.p, K, (size_t)nq * 4, cudaMemcpyHostToDevice, c->stream));
-  int rc = run_search(c, c->q_buf.as<float>(), nq, c->seed_buf.as<uint32_t>(), Lmax, c->lq_buf.as<uint32_t>(),
+  int rc = run_search_device(c, c->q_buf.as<float>(), nq, c->seed_buf.as<uint32_t>(), Lmax, c->lq_buf.as<uint32_t>(),
                       c->kq_buf.as<uint32_t>(), 0, 0, Lmax, c->out_ids_buf.as<uint32_t>(),
                       out_dist ? c->out_dist_buf.as<float>() : nullptr, out_stride, counters);
   if (rc) return rc;
@@ -339,7 +345,7 @@ int wv_search_device(wv_ctx *c, const float *d_queries, uint32_t nq, uint32_t L,
   if (counters) *counters = wv_counters{0, 0};
   if (nq == 0) return WV_OK;
   WV_CUDA(c, cudaSetDevice(c->device));
-  return run_search(c, d_queries, nq, d_seeds, L, nullptr, nullptr, L, K, L, d_out_ids, d_out_dist, K, counters);
+  return run_search_device(c, d_queries, nq, d_seeds, L, nullptr, nullptr, L, K, L, d_out_ids, d_out_dist, K, counters);
 }
 
 }  // extern "C"

@@ -77,6 +77,9 @@ struct wv_ctx {
   uint32_t fg_n = 0, fg_w = 0, fg_ep = 0;
   bool fg_has_ep = false;
 
+  // learned entry / beam model (wv_learn.cu), or null
+  void *learn = nullptr;
+
   // named grow-only work buffers of the build kernels
   std::map<std::string, wv::DevBuf> work;
   template <class T>
@@ -122,5 +125,11 @@ inline int fail(wv_ctx *c, int code, const char *fmt, ...) {
 
 // reads the device status word after a launch; maps kernel-reported errors
 int check_device_status(wv_ctx *c, const char *what);
+
+// the search kernel on device-resident queries / seeds / outputs (per-query
+// L and K optional); counters (nullable) are read back
+int run_search_device(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t *d_seeds, uint32_t seed_stride,
+                      const uint32_t *d_L, const uint32_t *d_K, uint32_t L, uint32_t K, uint32_t Lmax, uint32_t *d_out,
+                      float *d_dist, uint32_t out_stride, wv_counters *counters);
 
 }  // namespace wv

@@ -25,8 +25,10 @@ import numpy as np
 
 # ---------------------------------------------------------------- generators
 def int_mixture(n: int, d: int = 128, n_centers: int = 64, sigma: float = 20.0,
-                seed: int = 7, n_query: int = 0):
-    """Integer-valued Gaussian mixture (float32).  Returns (base, query)."""
+                seed: int = 7, n_query: int = 0, query_stream: int = 2):
+    """Integer-valued Gaussian mixture (float32).  Returns (base, query);
+    `query_stream` selects an independent stream of queries from the same
+    mixture (2: the evaluation queries; other values: e.g. training queries)."""
     rng = np.random.default_rng(seed)
     centers = rng.uniform(0.0, 255.0, size=(n_centers, d))
 
@@ -41,7 +43,7 @@ def int_mixture(n: int, d: int = 128, n_centers: int = 64, sigma: float = 20.0,
             out[s:s + c] = np.clip(np.rint(x), 0.0, 255.0)
         return out
 
-    return draw(n, 1), draw(n_query, 2)
+    return draw(n, 1), draw(n_query, query_stream)
 
 
 def unit_mixture(n: int, d: int = 96, n_dirs: int = 1000, cos: float = 0.7,

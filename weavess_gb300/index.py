@@ -154,6 +154,45 @@ class Context:
         self._check(self.L.wv_candidate_distances(self.h, q, q.shape[0], ids, ids.shape[1], out))
         return out
 
+    # -- learned entry point / beam width
+    def learn_fit(self, train_queries, **kw):
+        p = _lib.LearnParams()
+        self.L.wv_learn_default_params(C.byref(p))
+        for k, v in kw.items():
+            setattr(p, k, v)
+        rep = _lib.LearnReport()
+        tq = _f32(train_queries)
+        self._check(self.L.wv_learn_fit(self.h, tq, tq.shape[0], C.byref(p), C.byref(rep)))
+        return rep.as_dict()
+
+    def learn_set_margin(self, margin: float):
+        self._check(self.L.wv_learn_set_margin(self.h, margin))
+
+    def search_learned(self, queries, K: int = 10, return_L=False):
+        q = _f32(queries)
+        nq = q.shape[0]
+        out = np.zeros((nq, K), np.uint32)
+        Ls = np.zeros(nq, np.uint32)
+        cnt = _lib.Counters()
+        self._check(self.L.wv_search_learned(self.h, q, nq, K, out, None, C.byref(cnt), Ls.ctypes.data))
+        res = (out, int(cnt.dist_count), int(cnt.hop_count))
+        return res + (Ls,) if return_L else res
+
+    def search_learned_device(self, d_queries_ptr, nq, K, d_plain_seeds_ptr, d_out_ptr, counters=False):
+        cnt = _lib.Counters() if counters else None
+        self._check(self.L.wv_search_learned_device(self.h, C.c_void_p(d_queries_ptr), nq, K,
+                                                    C.c_void_p(d_plain_seeds_ptr), C.c_void_p(d_out_ptr), None,
+                                                    C.byref(cnt) if counters else None))
+        return (int(cnt.dist_count), int(cnt.hop_count)) if counters else None
+
+    def learn_grad(self, x, yc, yr, clusters, params, lam=0.5):
+        x = _f32(x)
+        grad = np.zeros_like(_f32(params))
+        loss = np.zeros(2, np.float32)
+        self._check(self.L.wv_learn_grad(self.h, x, _u32(yc), _f32(yr), x.shape[0], clusters, _f32(params), lam,
+                                         grad, loss))
+        return grad, loss
+
     def draw_seeds(self, nq: int, L: int, entry="rand"):
         out = np.zeros((nq, L), np.uint32)
         self._check(self.L.wv_draw_seeds(self.h, nq, ENTRY[entry], L, out))
