@@ -192,6 +192,11 @@ int wv_search_learned(wv_ctx *ctx, const float *queries, uint32_t nq, uint32_t K
 int wv_search_learned_device(wv_ctx *ctx, const float *d_queries, uint32_t nq, uint32_t K,
                              const uint32_t *d_plain_seeds, uint32_t *d_out_ids, float *d_out_dist,
                              wv_counters *counters);
+/* The model's entry cluster (argmax), its probability and the beam
+ * regressor output (log2 L) for nq host queries. */
+int wv_learn_predict(wv_ctx *ctx, const float *queries, uint32_t nq, uint32_t *cluster, float *prob, float *log2L);
+/* The k-means cluster of base ids (as the entry lists were built). */
+int wv_learn_assign(wv_ctx *ctx, const uint32_t *ids, uint32_t n, uint32_t *cluster);
 /* Overrides the calibrated beam margin (beam = margin * 2^regressor). */
 int wv_learn_set_margin(wv_ctx *ctx, float margin);
 /* Loss (ce, mse) and gradients of one batch for given parameters, for the

@@ -78,6 +78,17 @@ int wv_search_learned(wv_ctx *c, const float *queries, uint32_t nq, uint32_t K, 
   return WV_OK;
 }
 
+int wv_learn_predict(wv_ctx *c, const float *q, uint32_t nq, uint32_t *cluster, float *prob, float *log2L) {
+  if (!c || !q) return WV_ERR_ARG;
+  WV_CUDA(c, cudaSetDevice(c->device));
+  return learn_predict(c, q, nq, cluster, prob, log2L);
+}
+
+int wv_learn_assign(wv_ctx *c, const uint32_t *ids, uint32_t n, uint32_t *cluster) {
+  if (!c || !ids || !cluster) return WV_ERR_ARG;
+  return learn_assign(c, ids, n, cluster);
+}
+
 int wv_learn_set_margin(wv_ctx *c, float margin) {
   if (!c || !(margin > 0.f)) return WV_ERR_ARG;
   WV_CHECK(c, c->learn, WV_ERR_STATE, "no trained model");

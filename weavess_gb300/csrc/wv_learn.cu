@@ -242,6 +242,7 @@ __global__ void k_cluster_seeds(const uint32_t *label, uint32_t nq, const uint32
 // ================================================================ state
 struct LearnState {
   uint32_t C = 0, D = 0, SL = 0;
+  std::vector<uint32_t> h_assign;  // k-means cluster of every base row
   // parameter block (FP32 master): W1 D x H, b1 H, W2 H x H, b2 H, W3 H x (C+1), b3 C+1
   size_t oW1, ob1, oW2, ob2, oW3, ob3, np;
   DevBuf P, G, M, V, Pb;  // Pb: bf16 copies of the weights (same offsets)
@@ -460,6 +461,7 @@ int learn_fit(wv_ctx *c, const float *train_q, uint32_t nt, const LearnParams &p
   WV_CUDA(c, cudaMemcpyAsync(hd.data(), adist, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
   WV_CUDA(c, cudaStreamSynchronize(c->stream));
   S.SL = p.list_len;
+  S.h_assign = ha;
   std::vector<std::vector<uint32_t>> mem(C);
   for (uint32_t i = 0; i < n; i++) mem[ha[i]].push_back(i);
   std::vector<uint32_t> hl((size_t)C * S.SL, 0), hll(C, 0);
@@ -713,6 +715,45 @@ int learn_grad(wv_ctx *c, const float *x, const uint32_t *yc, const float *yr, u
   WV_CUDA(c, cudaMemcpyAsync(loss, dl, 8, cudaMemcpyDeviceToHost, c->stream));
   WV_CUDA(c, cudaStreamSynchronize(c->stream));
   S.ready = false;
+  return WV_OK;
+}
+
+int learn_predict(wv_ctx *c, const float *q, uint32_t nq, uint32_t *cluster, float *prob, float *log2L) {
+  WV_CHECK(c, c->learn && state(c).ready, WV_ERR_STATE, "no trained model");
+  LearnState &S = state(c);
+  cudaError_t e = cudaSuccess;
+  float *dq = c->buf<float>("lp_q", (size_t)nq * S.D, &e);
+  WV_CUDA(c, e);
+  WV_CUDA(c, cudaMemcpyAsync(dq, q, (size_t)nq * S.D * 4, cudaMemcpyHostToDevice, c->stream));
+  Work w;
+  int rc = alloc_work(c, nq, S.D, S.C, w);
+  if (rc) return rc;
+  rc = forward(c, S, dq, nullptr, nq, w);
+  if (rc) return rc;
+  std::vector<float> O((size_t)nq * (S.C + 1));
+  WV_CUDA(c, cudaMemcpyAsync(O.data(), w.O, O.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (uint32_t i = 0; i < nq; i++) {
+    const float *o = O.data() + (size_t)i * (S.C + 1);
+    uint32_t b = 0;
+    for (uint32_t k = 1; k < S.C; k++)
+      if (o[k] > o[b]) b = k;
+    double se = 0;
+    for (uint32_t k = 0; k < S.C; k++) se += std::exp((double)o[k] - o[b]);
+    if (cluster) cluster[i] = b;
+    if (prob) prob[i] = (float)(1.0 / se);
+    if (log2L) log2L[i] = o[S.C];
+  }
+  return WV_OK;
+}
+
+int learn_assign(wv_ctx *c, const uint32_t *ids, uint32_t n, uint32_t *cluster) {
+  WV_CHECK(c, c->learn && !state(c).h_assign.empty(), WV_ERR_STATE, "no clusters");
+  LearnState &S = state(c);
+  for (uint32_t i = 0; i < n; i++) {
+    WV_CHECK(c, ids[i] < S.h_assign.size(), WV_ERR_ARG, "id %u out of range", ids[i]);
+    cluster[i] = S.h_assign[ids[i]];
+  }
   return WV_OK;
 }
 

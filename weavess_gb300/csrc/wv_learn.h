@@ -11,6 +11,8 @@ struct LearnParams {
   uint32_t kmeans_iters = 8;
   uint32_t list_len = 512;     // seeds kept per cluster
   uint32_t L_trace = 512;      int learn_set_margin(wv_ctx *c, float margin);
+int learn_predict(wv_ctx *c, const float *q, uint32_t nq, uint32_t *cluster, float *prob, float *log2L);
+int learn_assign(wv_ctx *c, const uint32_t *ids, uint32_t n, uint32_t *cluster);
 // beam of the plain search that labels the traces
   uint32_t epochs = 6, batch = 1024;
   float lr = 1e-3f, lam = 0.5f;  // Adam step, weight of the beam regressor
@@ -35,6 +37,8 @@ int learn_grad(wv_ctx *c, const float *x, const uint32_t *yc, const float *yr, u
                const float *params, float lam, float *grad, float *loss);
 size_t learn_param_count(uint32_t d, uint32_t C);
 int learn_set_margin(wv_ctx *c, float margin);
+int learn_predict(wv_ctx *c, const float *q, uint32_t nq, uint32_t *cluster, float *prob, float *log2L);
+int learn_assign(wv_ctx *c, const uint32_t *ids, uint32_t n, uint32_t *cluster);
 // beam of the plain search the model falls back to (its trace beam)
 uint32_t learn_plain_beam(wv_ctx *c);
 void learn_free(wv_ctx *c);

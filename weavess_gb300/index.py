@@ -165,6 +165,20 @@ class Context:
         self._check(self.L.wv_learn_fit(self.h, tq, tq.shape[0], C.byref(p), C.byref(rep)))
         return rep.as_dict()
 
+    def learn_predict(self, queries):
+        q = _f32(queries)
+        c = np.zeros(q.shape[0], np.uint32)
+        p = np.zeros(q.shape[0], np.float32)
+        l2 = np.zeros(q.shape[0], np.float32)
+        self._check(self.L.wv_learn_predict(self.h, q, q.shape[0], c, p, l2))
+        return c, p, l2
+
+    def learn_assign(self, ids):
+        ids = _u32(ids)
+        out = np.zeros(ids.shape, np.uint32)
+        self._check(self.L.wv_learn_assign(self.h, ids.reshape(-1), ids.size, out.reshape(-1)))
+        return out
+
     def learn_set_margin(self, margin: float):
         self._check(self.L.wv_learn_set_margin(self.h, margin))
 
