@@ -37,7 +37,7 @@ from weavess_gb300 import datasets as ds  # noqa: E402
 
 CFG = dict(n=1_000_000, d=128, centers=256, nq=10_000, seed=7, S=20, K=64, L=80, ITER=8, R=100,
            R_refine=32, L_refine=64, C_refine=500, k=10, target_recall=0.95,
-           n_train=200_000, n_val=2000, clusters=64, L_trace=512, epochs=6,
+           n_train=200_000, n_val=2000, clusters=64, L_trace=1024, L_max_learned=512, epochs=6,
            L_grid=[16, 24, 32, 48, 64, 96, 128, 160, 192, 256, 320, 384, 448, 512, 640, 768, 896, 1024, 1280,
                    1536])
 METRIC = "QPS at recall@10>=0.95 (learned+BF16 vs plain FP32, 1 GB300); build sec"
@@ -154,15 +154,14 @@ def run_learned(ctx, cfg, base, query, gt, args, dev, stream, flush):
     _, tq = ds.int_mixture(0, cfg["d"], cfg["centers"], seed=cfg["seed"], n_query=nt + nval, query_stream=3)
     train, val = tq[:nt], tq[nt:]
     t = time.time()
-    rep = ctx.learn_fit(train, clusters=cfg["clusters"], L_trace=cfg["L_trace"], L_max=cfg["L_trace"],
-                        list_len=cfg["L_trace"], epochs=cfg["epochs"], batch=1024)
+    rep = ctx.learn_fit(train, clusters=cfg["clusters"], L_trace=cfg["L_trace"], L_max=cfg["L_max_learned"],
+                        list_len=cfg["L_max_learned"], epochs=cfg["epochs"], batch=1024)
     fit_s = time.time() - t
     log(f"learn_fit {fit_s:.1f}s {rep}")
     gtv = knn_fp64(base, val, 10)
     ctx.set_precision("bf16", rerank=0)
-    margin = rep["margin"]
     chosen = None
-    for m in [margin * f for f in (1.0, 1.25, 1.5, 2.0, 2.5, 3.0, 4.0, 6.0, 8.0)]:
+    for m in (0.5, 0.75, 1.0, 1.25, 1.5, 2.0, 2.5, 3.0, 4.0, 6.0, 8.0):
         ctx.learn_set_margin(m)
         ctx.srand(4321)
         rv, _, _ = ctx.search_learned(val, cfg["k"])
@@ -215,7 +214,7 @@ def run_ours(args):
     cfg = dict(CFG)
     if args.small:
         cfg.update(n=100_000, centers=64, nq=1000, S=10, K=32, L=40, ITER=8, R=100, R_refine=32, L_refine=32,
-                   n_train=40_000, clusters=32, L_trace=256)
+                   n_train=40_000, clusters=32, L_trace=512, L_max_learned=256)
     if args.nq:
         cfg["nq"] = args.nq
     dev = torch.device("cuda:0")

@@ -672,12 +672,14 @@ int learn_search(wv_ctx *c, const float *dq, uint32_t nq, uint32_t K, uint32_t *
   rc = forward(c, S, dq, nullptr, nq, w);
   if (rc) return rc;
   WV_CUDA(c, cudaMemsetAsync(fb, 0, 4, c->stream));
-  k_learn_seeds<<<nblk(nq), 128, 0, c->stream>>>(w.O, nq, S.C, S.lists.as<uint32_t>(), S.SL, S.llen.as<uint32_t>(),
+  k_learn_seeds<<<nblk(nq, 128), 128, 0, c->stream>>>(w.O, nq, S.C, S.lists.as<uint32_t>(), S.SL, S.llen.as<uint32_t>(),
                                                  S.margin, S.Lmin, S.Lmax, S.fallback_p, S.L_plain, d_plain_seeds,
                                                  seeds, stride, Lq, K, fb);
   WV_CUDA(c, cudaGetLastError());
   if (d_Lq_out) WV_CUDA(c, cudaMemcpyAsync(d_Lq_out, Lq, (size_t)nq * 4, cudaMemcpyDeviceToDevice, c->stream));
-  return run_search_device(c, dq, nq, seeds, stride, Lq, nullptr, 0, K, stride, dout, ddist, K, counters);
+  // without the fallback no query's beam exceeds Lmax: size the kernel for it
+  const uint32_t Lcap = (d_plain_seeds && S.fallback_p > 0.f) ? stride : S.Lmax;
+  return run_search_device(c, dq, nq, seeds, stride, Lq, nullptr, 0, K, Lcap, dout, ddist, K, counters);
 }
 
 int learn_grad(wv_ctx *c, const float *x, const uint32_t *yc, const float *yr, uint32_t B, uint32_t C,
