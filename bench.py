@@ -56,6 +56,16 @@ class Clocks:
 
     def __init__(self):
         self.rows, self.proc = [], None
+        self.win = None
+
+    def mark(self, t0, t1):
+        """The timed region, in time.perf_counter() seconds."""
+        self.win = (t0, t1)
+
+    def in_window(self):
+        if self.win is None:
+            return len(self.rows)
+        return sum(1 for r in self.rows if self.win[0] <= r[0] <= self.win[1] + 0.25)
 
     def __enter__(self):
         try:
@@ -69,7 +79,7 @@ class Clocks:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([x.strip() for x in line.split(",")])
+            self.rows.append([time.perf_counter()] + [x.strip() for x in line.split(",")])
 
     def __exit__(self, *a):
         if self.proc:
@@ -80,14 +90,48 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
-        if not self.rows:
+        """Samples from the timed region on; when the region was shorter than
+        the sampling period, the samples of the same steps repeated right after
+        it (the caller keeps the load on until enough samples arrived)."""
+        rows = [r[1:] for r in self.rows if self.win is None or r[0] >= self.win[0]]
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows), "samples_in_timed_region": self.in_window()}
+
+
+PROFILE_REGION = "search"  # which region a cudaProfilerStart/Stop pair brackets (for ncu --profile-from-start off)
+
+
+def timed_steps(step, steps, stream, flush, clk):
+    """`steps` CUDA-event-timed calls of `step` (L2 flushed before each), with
+    the clock sampler running; the same steps continue untimed until the
+    sampler has three readings from the timed region on.  Returns per-step ms."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    if PROFILE_REGION == "search":
+        torch.cuda.profiler.start()
+    for i in range(steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    if PROFILE_REGION == "search":
+        torch.cuda.profiler.stop()
+    clk.mark(t0, time.perf_counter())
+    deadline = time.perf_counter() + 3.0
+    while sum(1 for r in clk.rows if r[0] >= t0) < 3 and time.perf_counter() < deadline:
+        flush.zero_()
+        step()
+        torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
 
 
 def make_data(cfg):
@@ -116,6 +160,8 @@ def build_index(ctx, base, cfg):
     """GPU build; returns build seconds and per-stage stats."""
     import torch
     torch.cuda.synchronize()
+    if PROFILE_REGION == "build":
+        torch.cuda.profiler.start()
     t0 = time.time()
     ctx.upload_base(base)
     ctx.srand(1)
@@ -125,7 +171,10 @@ def build_index(ctx, base, cfg):
     stages["nsg"] = ctx.nsg_refine(cfg["L_refine"], cfg["R_refine"], cfg["C_refine"])
     ctx.load_built_graph()
     torch.cuda.synchronize()
-    return time.time() - t0, stages
+    dt = time.time() - t0
+    if PROFILE_REGION == "build":
+        torch.cuda.profiler.stop()
+    return dt, stages
 
 
 def cpu_search_qps(base, query, g_ids, g_deg, L, threads, sample):
@@ -180,31 +229,26 @@ def run_learned(ctx, cfg, base, query, gt, args, dev, stream, flush):
     counters = None
     for _ in range(args.warmup):
         counters = ctx.search_learned_device(dq.data_ptr(), nq, K, dps.data_ptr(), dout.data_ptr(), counters=True)
-    torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    for i in range(args.steps):
-        flush.zero_()
-        ev[i][0].record(stream)
-        ctx.search_learned_device(dq.data_ptr(), nq, K, dps.data_ptr(), dout.data_ptr())
-        ev[i][1].record(stream)
-    torch.cuda.synchronize()
-    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    with Clocks() as clk:
+        step_ms = timed_steps(lambda: ctx.search_learned_device(dq.data_ptr(), nq, K, dps.data_ptr(), dout.data_ptr()),
+                              args.steps, stream, flush, clk)
+    ms = float(np.mean(step_ms))
     res = dout.cpu().numpy().astype(np.uint32)
     r_test = recall(res, gt, K)
     # e2e through the public host-buffer call
     qpin = torch.from_numpy(query).pin_memory().numpy()
-    ctx.search_learned(qpin, K)
+    _, _, _, Ls = ctx.search_learned(qpin, K, return_L=True)
+    plain_beam = ctx.learn_plain_beam()  # host-drawn plain seeds per query the call copies (0: none)
     e2e_t = []
-    Ls = None
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        _, _, _, Ls = ctx.search_learned(qpin, K, return_L=True)
+        ctx.search_learned(qpin, K)
         e2e_t.append(time.perf_counter() - t0)
     ctx.set_precision("fp32")
     dc, hc = counters
     return {"qps": nq / (ms / 1e3), "ms": ms, "recall@10": r_test, "e2e_qps": nq / float(np.mean(e2e_t)),
             "margin": chosen, "mean_L": float(Ls.mean()), "fit_s": fit_s, "report": rep, "dist_count": dc,
-            "hop_count": hc, "n_train": nt}
+            "hop_count": hc, "n_train": nt, "plain_seeds_per_query": plain_beam, "clocks": clk.summary()}
 
 
 def run_ours(args):
@@ -217,11 +261,17 @@ def run_ours(args):
                    n_train=40_000, clusters=32, L_trace=512, L_max_learned=256)
     if args.nq:
         cfg["nq"] = args.nq
+    if args.n:
+        cfg["n"] = args.n
     dev = torch.device("cuda:0")
     torch.cuda.set_device(dev)
     base, query = make_data(cfg)
     ctx = Context(0)
-    stream = torch.cuda.current_stream()
+    # one stream for everything timed: the L2 flush, the events and the
+    # context's kernels (the legacy default stream would not order the
+    # context's non-blocking stream)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     build_s, stages = build_index(ctx, base, cfg)
     log(f"build {build_s:.2f}s {stages}")
@@ -253,17 +303,9 @@ def run_ours(args):
     counters = None
     for _ in range(args.warmup):
         counters = ctx.search_device(dq.data_ptr(), nq, Lsel, K, ds_.data_ptr(), dout.data_ptr(), counters=True)
-    torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     with Clocks() as clk:
-        torch.cuda.synchronize()
-        for i in range(args.steps):
-            flush.zero_()
-            ev[i][0].record(stream)
-            ctx.search_device(dq.data_ptr(), nq, Lsel, K, ds_.data_ptr(), dout.data_ptr())
-            ev[i][1].record(stream)
-        torch.cuda.synchronize()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
+        step_ms = timed_steps(lambda: ctx.search_device(dq.data_ptr(), nq, Lsel, K, ds_.data_ptr(), dout.data_ptr()),
+                              args.steps, stream, flush, clk)
     ms = float(np.mean(step_ms))
     value = nq / (ms / 1e3)
     res_dev = dout.cpu().numpy().astype(np.uint32)
@@ -296,7 +338,8 @@ def run_ours(args):
     sample = 2000 if not args.small else 1000
     cpu_qps, cpu_dt, _ = cpu_search_qps(base, query, g_ids, g_deg, Lsel, threads, sample)
     plain = {"qps": round(value, 1), "ms_per_step": round(ms, 4), "L_search": Lsel, "recall@10": round(r_dev, 4),
-             "recall_sweep": sweep, "e2e_qps": round(e2e_qps, 1), "dist_count": dc, "hop_count": hc}
+             "recall_sweep": sweep, "e2e_qps": round(e2e_qps, 1), "dist_count": dc, "hop_count": hc,
+             "clocks": clk.summary()}
     if learned is not None:
         head_qps, head_ms, head_e2e = learned["qps"], learned["ms"], learned["e2e_qps"]
         ldc, lhc = learned["dist_count"], learned["hop_count"]
@@ -307,8 +350,8 @@ def run_ours(args):
                 "frac": round(l_achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
                 "alg_bytes_per_launch": int(alg), "dist_count": ldc, "hop_count": lhc,
                 "kernel": "k_search (learned seeds, per-query L, bf16 candidate rows)"}
-        h2d = nq * d * 4 + nq * cfg["L_trace"] * 4
-        launches = args.steps * 5  # 3 GEMMs + the seed kernel + the search per step
+        h2d = nq * d * 4 + nq * learned["plain_seeds_per_query"] * 4
+        launches = args.steps * 6  # query normalisation, 3 GEMMs, the seed kernel, the search per step
     else:
         head_qps, head_ms, head_e2e = value, ms, e2e_qps
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
@@ -330,7 +373,7 @@ def run_ours(args):
                                if learned else None),
                    "plain_fp32": plain,
                    "speedup_vs_plain": round(head_qps / value, 3) if learned else 1.0,
-                   "l2": "flushed (256 MB write) between steps; base 512 MB > L2",
+                   "l2": f"flushed (256 MB write) between steps; base {cfg['n'] * d * 4 / 1e6:.0f} MB",
                    "build_s": round(build_s, 3),
                    "build_stages": {k: {kk: (round(vv, 2) if isinstance(vv, float) else vv) for kk, vv in v.items()}
                                     for k, v in stages.items()}},
@@ -341,7 +384,7 @@ def run_ours(args):
         "cpu_baseline": {"value": round(cpu_qps, 1), "unit": "queries/s", "cores": threads, "kind": "port",
                          "sample": f"first {sample} queries, same graph, plain search at L={Lsel}, oracle OpenMP "
                                    f"({cpu_dt:.2f}s)"},
-        "clocks": clk.summary(),
+        "clocks": learned["clocks"] if learned else clk.summary(),
     }
     print(json.dumps(line), flush=True)
 
@@ -405,8 +448,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="N=1e5 configuration (quick check)")
     ap.add_argument("--nq", type=int, default=0, help="override the number of queries")
+    ap.add_argument("--n", type=int, default=0, help="override the number of base vectors")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned + bf16 leg")
+    ap.add_argument("--profile-region", choices=["search", "build"], default="search",
+                    help="region bracketed by cudaProfilerStart/Stop (ncu --profile-from-start off)")
     args = ap.parse_args()
+    global PROFILE_REGION
+    PROFILE_REGION = args.profile_region
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         if rank == 0:

@@ -199,6 +199,10 @@ int wv_learn_predict(wv_ctx *ctx, const float *queries, uint32_t nq, uint32_t *c
 int wv_learn_assign(wv_ctx *ctx, const uint32_t *ids, uint32_t n, uint32_t *cluster);
 /* Overrides the calibrated beam margin (beam = margin * 2^regressor). */
 int wv_learn_set_margin(wv_ctx *ctx, float margin);
+/* Plain (SearchEntryRand) seeds per query that wv_search_learned draws on the
+ * host and copies to the device: the trace beam, or 0 when no query can read
+ * one (no fallback and every entry list covers the largest beam). */
+int wv_learn_plain_beam(wv_ctx *ctx, uint32_t *L);
 /* Loss (ce, mse) and gradients of one batch for given parameters, for the
  * gradient check; parameters packed as W1 (d x 256), b1, W2 (256 x 256), b2,
  * W3 (256 x (clusters + 1)), b3.  Overwrites (and unsets) a trained model. */

@@ -105,28 +105,33 @@ def test_gpu_gradients_match_fp64_oracle():
 
 
 def test_learned_search_beats_plain_at_equal_recall():
+    """1M x 128 integer mixture of 256 clusters (the bench workload, 1,000
+    queries): the plain search needs a wide beam to find the query's cluster
+    from random seeds; the learned entry lists and beam width reach the same
+    recall with far fewer distance computations.  (At 1e5 points the plain
+    search finds the cluster cheaply and the two cost about the same.)"""
     from weavess_gb300 import Context
-    base, query = ds.int_mixture(40000, 64, 48, seed=41, n_query=600)
-    _, train = ds.int_mixture(40000, 64, 48, seed=41, n_query=12600)
-    train = train[600:]  # queries of the same mixture, disjoint from the test set
-    gt = ds.groundtruth_fp64(base, query, 10)
+    from weavess_gb300.groundtruth import knn_fp64
+    base, query = ds.int_mixture(1_000_000, 128, 256, seed=7, n_query=1000)
+    _, train = ds.int_mixture(0, 128, 256, seed=7, n_query=60_000, query_stream=3)
+    gt = knn_fp64(base, query, 10)
     ctx = Context(0)
     ctx.upload_base(base)
     ctx.srand(1)
-    ctx.init_random(12)
-    ctx.nnd_refine(12, 32, 48, 6, 64)
-    ctx.nsg_refine(48, 24, 300)
+    ctx.init_random(20)
+    ctx.nnd_refine(20, 64, 80, 8, 100)
+    ctx.nsg_refine(64, 32, 500)
     ctx.load_built_graph()
-    rep = ctx.learn_fit(train, clusters=48, L_trace=256, L_max=256, epochs=8, batch=512)
+    rep = ctx.learn_fit(train, clusters=64, L_trace=1024, L_max=512, list_len=512, epochs=6, batch=1024)
     res, dc_l, _, Ls = ctx.search_learned(query, 10, return_L=True)
     r_l = ds.recall_at(res, gt)
     # the plain search at the smallest beam reaching the same recall
     dc_p = None
-    for L in (16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024):
+    for L in (64, 128, 192, 256, 320, 384, 448, 512, 640, 768, 1024, 1280, 1536):
         ctx.srand(9)
         rp, dc, _ = ctx.search(query, L, 10)
         if ds.recall_at(rp, gt) >= r_l:
             dc_p = dc
             break
     assert r_l >= 0.9, (r_l, rep)
-    assert dc_p is None or dc_p > 1.3 * dc_l, (dc_p, dc_l, r_l, rep, float(Ls.mean()))
+    assert dc_p is None or dc_p > 1.5 * dc_l, (dc_p, dc_l, r_l, rep, float(Ls.mean()))

@@ -56,19 +56,20 @@ int wv_search_learned(wv_ctx *c, const float *queries, uint32_t nq, uint32_t K, 
   if (nq == 0) return WV_OK;
   WV_CUDA(c, cudaSetDevice(c->device));
   WV_CHECK(c, c->learn, WV_ERR_STATE, "no trained model (call wv_learn_fit)");
-  // the plain seeds of the fallback, drawn as SearchEntryRand draws them
+  // the plain seeds of the fallback (and of short entry lists), drawn as
+  // SearchEntryRand draws them; skipped when the model can read none
   const uint32_t Lp = learn_plain_beam(c);
   std::vector<uint32_t> hs((size_t)nq * Lp);
-  draw_seeds_rand(c->rnd, nq, Lp, c->n, hs.data(), Lp);
+  if (Lp) draw_seeds_rand(c->rnd, nq, Lp, c->n, hs.data(), Lp);
   cudaError_t e = cudaSuccess;
   float *dq = c->buf<float>("sl_q", (size_t)nq * c->d, &e);
-  uint32_t *ds = c->buf<uint32_t>("sl_s", hs.size(), &e);
+  uint32_t *ds = Lp ? c->buf<uint32_t>("sl_s", hs.size(), &e) : nullptr;
   uint32_t *dout = c->buf<uint32_t>("sl_o", (size_t)nq * K, &e);
   float *dd = out_dist ? c->buf<float>("sl_d", (size_t)nq * K, &e) : nullptr;
   uint32_t *dL = c->buf<uint32_t>("sl_L", nq, &e);
   WV_CUDA(c, e);
   WV_CUDA(c, cudaMemcpyAsync(dq, queries, (size_t)nq * c->d * 4, cudaMemcpyHostToDevice, c->stream));
-  WV_CUDA(c, cudaMemcpyAsync(ds, hs.data(), hs.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  if (Lp) WV_CUDA(c, cudaMemcpyAsync(ds, hs.data(), hs.size() * 4, cudaMemcpyHostToDevice, c->stream));
   int rc = learn_search(c, dq, nq, K, dout, dd, counters, ds, dL);
   if (rc) return rc;
   WV_CUDA(c, cudaMemcpyAsync(out_ids, dout, (size_t)nq * K * 4, cudaMemcpyDeviceToHost, c->stream));
@@ -93,6 +94,13 @@ int wv_learn_set_margin(wv_ctx *c, float margin) {
   if (!c || !(margin > 0.f)) return WV_ERR_ARG;
   WV_CHECK(c, c->learn, WV_ERR_STATE, "no trained model");
   return learn_set_margin(c, margin);
+}
+
+int wv_learn_plain_beam(wv_ctx *c, uint32_t *L) {
+  if (!c || !L) return WV_ERR_ARG;
+  WV_CHECK(c, c->learn, WV_ERR_STATE, "no trained model");
+  *L = learn_plain_beam(c);
+  return WV_OK;
 }
 
 int wv_learn_param_count(uint32_t d, uint32_t clusters, unsigned long long *count) {

@@ -251,6 +251,7 @@ struct LearnState {
   std::vector<uint32_t> h_entry;
   float margin = 1.5f, fallback_p = 0.f;
   uint32_t Lmin = 16, Lmax = 512, L_plain = 512;
+  uint32_t min_llen = 0;  // shortest entry list (0 when a cluster is empty)
   int steps = 0;
   bool ready = false;
 
@@ -482,6 +483,7 @@ int learn_fit(wv_ctx *c, const float *train_q, uint32_t nt, const LearnParams &p
     for (size_t j = 0; j < ord.size() && t < S.SL; j++) hl[(size_t)k * S.SL + t++] = ord[j].second;
     hll[k] = t;
   }
+  S.min_llen = *std::min_element(hll.begin(), hll.end());
   WV_CUDA(c, S.lists.ensure(hl.size() * 4));
   WV_CUDA(c, S.llen.ensure((size_t)C * 4));
   WV_CUDA(c, cudaMemcpyAsync(S.lists.p, hl.data(), hl.size() * 4, cudaMemcpyHostToDevice, c->stream));
@@ -764,7 +766,14 @@ int learn_set_margin(wv_ctx *c, float margin) {
   return WV_OK;
 }
 
-uint32_t learn_plain_beam(wv_ctx *c) { return c->learn ? static_cast<LearnState *>(c->learn)->L_plain : 0u; }
+uint32_t learn_plain_beam(wv_ctx *c) {
+  if (!c->learn) return 0u;
+  const LearnState &S = *static_cast<LearnState *>(c->learn);
+  // without the fallback, and with every entry list at least as long as the
+  // largest beam, k_learn_seeds never reads a plain seed
+  if (!(S.fallback_p > 0.f) && S.min_llen >= S.Lmax) return 0u;
+  return S.L_plain;
+}
 
 size_t learn_param_count(uint32_t d, uint32_t C) {
   LearnState S;

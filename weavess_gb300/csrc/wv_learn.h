@@ -39,7 +39,8 @@ size_t learn_param_count(uint32_t d, uint32_t C);
 int learn_set_margin(wv_ctx *c, float margin);
 int learn_predict(wv_ctx *c, const float *q, uint32_t nq, uint32_t *cluster, float *prob, float *log2L);
 int learn_assign(wv_ctx *c, const uint32_t *ids, uint32_t n, uint32_t *cluster);
-// beam of the plain search the model falls back to (its trace beam)
+// plain seeds per query the learned search may read (the trace beam), or 0
+// when no query can read one (no fallback, every entry list covers L_max)
 uint32_t learn_plain_beam(wv_ctx *c);
 void learn_free(wv_ctx *c);
 

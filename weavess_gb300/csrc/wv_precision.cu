@@ -7,6 +7,7 @@
 
 #include "wv_common.cuh"
 #include "wv_ctx.h"
+#include "wv_lowp.cuh"
 
 using namespace wv;
 
@@ -33,29 +34,31 @@ __global__ void k_to_fp8(const float *x, uint32_t n, uint32_t d, __nv_fp8_storag
   }
 }
 
-// out[q, j] = candidate distance of query q to base id ids[q, j]
-__global__ void k_cand_dist(const float *base, const void *qb, const float *qs, int storage, uint32_t d,
-                            const float *queries, const uint32_t *ids, uint32_t nq, uint32_t m, float *out) {
+// out[q, j] = candidate distance of query q to base id ids[q, j]: fp32 in the
+// reference's order, or the search kernel's low-precision distance (one warp
+// per query and 32 ids, the same lowp_rows_dist the search calls)
+__global__ void k_cand_dist(const float *base, LowpRows lp, uint32_t d, const float *queries, const uint32_t *ids,
+                            uint32_t nq, uint32_t m, float *out) {
   const int lane = threadIdx.x & 31;
   const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
-  if (w >= (size_t)nq * m) return;
-  const uint32_t q = (uint32_t)(w / m), id = ids[w];
+  const uint32_t chunks = (m + 31) / 32;
+  if (w >= (size_t)nq * chunks) return;
+  const uint32_t q = (uint32_t)(w / chunks), j0 = (uint32_t)(w % chunks) * 32;
+  const int cnt = (int)min(32u, m - j0);
   const float *qv = queries + (size_t)q * d;
-  float part = 0.f;
-  for (uint32_t k = lane; k < d; k += 32) {
-    float x;
-    if (storage == 0) x = base[(size_t)id * d + k];
-    else if (storage == 1) x = __bfloat162float(reinterpret_cast<const __nv_bfloat16 *>(qb)[(size_t)id * d + k]);
-    else {
-      const __half_raw h =
-          __nv_cvt_fp8_to_halfraw(reinterpret_cast<const __nv_fp8_storage_t *>(qb)[(size_t)id * d + k], __NV_E4M3);
-      x = qs[id] * __half2float(*reinterpret_cast<const __half *>(&h));
+  const uint32_t my = lane < cnt ? ids[(size_t)q * m + j0 + lane] : 0u;
+  float v;
+  if (lp.storage == 0) {
+    v = 0.f;
+    if (lane < cnt) {
+      const float4 *row = reinterpret_cast<const float4 *>(base + (size_t)my * d);
+      const float4 *q4 = reinterpret_cast<const float4 *>(qv);
+      for (uint32_t g = 0; g < d / 4; g++) v = __fadd_rn(v, group4(row[g], q4[g]));
     }
-    const float e = qv[k] - x;
-    part += e * e;
+  } else {
+    v = lowp_rows_dist(lp, my, cnt, qv, lane);
   }
-  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
-  if (lane == 0) out[w] = part;
+  if (lane < cnt) out[(size_t)q * m + j0 + lane] = v;
 }
 
 }  // namespace
@@ -89,6 +92,7 @@ int wv_candidate_distances(wv_ctx *c, const float *queries, uint32_t nq, const u
                            float *out) {
   if (!c || !queries || !ids || !out) return WV_ERR_ARG;
   WV_CHECK(c, c->n > 0, WV_ERR_STATE, "no base uploaded");
+  WV_CHECK(c, c->d % 4 == 0, WV_ERR_LIMIT, "dimension %u is not a multiple of 4", c->d);
   for (size_t i = 0; i < (size_t)nq * m; i++) WV_CHECK(c, ids[i] < c->n, WV_ERR_ARG, "id %u >= n", ids[i]);
   WV_CUDA(c, cudaSetDevice(c->device));
   cudaError_t e = cudaSuccess;
@@ -98,9 +102,9 @@ int wv_candidate_distances(wv_ctx *c, const float *queries, uint32_t nq, const u
   WV_CUDA(c, e);
   WV_CUDA(c, cudaMemcpyAsync(dq, queries, (size_t)nq * c->d * 4, cudaMemcpyHostToDevice, c->stream));
   WV_CUDA(c, cudaMemcpyAsync(di, ids, (size_t)nq * m * 4, cudaMemcpyHostToDevice, c->stream));
-  const size_t warps = (size_t)nq * m;
+  const size_t warps = (size_t)nq * ((m + 31) / 32);
   k_cand_dist<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, c->stream>>>(
-      c->base.as<float>(), c->qbase.p, c->qscale.as<float>(), c->storage, c->d, dq, di, nq, m, dout);
+      c->base.as<float>(), LowpRows{c->qbase.p, c->qscale.as<float>(), c->storage, c->d}, c->d, dq, di, nq, m, dout);
   WV_CUDA(c, cudaGetLastError());
   WV_CUDA(c, cudaMemcpyAsync(out, dout, (size_t)nq * m * 4, cudaMemcpyDeviceToHost, c->stream));
   WV_CUDA(c, cudaStreamSynchronize(c->stream));

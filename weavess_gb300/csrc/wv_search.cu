@@ -40,6 +40,7 @@
 
 #include "warp_sort.cuh"
 #include "wv_common.cuh"
+#include "wv_lowp.cuh"
 #include "wv_search.h"
 
 namespace wv {
@@ -276,16 +277,20 @@ __device__ __forceinline__ float batch_dist(const float *__restrict__ base, uint
     constexpr int G = 8;
     for (int c0 = 0; c0 < cnt; c0 += G) {
       float part[G];
-#pragma unroll
-      for (int g = 0; g < G; g++) part[g] = 0.f;
+      const float4 *row[G];
 #pragma unroll
       for (int g = 0; g < G; g++) {
         const int c = c0 + g;
         const uint32_t id = __shfl_sync(FULL, my, c & 31);
-        if (c < cnt) {
-          const float4 *row = reinterpret_cast<const float4 *>(base + (size_t)id * d);
-          for (uint32_t k = lane; k < d4; k += 32) part[g] += group4(__ldg(row + k), q4[k]);
-        }
+        part[g] = 0.f;
+        row[g] = c < cnt ? reinterpret_cast<const float4 *>(base + (size_t)id * d) : nullptr;
+      }
+      // chunk-major: the G rows' loads of one step are independent
+      for (uint32_t k = lane; k < d4; k += 32) {
+        const float4 qk = q4[k];
+#pragma unroll
+        for (int g = 0; g < G; g++)
+          if (row[g]) part[g] += group4(__ldg(row[g] + k), qk);
       }
 #pragma unroll
       for (int g = 0; g < G; g++) {
@@ -303,48 +308,9 @@ __device__ __forceinline__ float batch_dist(const float *__restrict__ base, uint
   return out;
 }
 
-// distances of `cnt` rows to the query from the low-precision copy: one warp
-// per row, lanes over groups of four dimensions, FP32 accumulation
-__device__ __forceinline__ float lowp_dist(const SearchArgs &a, uint32_t my, int cnt, const float *qv, int lane) {
-  float out = 0.f;
-  const uint32_t d4 = a.d >> 2;
-  const float4 *q4 = reinterpret_cast<const float4 *>(qv);
-  for (int c = 0; c < cnt; c++) {
-    const uint32_t id = __shfl_sync(FULL, my, c);
-    float part = 0.f;
-    if (a.storage == 1) {
-      const uint2 *row = reinterpret_cast<const uint2 *>(a.qbase) + (size_t)id * d4;
-      for (uint32_t k = lane; k < d4; k += 32) {
-        const uint2 v = __ldg(row + k);
-        const float2 x01 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&v.x));
-        const float2 x23 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&v.y));
-        const float4 q = q4[k];
-        const float e0 = q.x - x01.x, e1 = q.y - x01.y, e2 = q.z - x23.x, e3 = q.w - x23.y;
-        part += e0 * e0 + e1 * e1 + e2 * e2 + e3 * e3;
-      }
-    } else {
-      const uint32_t *row = reinterpret_cast<const uint32_t *>(a.qbase) + (size_t)id * d4;
-      const float sc = __ldg(a.qscale + id);
-      for (uint32_t k = lane; k < d4; k += 32) {
-        const uint32_t v = __ldg(row + k);
-        const __half2_raw h01 = __nv_cvt_fp8x2_to_halfraw2((__nv_fp8x2_storage_t)(v & 0xffffu), __NV_E4M3);
-        const __half2_raw h23 = __nv_cvt_fp8x2_to_halfraw2((__nv_fp8x2_storage_t)(v >> 16), __NV_E4M3);
-        const float2 x01 = __half22float2(*reinterpret_cast<const __half2 *>(&h01));
-        const float2 x23 = __half22float2(*reinterpret_cast<const __half2 *>(&h23));
-        const float4 q = q4[k];
-        const float e0 = q.x - sc * x01.x, e1 = q.y - sc * x01.y, e2 = q.z - sc * x23.x, e3 = q.w - sc * x23.y;
-        part += e0 * e0 + e1 * e1 + e2 * e2 + e3 * e3;
-      }
-    }
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(FULL, part, o);
-    if (lane == c) out = part;
-  }
-  return out;
-}
-
 __device__ __forceinline__ float cand_dist(const SearchArgs &a, bool ints, uint32_t my, int cnt, const float *qv,
                                            int lane) {
-  if (a.storage != 0) return lowp_dist(a, my, cnt, qv, lane);
+  if (a.storage != 0) return lowp_rows_dist(LowpRows{a.qbase, a.qscale, a.storage, a.d}, my, cnt, qv, lane);
   return ints ? batch_dist<true>(a.base, a.d, my, cnt, qv, lane) : batch_dist<false>(a.base, a.d, my, cnt, qv, lane);
 }
 
@@ -434,18 +400,21 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
       if (lane == 0) pi[k] = node;  // flag = false
       __syncwarp();
       hcount++;
-      uint32_t deg = a.gdeg[node];
+      const uint32_t *row = a.gids + (size_t)node * a.gw;
+      // the degree and the first 32 slots of the row are loaded together
+      // (slots past the degree are read but ignored; rows are gw wide)
+      uint32_t deg = __ldg(a.gdeg + node);
+      const uint32_t head = lane < a.gw ? __ldg(row + lane) : INVALID;
       if (deg > a.gw) {
         set_err(a.status, DEV_BAD_ID);
         deg = a.gw;
       }
-      const uint32_t *row = a.gids + (size_t)node * a.gw;
       const float thr = pd[L - 1];
       // 1) the fresh neighbours, in adjacency order
       uint32_t nfresh = 0;
       for (uint32_t m0 = 0; m0 < deg; m0 += 32) {
         const uint32_t m = m0 + lane;
-        uint32_t id = m < deg ? __ldg(row + m) : INVALID;
+        uint32_t id = m < deg ? (m0 == 0 ? head : __ldg(row + m)) : INVALID;
         if (id != INVALID && id >= a.n) {
           set_err(a.status, DEV_BAD_ID);
           id = INVALID;

@@ -182,6 +182,11 @@ class Context:
     def learn_set_margin(self, margin: float):
         self._check(self.L.wv_learn_set_margin(self.h, margin))
 
+    def learn_plain_beam(self) -> int:
+        v = C.c_uint32()
+        self._check(self.L.wv_learn_plain_beam(self.h, C.byref(v)))
+        return int(v.value)
+
     def search_learned(self, queries, K: int = 10, return_L=False):
         q = _f32(queries)
         nq = q.shape[0]
