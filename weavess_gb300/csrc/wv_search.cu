@@ -49,6 +49,10 @@ namespace {
 
 constexpr int WARPS = 4;  // warps per block
 constexpr uint32_t EMPTY = 0xffffffffu;
+// a visited-hash entry of an unexpanded seed: route mode does not mark seeds
+// visited, so the first time a seed comes back as a neighbour it is still
+// counted (and rejected as already pooled); ids are below 2^31
+constexpr uint32_t SEEDBIT = 0x80000000u;
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 __host__ __device__ inline uint32_t pow2_at_least(uint32_t x) {
@@ -56,29 +60,30 @@ __host__ __device__ inline uint32_t pow2_at_least(uint32_t x) {
   while (p < x) p <<= 1;
   return p;
 }
-// pool arrays: room for L + 1 entries and for the bitonic sort of nextpow2(L)
-__host__ __device__ inline uint32_t pool_cap(uint32_t Lmax) { return max(pow2_at_least(Lmax), Lmax + 1); }
-// hash slots: >= 2048, and room for the seed sort's partition scratch
+// pool: L entries, merged in place
+__host__ __device__ inline uint32_t pool_cap(uint32_t Lmax) { return (Lmax + 3) & ~3u; }
+// hash slots (a power of two): >= 2048, and room for the seed sort's scratch
+// (the bitonic keys 2 * pow2(L) <= pow2(2L + 256), the introsort's
+// 2L + 256 words, the rerank's 2L words)
 __host__ __device__ inline uint32_t hash_cap(uint32_t Lmax) { return pow2_at_least(max(2048u, 2 * Lmax + 256)); }
 
 struct WarpSmem {
-  uint32_t *hash;  // hcap
+  uint32_t *hash;  // hcap words: visited set; scratch of the seed sort and the rerank
   float *qv;       // dpad
-  float *pa_d;     // pool A (pcap)
-  uint32_t *pa_i;
-  float *pb_d;     // pool B (pcap)
-  uint32_t *pb_i;
-  float *cd;       // accepted candidates (cap)
-  uint32_t *ci;
-  uint32_t *fi;    // fresh ids of one expansion (cap)
+  float *pd;       // pool distances (pcap), directly followed by
+  uint32_t *pi;    // pool ids | FLAG (unexpanded) (pcap)
+  float *cd;       // accepted candidates of one expansion, adjacency order (cap)
+  uint32_t *ci;    //   (then the candidates' insertion bounds)
+  float *sd;       // accepted candidates sorted (cap)
+  uint32_t *si;    //   (before that: the expansion's fresh ids)
 };
 
 __host__ __device__ inline size_t warp_smem_bytes(uint32_t d, uint32_t Lmax, uint32_t cap) {
   size_t b = 0;
   b += align16((size_t)hash_cap(Lmax) * 4);
   b += align16(((d + 3) & ~3u) * 4);
-  b += 4 * align16((size_t)pool_cap(Lmax) * 4);
-  b += 3 * align16(cap * 4);
+  b += 2 * align16((size_t)pool_cap(Lmax) * 4);
+  b += 4 * align16(cap * 4);
   return b;
 }
 
@@ -89,19 +94,17 @@ __device__ inline WarpSmem carve(uint8_t *p, uint32_t d, uint32_t Lmax, uint32_t
   p += align16((size_t)hash_cap(Lmax) * 4);
   s.qv = (float *)p;
   p += align16(((d + 3) & ~3u) * 4);
-  s.pa_d = (float *)p;
+  s.pd = (float *)p;
   p += align16((size_t)pc * 4);
-  s.pa_i = (uint32_t *)p;
-  p += align16((size_t)pc * 4);
-  s.pb_d = (float *)p;
-  p += align16((size_t)pc * 4);
-  s.pb_i = (uint32_t *)p;
+  s.pi = (uint32_t *)p;
   p += align16((size_t)pc * 4);
   s.cd = (float *)p;
   p += align16(cap * 4);
   s.ci = (uint32_t *)p;
   p += align16(cap * 4);
-  s.fi = (uint32_t *)p;
+  s.sd = (float *)p;
+  p += align16(cap * 4);
+  s.si = (uint32_t *)p;
   return s;
 }
 
@@ -116,21 +119,12 @@ __device__ inline int first_flag(const uint32_t *pi, int from, int L, int lane) 
 }
 
 // number of entries of the sorted array a[0..n) with a[i] <= x (upper bound)
-__device__ inline int upper_bound_f(const float *a, int n, float x) {
+template <class T>
+__device__ inline int upper_bound_of(const T *a, int n, T x) {
   int lo = 0, hi = n;
   while (lo < hi) {
     int mid = (lo + hi) >> 1;
     if (a[mid] <= x) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-// number of entries with a[i] < x (lower bound)
-__device__ inline int lower_bound_f(const float *a, int n, float x) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (a[mid] < x) lo = mid + 1;
     else hi = mid;
   }
   return lo;
@@ -153,22 +147,48 @@ struct Visited {
     spill = false;
     ntouch = 0;
   }
+  // route mode: records the seeds (not visited) so that a seed met again is
+  // known; warp-uniform call, ids distinct among the `want` lanes; the hash
+  // has room for every seed (limit >= SEARCH_MAX_L + 128)
+  __device__ void add_seed(bool want, uint32_t id) {
+    bool added = false;
+    if (want) {
+      uint32_t h = hslot(id, mask);
+      while (true) {
+        const uint32_t old = atomicCAS(&hash[h], EMPTY, id | SEEDBIT);
+        if (old == EMPTY) {
+          added = true;
+          break;
+        }
+        if (old == (id | SEEDBIT)) break;
+        h = (h + 1) & mask;
+      }
+    }
+    inserted += __popc(__ballot_sync(FULL, added));
+  }
   // warp-uniform call; `want` lanes test `id` (ids distinct among lanes);
-  // returns true for lanes whose id was not visited before
-  __device__ bool test_and_set(bool want, uint32_t id, int lane) {
+  // returns true for lanes whose id was not visited before; `seed` is set
+  // for a fresh id that is a recorded seed (still unvisited until now)
+  __device__ bool test_and_set(bool want, uint32_t id, int lane, bool &seed) {
     const unsigned wm = __ballot_sync(FULL, want);
     if (!spill && inserted + __popc(wm) > limit) spill = true;
-    bool fresh = false, newword = false;
+    bool fresh = false, newword = false, added = false;
+    seed = false;
     if (want) {
       uint32_t h = hslot(id, mask);
       if (!spill) {
         while (true) {
           const uint32_t old = atomicCAS(&hash[h], EMPTY, id);
           if (old == EMPTY) {
-            fresh = true;
+            fresh = added = true;
             break;
           }
           if (old == id) break;
+          if (old == (id | SEEDBIT)) {  // only this lane holds this id
+            hash[h] = id;
+            fresh = seed = true;
+            break;
+          }
           h = (h + 1) & mask;
         }
       } else {
@@ -177,6 +197,11 @@ struct Visited {
           const uint32_t v = hash[h];
           if (v == id) {
             in_hash = true;
+            break;
+          }
+          if (v == (id | SEEDBIT)) {
+            hash[h] = id;
+            in_hash = fresh = seed = true;
             break;
           }
           if (v == EMPTY) break;
@@ -190,8 +215,7 @@ struct Visited {
         }
       }
     }
-    const unsigned fm = __ballot_sync(FULL, fresh);
-    if (!spill) inserted += __popc(fm);
+    if (!spill) inserted += __popc(__ballot_sync(FULL, added));
     const unsigned nwm = __ballot_sync(FULL, newword);
     if (newword) touched[ntouch + __popc(nwm & ((1u << lane) - 1u))] = id >> 5;
     ntouch += __popc(nwm);
@@ -199,17 +223,19 @@ struct Visited {
   }
 };
 
-// Orders the L seeds (pa_*, in drawn order) into pb_* exactly as std::sort
-// would, flags set.  A bitonic sort on (dist, seed position) gives the stable
-// order, which is std::sort's whenever L <= 16 or no two seed distances tie;
-// otherwise the warp replays libstdc++'s introsort (warp_sort.cuh).  Uses the
-// hash area as scratch (the caller clears it afterwards).
+// Orders the L seeds -- (dist, id) pairs in drawn order, stored as DI over the
+// pool region -- into the pool exactly as std::sort would, flags set.  A
+// bitonic sort on (dist, seed position) gives the stable order, which is
+// std::sort's whenever L <= 16 or no two seed distances tie; otherwise the
+// warp replays libstdc++'s introsort (warp_sort.cuh) on the drawn order.  The
+// hash area is the scratch (the caller clears it afterwards).
 __device__ void sort_seeds(WarpSmem &s, int L, int lane) {
   const int P = (int)pow2_at_least((uint32_t)L);
-  float *kd = s.pb_d;
-  uint32_t *kx = s.pb_i;
+  const DI *dv = reinterpret_cast<const DI *>(s.pd);
+  float *kd = reinterpret_cast<float *>(s.hash);
+  uint32_t *kx = s.hash + P;
   for (int i = lane; i < P; i += 32) {
-    kd[i] = i < L ? s.pa_d[i] : __int_as_float(0x7f800000);
+    kd[i] = i < L ? dv[i].d : __int_as_float(0x7f800000);
     kx[i] = i;
   }
   __syncwarp();
@@ -237,28 +263,26 @@ __device__ void sort_seeds(WarpSmem &s, int L, int lane) {
   for (int i = lane + 1; i < L; i += 32) tie |= kd[i] == kd[i - 1];
   tie = __any_sync(FULL, tie);
   if (!tie || L <= 16) {
-    // kd already holds the sorted distances; each lane rewrites its own slots
-    for (int i = lane; i < L; i += 32) s.pb_i[i] = s.pa_i[kx[i]] | FLAG;
-  } else {
-    // ties and L > 16: replay libstdc++ introsort on the drawn order; the
-    // pairs sort in the B pool region (pb_d and pb_i are contiguous,
-    // 2 * pcap >= 2L words), the partition scratch sits in the hash area
+    for (int i = lane; i < L; i += 32) kx[i] = dv[kx[i]].i;
     __syncwarp();
-    DI *tmp = reinterpret_cast<DI *>(s.pb_d);
-    for (int i = lane; i < L; i += 32) tmp[i] = DI{s.pa_d[i], s.pa_i[i]};
-    int *scr = reinterpret_cast<int *>(s.hash);
-    __syncwarp();
-    warp_std_sort(tmp, L, DILess(), WarpSortScratch{scr, scr + L, scr + 2 * L, scr + 2 * L + 192}, lane);
-    // unpack through pool A (the drawn order is no longer needed)
     for (int i = lane; i < L; i += 32) {
-      const DI x = tmp[i];
-      s.pa_d[i] = x.d;
-      s.pa_i[i] = x.i;
+      s.pd[i] = kd[i];
+      s.pi[i] = kx[i] | FLAG;
     }
+  } else {
+    // ties and L > 16: libstdc++ introsort on the drawn order, in place over
+    // the pool region (pd and pi are contiguous, 2 * pcap >= 2L words), the
+    // partition scratch in the hash area; unpacked through the hash area
+    __syncwarp();
+    DI *tmp = reinterpret_cast<DI *>(s.pd);
+    int *scr = reinterpret_cast<int *>(s.hash);
+    warp_std_sort(tmp, L, DILess(), WarpSortScratch{scr, scr + L, scr + 2 * L, scr + 2 * L + 192}, lane);
+    DI *cp = reinterpret_cast<DI *>(s.hash);
+    for (int i = lane; i < L; i += 32) cp[i] = tmp[i];
     __syncwarp();
     for (int i = lane; i < L; i += 32) {
-      s.pb_d[i] = s.pa_d[i];
-      s.pb_i[i] = s.pa_i[i] | FLAG;
+      s.pd[i] = cp[i].d;
+      s.pi[i] = cp[i].i | FLAG;
     }
   }
   __syncwarp();
@@ -338,6 +362,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
   vis.spill = false;
   unsigned long long dcount = 0, hcount = 0;
   const unsigned lt = (1u << lane) - 1u;
+  float *pd = s.pd;
+  uint32_t *pi = s.pi;
 
   while (true) {
     uint32_t q = 0;
@@ -355,10 +381,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
     }
     // integer base and query: any summation order gives the reference's value
     const bool ints = a.int_exact && a.d <= 256 && __all_sync(FULL, qint);
-    // ---- seeds (SearchEntryInner): distances in drawn order ----
+    // ---- seeds (SearchEntryInner): distances in drawn order, as (dist, id)
+    // pairs over the pool region ----
     const uint32_t *seeds = a.seeds + (size_t)q * a.seed_stride;
     uint32_t nvis = 0;
     DI *vis_out = BUILD ? a.vis + (size_t)q * a.vcap : nullptr;
+    DI *drawn = reinterpret_cast<DI *>(s.pd);
     __syncwarp();
     for (int b = 0; b < L; b += 32) {
       const int cnt = min(32, L - b);
@@ -369,8 +397,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
       }
       const float dist = cand_dist(a, ints, id, cnt, s.qv, lane);
       if (lane < cnt) {
-        s.pa_d[b + lane] = dist;
-        s.pa_i[b + lane] = id;
+        drawn[b + lane] = DI{dist, id};
         if (BUILD && nvis + lane < a.vlimit) vis_out[nvis + lane] = DI{dist, id};
       }
       nvis += cnt;
@@ -379,18 +406,21 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
     __syncwarp();
     sort_seeds(s, L, lane);
     vis.clear(lane);  // the seed sort used the hash as scratch
-    if (BUILD) {
-      // CandidateNSG flags its seeds (component_candidate.cpp:21-29)
-      for (int b = 0; b < L; b += 32) {
-        const int i = b + lane;
-        const uint32_t id = i < L ? (s.pb_i[i] & ID_MASK) : EMPTY;
-        // duplicate seeds among lanes: only the first tests
-        const unsigned same = __match_any_sync(FULL, id);
-        vis.test_and_set(i < L && (__ffs(same) - 1) == lane, id, lane);
+    // CandidateNSG flags its seeds (component_candidate.cpp:21-29); the route
+    // leaves them unvisited and records them as seeds
+    for (int b = 0; b < L; b += 32) {
+      const int i = b + lane;
+      const uint32_t id = i < L ? (pi[i] & ID_MASK) : EMPTY;
+      // duplicate seeds among lanes: only the first records
+      const unsigned same = __match_any_sync(FULL, id);
+      const bool first = i < L && (__ffs(same) - 1) == lane;
+      if (BUILD) {
+        bool sd;
+        vis.test_and_set(first, id, lane, sd);
+      } else {
+        vis.add_seed(first, id);
       }
     }
-    float *pd = s.pb_d, *od = s.pa_d;
-    uint32_t *pi = s.pb_i, *oi = s.pa_i;
 
     // ---- route (RouteInner) ----
     int k = first_flag(pi, 0, L, lane);
@@ -410,7 +440,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
         deg = a.gw;
       }
       const float thr = pd[L - 1];
-      // 1) the fresh neighbours, in adjacency order
+      // 1) the fresh neighbours, in adjacency order (a seed marked SEEDBIT)
       uint32_t nfresh = 0;
       for (uint32_t m0 = 0; m0 < deg; m0 += 32) {
         const uint32_t m = m0 + lane;
@@ -422,31 +452,27 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
         // a repeated id inside this chunk: only its first position visits it
         const unsigned same = __match_any_sync(FULL, id);
         const bool leader = (__ffs(same) - 1) == lane;
-        const bool fresh = vis.test_and_set(id != INVALID && leader, id, lane);
+        bool was_seed;
+        const bool fresh = vis.test_and_set(id != INVALID && leader, id, lane, was_seed);
         const unsigned fm = __ballot_sync(FULL, fresh);
-        if (fresh) s.fi[nfresh + __popc(fm & lt)] = id;
+        if (fresh) s.si[nfresh + __popc(fm & lt)] = id | (was_seed ? SEEDBIT : 0u);
         nfresh += __popc(fm);
       }
       __syncwarp();
-      // 2) their distances, 3) the accepted ones in adjacency order
+      // 2) their distances, 3) the accepted ones in adjacency order: closer
+      // than the pool's last entry, and not a seed (a seed still closer than
+      // the last entry is still in the pool: InsertIntoPool rejects it)
       int ncand = 0;
       for (uint32_t b = 0; b < nfresh; b += 32) {
         const int cnt = (int)min(32u, nfresh - b);
-        const uint32_t my = lane < cnt ? s.fi[b + lane] : 0u;
+        const uint32_t raw = lane < cnt ? s.si[b + lane] : 0u;
+        const uint32_t my = raw & ID_MASK;
         const float dist = cand_dist(a, ints, my, cnt, s.qv, lane);
         if (BUILD) {
           if (lane < cnt && nvis + lane < a.vlimit) vis_out[nvis + lane] = DI{dist, my};
           nvis += cnt;
         }
-        bool acc = false;
-        if (lane < cnt && dist < thr) {
-          // reject an id already in the pool (an unvisited seed): same id
-          // implies same distance, so look inside the run of equal distances
-          int lo = lower_bound_f(pd, L, dist), hi = upper_bound_f(pd, L, dist);
-          acc = true;
-          for (int t = lo; t < hi; t++)
-            if ((pi[t] & ID_MASK) == my) acc = false;
-        }
+        const bool acc = lane < cnt && dist < thr && !(raw & SEEDBIT);
         const unsigned am = __ballot_sync(FULL, acc);
         if (acc) {
           const int r = ncand + __popc(am & lt);
@@ -459,11 +485,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
       __syncwarp();
       int nk = L;
       if (ncand > 0) {
-        // stable rank of each candidate by distance (adjacency order on ties)
-        float myd[8];
-        uint32_t myi[8];
-        int myr[8];
-        int nmine = 0;
+        // stable order of the candidates by distance (adjacency order on ties)
         for (int c = lane; c < ncand; c += 32) {
           const float dc = s.cd[c];
           int r = 0;
@@ -471,41 +493,52 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
             const float d2 = s.cd[c2];
             r += (d2 < dc) || (d2 == dc && c2 < c);
           }
-          myd[nmine] = dc;
-          myi[nmine] = s.ci[c];
-          myr[nmine] = r;
-          nmine++;
+          s.sd[r] = dc;
+          s.si[r] = s.ci[c];
         }
         __syncwarp();
-        for (int t = 0; t < nmine; t++) s.cd[myr[t]] = myd[t];  // sorted distances
-        __syncwarp();
-        // pool entries move down by the number of strictly closer candidates
-        for (int j = lane; j < L; j += 32) {
-          const int pos = j + lower_bound_f(s.cd, ncand, pd[j]);
-          if (pos < L) {
-            od[pos] = pd[j];
-            oi[pos] = pi[j];
-          }
-        }
-        // candidates go after every pool entry of equal or smaller distance
+        // candidate c goes after every pool entry of equal or smaller
+        // distance: final position ub[c] + c (ub non-decreasing in c)
+        uint32_t *ub = s.ci;
         int mink = L;
-        for (int t = 0; t < nmine; t++) {
-          const int pos = myr[t] + upper_bound_f(pd, L, myd[t]);
-          if (pos < L) {
-            od[pos] = myd[t];
-            oi[pos] = myi[t] | FLAG;
-            mink = min(mink, pos);
-          }
+        for (int c = lane; c < ncand; c += 32) {
+          const int u = upper_bound_of(pd, L, s.sd[c]);
+          ub[c] = (uint32_t)u;
+          if (u + c < L) mink = min(mink, u + c);
         }
         for (int o = 16; o > 0; o >>= 1) mink = min(mink, __shfl_xor_sync(FULL, mink, o));
+        __syncwarp();
+        // pool entry j moves down by the number of candidates placed before
+        // it (those with ub <= j); in place, from the end, 32 at a time: a
+        // chunk is read before it is written and only moves to higher slots
+        const int lo = (int)ub[0];
+        for (int jt = L; jt > lo; jt -= 32) {
+          const int j = jt - 32 + lane;
+          const bool act = j >= lo;
+          float v = 0.f;
+          uint32_t id = 0;
+          int pos = L;
+          if (act) {
+            v = pd[j];
+            id = pi[j];
+            pos = j + upper_bound_of(ub, ncand, (uint32_t)j);
+          }
+          __syncwarp();
+          if (act && pos < L) {
+            pd[pos] = v;
+            pi[pos] = id;
+          }
+          __syncwarp();
+        }
+        for (int c = lane; c < ncand; c += 32) {
+          const int pos = (int)ub[c] + c;
+          if (pos < L) {
+            pd[pos] = s.sd[c];
+            pi[pos] = s.si[c] | FLAG;
+          }
+        }
         nk = mink;
         __syncwarp();
-        float *t1 = pd;
-        pd = od;
-        od = t1;
-        uint32_t *t2 = pi;
-        pi = oi;
-        oi = t2;
       }
       const int next = (nk <= k) ? nk : k + 1;
       k = first_flag(pi, next, L, lane);
@@ -513,28 +546,30 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
     // ---- exact FP32 rerank of the final pool (low-precision storage) ----
     if (!BUILD && a.storage != 0 && a.rerank > 0) {
       const int R = min((int)a.rerank, L);
+      float *xd = reinterpret_cast<float *>(s.hash);  // the visited set is done with
+      uint32_t *xi = s.hash + R;
       for (int b = 0; b < R; b += 32) {
         const int cnt = min(32, R - b);
         const uint32_t id = lane < cnt ? (pi[b + lane] & ID_MASK) : 0u;
         const float ex = ints ? batch_dist<true>(a.base, a.d, id, cnt, s.qv, lane)
                               : batch_dist<false>(a.base, a.d, id, cnt, s.qv, lane);
         if (lane < cnt) {
-          od[b + lane] = ex;
-          oi[b + lane] = id;
+          xd[b + lane] = ex;
+          xi[b + lane] = id;
         }
       }
       dcount += R;
       __syncwarp();
       // stable order by the exact distance (pool position breaks ties)
       for (int c = lane; c < R; c += 32) {
-        const float dc = od[c];
+        const float dc = xd[c];
         int r = 0;
         for (int c2 = 0; c2 < R; c2++) {
-          const float d2 = od[c2];
+          const float d2 = xd[c2];
           r += (d2 < dc) || (d2 == dc && c2 < c);
         }
-        pd[r] = dc;  // pd / pi receive the re-sorted head of the pool
-        pi[r] = oi[c];
+        pd[r] = dc;  // the head of the pool, re-sorted
+        pi[r] = xi[c];
       }
       __syncwarp();
     }
@@ -548,6 +583,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
         a.out_ids[(size_t)q * a.out_stride + i] = pi[i] & ID_MASK;
         if (a.out_dist) a.out_dist[(size_t)q * a.out_stride + i] = pd[i];
       }
+    __syncwarp();
     vis.clear(lane);
   }
   if (!BUILD && lane == 0 && a.counters) {
