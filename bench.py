@@ -107,10 +107,12 @@ class Clocks:
 PROFILE_REGION = "search"  # which region a cudaProfilerStart/Stop pair brackets (for ncu --profile-from-start off)
 
 
-def timed_steps(step, steps, stream, flush, clk):
+def timed_steps(step, steps, stream, flush, clk, after=None):
     """`steps` CUDA-event-timed calls of `step` (L2 flushed before each), with
     the clock sampler running; the same steps continue untimed until the
-    sampler has three readings from the timed region on.  Returns per-step ms."""
+    sampler has three readings from the timed region on.  `after(i)` runs
+    after step i is enqueued (e.g. to read its kernel time).  Returns per-step
+    ms."""
     import torch
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     torch.cuda.synchronize()
@@ -122,6 +124,8 @@ def timed_steps(step, steps, stream, flush, clk):
         ev[i][0].record(stream)
         step()
         ev[i][1].record(stream)
+        if after is not None:
+            after(i)
     torch.cuda.synchronize()
     if PROFILE_REGION == "search":
         torch.cuda.profiler.stop()
@@ -221,34 +225,56 @@ def run_learned(ctx, cfg, base, query, gt, args, dev, stream, flush):
             break
     ctx.learn_set_margin(chosen)
     nq, K = query.shape[0], cfg["k"]
-    ctx.srand(777)
-    pseeds = ctx.draw_seeds(nq, cfg["L_trace"], "rand")
+    # the batched form: a plan bound to device buffers, launch shape tuned on
+    # these queries, the whole step (forward pass, seeds, search) one graph
     dq = torch.from_numpy(query).to(dev)
-    dps = torch.from_numpy(pseeds.astype(np.int32)).to(dev)
     dout = torch.empty((nq, K), dtype=torch.int32, device=dev)
-    counters = None
+    plan = ctx.plan(nq, K, dq.data_ptr(), dout.data_ptr(), mode="learned")
+    tune = plan.tune(nq)
+    log(f"plan tuning {tune}")
+    plan.run(nq)
+    counters = plan.wait()
     for _ in range(args.warmup):
-        counters = ctx.search_learned_device(dq.data_ptr(), nq, K, dps.data_ptr(), dout.data_ptr(), counters=True)
+        plan.run(nq)
+        plan.wait()
+    kms = []
     with Clocks() as clk:
-        step_ms = timed_steps(lambda: ctx.search_learned_device(dq.data_ptr(), nq, K, dps.data_ptr(), dout.data_ptr()),
-                              args.steps, stream, flush, clk)
+        step_ms = timed_steps(lambda: plan.run(nq), args.steps, stream, flush, clk,
+                              after=lambda i: kms.append(plan.search_ms()))
+    plan.wait()
     ms = float(np.mean(step_ms))
     res = dout.cpu().numpy().astype(np.uint32)
     r_test = recall(res, gt, K)
-    # e2e through the public host-buffer call
-    qpin = torch.from_numpy(query).pin_memory().numpy()
-    _, _, _, Ls = ctx.search_learned(qpin, K, return_L=True)
-    plain_beam = ctx.learn_plain_beam()  # host-drawn plain seeds per query the call copies (0: none)
+    # e2e through the public plan API: pinned host queries in, ids out
+    qpin = torch.from_numpy(query).pin_memory()
+    opin = torch.empty((nq, K), dtype=torch.int32).pin_memory()
     e2e_t = []
+    for _ in range(args.steps + 1):
+        t0 = time.perf_counter()
+        dq.copy_(qpin, non_blocking=True)
+        plan.run(nq)
+        opin.copy_(dout, non_blocking=True)
+        plan.wait()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_t = e2e_t[1:]
+    assert np.array_equal(opin.numpy().view(np.uint32), res)
+    plan.close()
+    # and through the one-call host API (wv_search_learned)
+    qnp = qpin.numpy()
+    _, _, _, Ls = ctx.search_learned(qnp, K, return_L=True)
+    plain_beam = ctx.learn_plain_beam()  # host-drawn plain seeds per query the call copies (0: none)
+    call_t = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        ctx.search_learned(qpin, K)
-        e2e_t.append(time.perf_counter() - t0)
+        ctx.search_learned(qnp, K)
+        call_t.append(time.perf_counter() - t0)
     ctx.set_precision("fp32")
     dc, hc = counters
     return {"qps": nq / (ms / 1e3), "ms": ms, "recall@10": r_test, "e2e_qps": nq / float(np.mean(e2e_t)),
-            "margin": chosen, "mean_L": float(Ls.mean()), "fit_s": fit_s, "report": rep, "dist_count": dc,
-            "hop_count": hc, "n_train": nt, "plain_seeds_per_query": plain_beam, "clocks": clk.summary()}
+            "e2e_call_qps": nq / float(np.mean(call_t)), "margin": chosen, "mean_L": float(Ls.mean()),
+            "fit_s": fit_s, "report": rep, "dist_count": dc, "hop_count": hc, "n_train": nt,
+            "plain_seeds_per_query": plain_beam, "tuned_shape": tune["chosen"], "tune": tune["tried"],
+            "search_kernel_ms": float(np.mean(kms)), "clocks": clk.summary()}
 
 
 def run_ours(args):
@@ -345,19 +371,22 @@ def run_ours(args):
         ldc, lhc = learned["dist_count"], learned["hop_count"]
         # bf16 candidate rows (2d bytes), graph rows, query rows
         alg = ldc * d * 2 + lhc * (avg_deg * 4 + 4) + nq * d * 4
-        l_achieved = alg / (head_ms / 1e3) / 1e9
+        l_achieved = alg / (learned["search_kernel_ms"] / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": round(l_achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(l_achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
                 "alg_bytes_per_launch": int(alg), "dist_count": ldc, "hop_count": lhc,
-                "kernel": "k_search (learned seeds, per-query L, bf16 candidate rows)"}
-        h2d = nq * d * 4 + nq * learned["plain_seeds_per_query"] * 4
+                "kernel": "k_search (learned seeds, per-query L, bf16 candidate rows)",
+                "kernel_ms": round(learned["search_kernel_ms"], 4),
+                "timing": "CUDA events captured around the search kernel in each timed replay"}
+        # queries, the replay's query count, the rand() values of the plain seeds (if any)
+        h2d = nq * d * 4 + 4 + (nq * 4 if learned["plain_seeds_per_query"] else 0)
         launches = args.steps * 6  # query normalisation, 3 GEMMs, the seed kernel, the search per step
     else:
         head_qps, head_ms, head_e2e = value, ms, e2e_qps
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
                 "alg_bytes_per_launch": int(alg_bytes), "dist_count": dc, "hop_count": hc, "kernel": "k_search"}
-        h2d = nq * d * 4 + nq * Lsel * 4
+        h2d = nq * d * 4 + nq * 4  # queries and one rand() value per query (seeds drawn on the device)
         launches = args.steps
     line = {
         "metric": METRIC, "value": round(head_qps, 1), "unit": "queries/s", "n_gpus": 1, "steps": args.steps,

@@ -213,6 +213,60 @@ int wv_learn_grad(wv_ctx *ctx, const float *x, const uint32_t *y_cluster, const 
 /* The seed ids SearchEntryInner would draw for nq queries (host nq x L),
  * consuming the context's rand stream exactly as the reference does. */
 int wv_draw_seeds(wv_ctx *ctx, uint32_t nq, int entry, uint32_t L, uint32_t *seeds);
+/* The same SEARCH_ENTRY_RAND seeds written to device memory (row q at
+ * d_seeds + q * stride): one rand() per query on the host, the mt19937 /
+ * GenRandom draws on the device; asynchronous on the context's stream. */
+int wv_draw_seeds_device(wv_ctx *ctx, uint32_t nq, uint32_t L, uint32_t *d_seeds, uint32_t stride);
+
+/* ---- batched search plans (CUDA graphs, tuned launch shape) -------------- */
+/* No counterpart in the reference (IndexBuilder::search loops over queries,
+ * src/builder.cpp:445-454).  A plan binds one batch layout to caller-owned
+ * device buffers -- queries (nq_max x d), per-query L and K (nullable: L_max,
+ * K_max for every query), caller seeds (WV_PLAN_SEEDS: nq_max x L_max),
+ * result ids and distances (nq_max x out_stride) -- and captures the whole
+ * step as a CUDA graph: WV_PLAN_RAND draws SearchEntryRand seeds (one rand()
+ * per query from the context's stream, the mt19937 draws on the device),
+ * WV_PLAN_LEARNED runs the learned model's forward pass and picks each
+ * query's entry and L; then the search of the first nq queries (nq given at
+ * run time, <= nq_max) in one persistent launch.  Results equal
+ * wv_search_batch / wv_search_learned on the same inputs and rand stream.
+ * The caller rewrites its buffers between runs (after wv_plan_wait).  A plan
+ * refuses to run after the base, graph, precision or model changed; destroy
+ * plans before their context. */
+enum { WV_PLAN_RAND = 0, WV_PLAN_SEEDS = 1, WV_PLAN_LEARNED = 2 };
+typedef struct {
+  uint32_t nq_max, L_max, K_max, out_stride;
+  int mode;
+} wv_plan_params;
+typedef struct {
+  int warps_per_block;
+  uint32_t hash_slots; /* visited-hash slots per warp */
+  int blocks;
+  float ms; /* measured search time (tuning) */
+} wv_plan_shape;
+#define WV_TUNE_MAX 16
+typedef struct {
+  int n, chosen;
+  wv_plan_shape tried[WV_TUNE_MAX];
+} wv_tune_report;
+typedef struct wv_plan wv_plan;
+int wv_plan_create(wv_ctx *ctx, const wv_plan_params *p, const float *d_queries, const uint32_t *d_L,
+                   const uint32_t *d_K, const uint32_t *d_seeds, uint32_t *d_out_ids, float *d_out_dist,
+                   wv_plan **out);
+/* Enqueues one replay on the context's stream for the first nq queries
+ * (asynchronous; waits for the previous replay of this plan first). */
+int wv_plan_run(wv_plan *plan, uint32_t nq);
+/* Waits for the last replay; device-reported errors; counters (nullable). */
+int wv_plan_wait(wv_plan *plan, wv_counters *counters);
+/* Times the search of the current inputs (first nq queries) in every launch
+ * shape that fits, recaptures with the fastest; consumes one replay's rand()
+ * draws.  The report lists every shape tried. */
+int wv_plan_tune(wv_plan *plan, uint32_t nq, wv_tune_report *report);
+int wv_plan_shape_of(wv_plan *plan, wv_plan_shape *shape);
+/* Device time of the search kernel in the last replay (CUDA events captured
+ * around it in the graph); waits for the replay. */
+int wv_plan_search_ms(wv_plan *plan, float *ms);
+int wv_plan_destroy(wv_plan *plan);
 
 /* ---- allocation-free search ---------------------------------------------- */
 /* No counterpart in the reference: an extra entry point for callers that

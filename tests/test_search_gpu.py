@@ -56,6 +56,29 @@ def test_seed_draws_match_oracle(ctx, entry):
         assert ctx.rand() == r2.next()  # both streams advanced alike
 
 
+@pytest.mark.parametrize("n", [3000, 1601])
+def test_device_seed_draws_match_oracle(ctx, n):
+    """SEARCH_ENTRY_RAND seeds drawn on the device (one host rand() per query,
+    mt19937 + GenRandom per warp) equal the oracle's host draws, including
+    beams that need several mt19937 twists and N - L small."""
+    import torch
+    base, _ = ds.int_mixture(n, 16, 4, seed=3, n_query=0)
+    ctx.upload_base(base)
+    dummy = O.Graph(np.zeros((n, 1), np.uint32), np.zeros((n, 1), np.float32), np.zeros(n, np.uint32), 0)
+    for L in (1, 10, 17, 623, 624, 1000, 1536 if n > 1536 else n - 1):
+        ctx.srand(91)
+        r2 = O.Rand(91)
+        stride = L + 3
+        d = torch.full((37, stride), -1, dtype=torch.int32, device="cuda")
+        ctx.draw_seeds_device(37, L, d.data_ptr(), stride)
+        torch.cuda.synchronize()
+        got = d.cpu().numpy().view(np.uint32)
+        want = O.search_seeds(n, 37, dummy, L, r2, entry="rand")
+        assert np.array_equal(got[:, :L], want), L
+        assert np.all(got[:, L:] == 0xFFFFFFFF)
+        assert ctx.rand() == r2.next()
+
+
 @pytest.fixture(scope="module")
 def kgraph20k():
     base, query = ds.int_mixture(20000, 128, 32, seed=21, n_query=300)

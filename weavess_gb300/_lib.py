@@ -37,6 +37,19 @@ class LearnParams(C.Structure):
                 ("fallback_p", C.c_float), ("seed", C.c_uint32)]
 
 
+class PlanParams(C.Structure):
+    _fields_ = [("nq_max", C.c_uint32), ("L_max", C.c_uint32), ("K_max", C.c_uint32), ("out_stride", C.c_uint32),
+                ("mode", C.c_int)]
+
+
+class PlanShape(C.Structure):
+    _fields_ = [("warps_per_block", C.c_int), ("hash_slots", C.c_uint32), ("blocks", C.c_int), ("ms", C.c_float)]
+
+
+class TuneReport(C.Structure):
+    _fields_ = [("n", C.c_int), ("chosen", C.c_int), ("tried", PlanShape * 16)]
+
+
 class LearnReport(C.Structure):
     _fields_ = [("loss_ce", C.c_float), ("loss_mse", C.c_float), ("margin", C.c_float),
                 ("val_agreement", C.c_float), ("ms", C.c_float), ("mean_label_L", C.c_float),
@@ -88,6 +101,7 @@ def load(build_if_needed: bool = True):
                                   C.POINTER(Counters)]
     L.wv_search_device.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, vp, vp, vp, C.POINTER(Counters)]
     L.wv_draw_seeds.argtypes = [vp, C.c_uint32, C.c_int, C.c_uint32, u32p]
+    L.wv_draw_seeds_device.argtypes = [vp, C.c_uint32, C.c_uint32, vp, C.c_uint32]
     L.wv_set_graph.argtypes = [vp, u32p, vp, u32p, C.c_uint32, C.c_uint32, C.c_uint32]
     L.wv_graph_width.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
     L.wv_get_graph.argtypes = [vp, vp, vp, vp, C.c_uint32]
@@ -113,5 +127,12 @@ def load(build_if_needed: bool = True):
     L.wv_debug_sort.argtypes = [vp, f32p, u32p, u32p, C.c_uint32, C.c_int]
     L.wv_search_noalloc.argtypes = [vp, C.c_uint32, C.c_uint32, vp, vp, C.c_uint32, vp, C.c_uint32, vp, C.c_uint32,
                                     C.c_uint32, vp, vp, vp]
+    L.wv_plan_create.argtypes = [vp, C.POINTER(PlanParams), vp, vp, vp, vp, vp, vp, C.POINTER(vp)]
+    L.wv_plan_run.argtypes = [vp, C.c_uint32]
+    L.wv_plan_wait.argtypes = [vp, C.POINTER(Counters)]
+    L.wv_plan_tune.argtypes = [vp, C.c_uint32, C.POINTER(TuneReport)]
+    L.wv_plan_shape_of.argtypes = [vp, C.POINTER(PlanShape)]
+    L.wv_plan_search_ms.argtypes = [vp, C.POINTER(C.c_float)]
+    L.wv_plan_destroy.argtypes = [vp]
     _lib = L
     return L

@@ -36,7 +36,7 @@ __device__ __forceinline__ void flush_leaves(T *a, Less less, const int *leaf, i
 }
 
 template <class T, class Less>
-__device__ void warp_std_sort(T *a, int n, Less less, WarpSortScratch s, int lane) {
+__device__ __forceinline__ void warp_std_sort(T *a, int n, Less less, WarpSortScratch s, int lane) {
   if (n <= 1) return;
   const unsigned FULLM = 0xffffffffu;
   const unsigned lt = (1u << lane) - 1u;

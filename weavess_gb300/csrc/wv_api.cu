@@ -5,6 +5,7 @@
 #include "wv_ctx.h"
 #include "wv_learn.h"
 #include "wv_search.h"
+#include "wv_seeds.h"
 
 using namespace wv;
 
@@ -38,12 +39,13 @@ __global__ void k_check_int(const float *x, size_t count, int *ok) {
   }
 }
 
-int ensure_search_scratch(wv_ctx *c, uint32_t Lmax) {
+// status code; *out_blocks = the persistent grid of the shape
+int ensure_search_scratch(wv_ctx *c, uint32_t Lmax, SearchShape sh, int *out_blocks) {
   const uint32_t cap = c->gw + 32;
-  int blocks = search_grid(c->d, Lmax, cap, c->device);
+  int blocks = search_grid(c->d, Lmax, cap, c->device, sh);
   WV_CHECK(c, blocks > 0, WV_ERR_LIMIT, "search kernel cannot run with d=%u L=%u width=%u (shared memory)", c->d,
            Lmax, c->gw);
-  size_t slots = (size_t)blocks * search_warps_per_block();
+  size_t slots = (size_t)blocks * sh.wpb;
   size_t words = (c->n + 31) / 32;
   if (slots > c->vis_slots || words != c->vis_words) {
     c->visited.release();
@@ -54,18 +56,19 @@ int ensure_search_scratch(wv_ctx *c, uint32_t Lmax) {
     c->vis_slots = slots;
     c->vis_words = words;
   }
-  return blocks;
+  *out_blocks = blocks;
+  return WV_OK;
 }
 
 }  // namespace
 
-// runs the kernel on device-resident queries / seeds / outputs
-int wv::run_search_device(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t *d_seeds, uint32_t seed_stride,
-               const uint32_t *d_L, const uint32_t *d_K, uint32_t L, uint32_t K, uint32_t Lmax, uint32_t *d_out,
-               float *d_dist, uint32_t out_stride, wv_counters *counters) {
-  int blocks = ensure_search_scratch(c, Lmax);
-  if (blocks <= 0) return blocks < 0 ? -blocks : WV_ERR_LIMIT;
-  WV_CUDA(c, cudaMemsetAsync(c->misc.p, 0, 32, c->stream));
+int wv::search_prepare(wv_ctx *c, uint32_t Lmax, SearchShape shape, int *blocks) {
+  return ensure_search_scratch(c, Lmax, shape, blocks);
+}
+
+SearchArgs wv::search_args(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t *nq_dev, const uint32_t *d_seeds,
+                           uint32_t seed_stride, const uint32_t *d_L, const uint32_t *d_K, uint32_t L, uint32_t K,
+                           uint32_t Lmax, uint32_t *d_out, float *d_dist, uint32_t out_stride) {
   SearchArgs a{};
   a.base = c->base.as<float>();
   a.n = c->n;
@@ -75,6 +78,7 @@ int wv::run_search_device(wv_ctx *c, const float *d_q, uint32_t nq, const uint32
   a.gw = c->gw;
   a.queries = d_q;
   a.nq = nq;
+  a.nq_dev = nq_dev;
   a.seeds = d_seeds;
   a.seed_stride = seed_stride;
   a.Lq = d_L;
@@ -97,9 +101,29 @@ int wv::run_search_device(wv_ctx *c, const float *d_q, uint32_t nq, const uint32
   a.qbase = c->qbase.p;
   a.qscale = c->qscale.as<float>();
   a.rerank = c->rerank == 0 ? Lmax : c->rerank;
-  int nb = std::min<long>(blocks, ((long)nq + search_warps_per_block() - 1) / search_warps_per_block());
+  return a;
+}
+
+int wv::search_enqueue(wv_ctx *c, const SearchArgs &a, SearchShape shape, int blocks) {
+  WV_CUDA(c, cudaMemsetAsync(c->misc.p, 0, 32, c->stream));
+  WV_CUDA(c, launch_search(a, shape, blocks, c->stream));
+  return WV_OK;
+}
+
+// runs the kernel on device-resident queries / seeds / outputs
+int wv::run_search_device(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t *d_seeds, uint32_t seed_stride,
+               const uint32_t *d_L, const uint32_t *d_K, uint32_t L, uint32_t K, uint32_t Lmax, uint32_t *d_out,
+               float *d_dist, uint32_t out_stride, wv_counters *counters) {
+  const SearchShape sh{};
+  int blocks = 0;
+  int rc = search_prepare(c, Lmax, sh, &blocks);
+  if (rc) return rc;
+  const SearchArgs a =
+      search_args(c, d_q, nq, nullptr, d_seeds, seed_stride, d_L, d_K, L, K, Lmax, d_out, d_dist, out_stride);
+  int nb = std::min<long>(blocks, ((long)nq + sh.wpb - 1) / sh.wpb);
   if (nb < 1) nb = 1;
-  WV_CUDA(c, launch_search_exact(a, nb, c->stream));
+  rc = search_enqueue(c, a, sh, nb);
+  if (rc) return rc;
   if (counters) {
     unsigned long long h[2];
     WV_CUDA(c, cudaMemcpyAsync(h, c->d_counters(), 16, cudaMemcpyDeviceToHost, c->stream));
@@ -215,6 +239,7 @@ int wv_upload_base(wv_ctx *c, const float *base, uint32_t n, uint32_t d) {
   WV_CUDA(c, c->base.ensure((size_t)n * d * 4));
   WV_CUDA(c, cudaMemcpyAsync(c->base.p, base, (size_t)n * d * 4, cudaMemcpyHostToDevice, c->stream));
   WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->generation++;
   if (c->n != n) c->gn = 0;  // the old graph no longer matches
   c->storage = 0;            // a low-precision copy no longer matches
   c->n = n;
@@ -242,6 +267,7 @@ int wv_upload_graph(wv_ctx *c, const uint32_t *ids, const uint32_t *deg, uint32_
   WV_CUDA(c, cudaMemcpyAsync(c->gids.p, ids, (size_t)n * width * 4, cudaMemcpyHostToDevice, c->stream));
   WV_CUDA(c, cudaMemcpyAsync(c->gdeg.p, deg, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
   WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->generation++;
   c->gn = n;
   c->gw = width;
   c->ep = ep;
@@ -256,6 +282,15 @@ int wv_draw_seeds(wv_ctx *c, uint32_t nq, int entry, uint32_t L, uint32_t *seeds
   return draw(c, nq, entry, L, seeds, L);
 }
 
+int wv_draw_seeds_device(wv_ctx *c, uint32_t nq, uint32_t L, uint32_t *d_seeds, uint32_t stride) {
+  if (!c || !d_seeds) return WV_ERR_ARG;
+  WV_CHECK(c, c->n > 0 && L < c->n, WV_ERR_ARG, "L=%u must be smaller than n=%u", L, c->n);
+  WV_CHECK(c, stride >= L, WV_ERR_ARG, "stride %u < L=%u", stride, L);
+  if (nq == 0) return WV_OK;
+  WV_CUDA(c, cudaSetDevice(c->device));
+  return draw_seeds_rand_device(c, nq, nullptr, L, L, d_seeds, stride);
+}
+
 int wv_search(wv_ctx *c, const float *queries, uint32_t nq, int entry, uint32_t L, uint32_t K,
               const uint32_t *seeds, uint32_t *out_ids, float *out_dist, wv_counters *counters) {
   if (!c) return WV_ERR_ARG;
@@ -265,22 +300,27 @@ int wv_search(wv_ctx *c, const float *queries, uint32_t nq, int entry, uint32_t 
   if (counters) *counters = wv_counters{0, 0};
   if (nq == 0) return WV_OK;
   WV_CUDA(c, cudaSetDevice(c->device));
+  WV_CUDA(c, c->q_buf.ensure((size_t)nq * c->d * 4));
+  WV_CUDA(c, c->seed_buf.ensure((size_t)nq * L * 4));
+  WV_CUDA(c, c->out_ids_buf.ensure((size_t)nq * K * 4));
+  if (out_dist) WV_CUDA(c, c->out_dist_buf.ensure((size_t)nq * K * 4));
+  WV_CUDA(c, cudaMemcpyAsync(c->q_buf.p, queries, (size_t)nq * c->d * 4, cudaMemcpyHostToDevice, c->stream));
   std::vector<uint32_t> hs;
   if (entry == WV_ENTRY_SEEDS) {
     WV_CHECK(c, seeds != nullptr, WV_ERR_ARG, "WV_ENTRY_SEEDS needs seeds");
     for (size_t i = 0; i < (size_t)nq * L; i++) WV_CHECK(c, seeds[i] < c->n, WV_ERR_ARG, "seed id %u >= n", seeds[i]);
+  } else if (entry == WV_ENTRY_RAND) {
+    // one rand() per query on the host, the mt19937 draws on the device
+    rc = draw_seeds_rand_device(c, nq, nullptr, L, L, c->seed_buf.as<uint32_t>(), L);
+    if (rc) return rc;
   } else {
     hs.resize((size_t)nq * L);
     rc = draw(c, nq, entry, L, hs.data(), L);
     if (rc) return rc;
     seeds = hs.data();
   }
-  WV_CUDA(c, c->q_buf.ensure((size_t)nq * c->d * 4));
-  WV_CUDA(c, c->seed_buf.ensure((size_t)nq * L * 4));
-  WV_CUDA(c, c->out_ids_buf.ensure((size_t)nq * K * 4));
-  if (out_dist) WV_CUDA(c, c->out_dist_buf.ensure((size_t)nq * K * 4));
-  WV_CUDA(c, cudaMemcpyAsync(c->q_buf.p, queries, (size_t)nq * c->d * 4, cudaMemcpyHostToDevice, c->stream));
-  WV_CUDA(c, cudaMemcpyAsync(c->seed_buf.p, seeds, (size_t)nq * L * 4, cudaMemcpyHostToDevice, c->stream));
+  if (seeds)
+    WV_CUDA(c, cudaMemcpyAsync(c->seed_buf.p, seeds, (size_t)nq * L * 4, cudaMemcpyHostToDevice, c->stream));
   rc = run_search_device(c, c->q_buf.as<float>(), nq, c->seed_buf.as<uint32_t>(), L, nullptr, nullptr, L, K, L,
                   c->out_ids_buf.as<uint32_t>(), out_dist ? c->out_dist_buf.as<float>() : nullptr, K, counters);
   if (rc) return rc;
@@ -306,23 +346,29 @@ int wv_search_batch(wv_ctx *c, const float *queries, uint32_t nq, int entry, con
     Lmax = std::max(Lmax, L[q]);
   }
   WV_CUDA(c, cudaSetDevice(c->device));
-  // seeds drawn query by query with each query's own L, as the reference's
-  // loop would draw them
-  std::vector<uint32_t> hs((size_t)nq * Lmax);
-  for (uint32_t q = 0; q < nq; q++) {
-    int rc = draw(c, 1, entry, L[q], hs.data() + (size_t)q * Lmax, Lmax);
-    if (rc) return rc;
-  }
   WV_CUDA(c, c->q_buf.ensure((size_t)nq * c->d * 4));
-  WV_CUDA(c, c->seed_buf.ensure(hs.size() * 4));
+  WV_CUDA(c, c->seed_buf.ensure((size_t)nq * Lmax * 4));
   WV_CUDA(c, c->out_ids_buf.ensure((size_t)nq * out_stride * 4));
   WV_CUDA(c, c->lq_buf.ensure((size_t)nq * 4));
   WV_CUDA(c, c->kq_buf.ensure((size_t)nq * 4));
   if (out_dist) WV_CUDA(c, c->out_dist_buf.ensure((size_t)nq * out_stride * 4));
   WV_CUDA(c, cudaMemcpyAsync(c->q_buf.p, queries, (size_t)nq * c->d * 4, cudaMemcpyHostToDevice, c->stream));
-  WV_CUDA(c, cudaMemcpyAsync(c->seed_buf.p, hs.data(), hs.size() * 4, cudaMemcpyHostToDevice, c->stream));
   WV_CUDA(c, cudaMemcpyAsync(c->lq_buf.p, L, (size_t)nq * 4, cudaMemcpyHostToDevice, c->stream));
   WV_CUDA(c, cudaMemcpyAsync(c->kq_buf.p, K, (size_t)nq * 4, cudaMemcpyHostToDevice, c->stream));
+  // seeds drawn query by query with each query's own L, as the reference's
+  // loop would draw them (Rand: one rand() per query, the rest on the device)
+  std::vector<uint32_t> hs;
+  if (entry == WV_ENTRY_RAND) {
+    int rc = draw_seeds_rand_device(c, nq, c->lq_buf.as<uint32_t>(), 0, Lmax, c->seed_buf.as<uint32_t>(), Lmax);
+    if (rc) return rc;
+  } else {
+    hs.resize((size_t)nq * Lmax);
+    for (uint32_t q = 0; q < nq; q++) {
+      int rc = draw(c, 1, entry, L[q], hs.data() + (size_t)q * Lmax, Lmax);
+      if (rc) return rc;
+    }
+    WV_CUDA(c, cudaMemcpyAsync(c->seed_buf.p, hs.data(), hs.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  }
   int rc = run_search_device(c, c->q_buf.as<float>(), nq, c->seed_buf.as<uint32_t>(), Lmax, c->lq_buf.as<uint32_t>(),
                       c->kq_buf.as<uint32_t>(), 0, 0, Lmax, c->out_ids_buf.as<uint32_t>(),
                       out_dist ? c->out_dist_buf.as<float>() : nullptr, out_stride, counters);

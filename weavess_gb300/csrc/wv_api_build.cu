@@ -74,6 +74,7 @@ int wv_load_built_graph(wv_ctx *c) {
   if (dep)
     WV_CUDA(c, cudaMemcpy(c->ep_row.data(), c->fg_ids.as<uint32_t>() + (size_t)ep * w, dep * 4,
                           cudaMemcpyDeviceToHost));
+  c->generation++;
   c->gn = (uint32_t)n;
   c->gw = (uint32_t)w;
   c->ep = ep;

@@ -3,6 +3,7 @@
 
 #include "wv_ctx.h"
 #include "wv_learn.h"
+#include "wv_seeds.h"
 
 using namespace wv;
 
@@ -36,6 +37,7 @@ int wv_learn_fit(wv_ctx *c, const float *train_q, uint32_t nt, const wv_learn_pa
   WV_CHECK(c, lp.L_trace >= 10 && lp.L_trace < c->n && lp.L_max < c->n && lp.L_min >= 10, WV_ERR_ARG,
            "beam limits out of range");
   LearnReport r;
+  c->generation++;
   int rc = learn_fit(c, train_q, nt, lp, &r);
   if (rep) *rep = wv_learn_report{r.loss_ce, r.loss_mse, r.margin, r.val_agreement, r.ms, r.mean_label_L, r.steps,
                                   r.labelled};
@@ -59,17 +61,18 @@ int wv_search_learned(wv_ctx *c, const float *queries, uint32_t nq, uint32_t K, 
   // the plain seeds of the fallback (and of short entry lists), drawn as
   // SearchEntryRand draws them; skipped when the model can read none
   const uint32_t Lp = learn_plain_beam(c);
-  std::vector<uint32_t> hs((size_t)nq * Lp);
-  if (Lp) draw_seeds_rand(c->rnd, nq, Lp, c->n, hs.data(), Lp);
   cudaError_t e = cudaSuccess;
   float *dq = c->buf<float>("sl_q", (size_t)nq * c->d, &e);
-  uint32_t *ds = Lp ? c->buf<uint32_t>("sl_s", hs.size(), &e) : nullptr;
+  uint32_t *ds = Lp ? c->buf<uint32_t>("sl_s", (size_t)nq * Lp, &e) : nullptr;
   uint32_t *dout = c->buf<uint32_t>("sl_o", (size_t)nq * K, &e);
   float *dd = out_dist ? c->buf<float>("sl_d", (size_t)nq * K, &e) : nullptr;
   uint32_t *dL = c->buf<uint32_t>("sl_L", nq, &e);
   WV_CUDA(c, e);
   WV_CUDA(c, cudaMemcpyAsync(dq, queries, (size_t)nq * c->d * 4, cudaMemcpyHostToDevice, c->stream));
-  if (Lp) WV_CUDA(c, cudaMemcpyAsync(ds, hs.data(), hs.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  if (Lp) {
+    const int rc = draw_seeds_rand_device(c, nq, nullptr, Lp, Lp, ds, Lp);
+    if (rc) return rc;
+  }
   int rc = learn_search(c, dq, nq, K, dout, dd, counters, ds, dL);
   if (rc) return rc;
   WV_CUDA(c, cudaMemcpyAsync(out_ids, dout, (size_t)nq * K * 4, cudaMemcpyDeviceToHost, c->stream));
@@ -93,6 +96,7 @@ int wv_learn_assign(wv_ctx *c, const uint32_t *ids, uint32_t n, uint32_t *cluste
 int wv_learn_set_margin(wv_ctx *c, float margin) {
   if (!c || !(margin > 0.f)) return WV_ERR_ARG;
   WV_CHECK(c, c->learn, WV_ERR_STATE, "no trained model");
+  c->generation++;
   return learn_set_margin(c, margin);
 }
 
@@ -115,6 +119,7 @@ int wv_learn_grad(wv_ctx *c, const float *x, const uint32_t *yc, const float *yr
   WV_CHECK(c, c->d > 0, WV_ERR_STATE, "upload a base first (it sets the input width)");
   for (uint32_t i = 0; i < B; i++) WV_CHECK(c, yc[i] < clusters, WV_ERR_ARG, "label %u >= clusters", yc[i]);
   WV_CUDA(c, cudaSetDevice(c->device));
+  c->generation++;
   return learn_grad(c, x, yc, yr, B, clusters, params, lam, grad, loss);
 }
 

@@ -80,6 +80,10 @@ struct wv_ctx {
   // learned entry / beam model (wv_learn.cu), or null
   void *learn = nullptr;
 
+  // bumped whenever the base, the search graph, the candidate precision or
+  // the learned model change: captured plans hold their pointers and values
+  unsigned long long generation = 0;
+
   // named grow-only work buffers of the build kernels
   std::map<std::string, wv::DevBuf> work;
   template <class T>
@@ -125,6 +129,30 @@ inline int fail(wv_ctx *c, int code, const char *fmt, ...) {
 
 // reads the device status word after a launch; maps kernel-reported errors
 int check_device_status(wv_ctx *c, const char *what);
+
+}  // namespace wv
+
+#include "wv_search.h"
+
+namespace wv {
+
+// visited-set scratch for `shape` at beams up to Lmax (may allocate: call it
+// before a stream capture); *blocks = the persistent grid of that shape
+int search_prepare(wv_ctx *c, uint32_t Lmax, SearchShape shape, int *blocks);
+// the kernel arguments of a search on device-resident buffers (nq_dev: the
+// query count read on the device, or null)
+SearchArgs search_args(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t *nq_dev, const uint32_t *d_seeds,
+                       uint32_t seed_stride, const uint32_t *d_L, const uint32_t *d_K, uint32_t L, uint32_t K,
+                       uint32_t Lmax, uint32_t *d_out, float *d_dist, uint32_t out_stride);
+// clears the query counter and the counters, launches; nothing synchronizes
+// (capturable once search_prepare ran)
+int search_enqueue(wv_ctx *c, const SearchArgs &a, SearchShape shape, int blocks);
+
+// visited-set scratch owned by someone other than the context (a plan)
+struct SearchScratch {
+  uint32_t *visited = nullptr, *touched = nullptr;
+  uint32_t words = 0;
+};
 
 // the search kernel on device-resident queries / seeds / outputs (per-query
 // L and K optional); counters (nullable) are read back

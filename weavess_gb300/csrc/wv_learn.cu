@@ -25,6 +25,7 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <string>
 #include <vector>
 
 #include "wv_common.cuh"
@@ -32,6 +33,7 @@
 #include "wv_learn.h"
 #include "wv_mlp.cuh"
 #include "wv_search.h"
+#include "wv_seeds.h"
 
 namespace wv {
 namespace {
@@ -290,22 +292,29 @@ struct Work {  // activations and gradients of one batch
   float *H1, *H2, *O, *dO, *dH2, *dZ2, *dH1, *dZ1;
 };
 
-int alloc_work(wv_ctx *c, uint32_t B, uint32_t D, uint32_t C, Work &w) {
+// `pfx` names the buffers (a captured plan keeps its own); `grads`: the
+// backward-pass buffers too
+int alloc_work(wv_ctx *c, uint32_t B, uint32_t D, uint32_t C, Work &w, const std::string &pfx = "ml_",
+               bool grads = true) {
   cudaError_t e = cudaSuccess;
-  w.Xb = c->buf<__nv_bfloat16>("ml_Xb", (size_t)B * D, &e);
-  w.H1b = c->buf<__nv_bfloat16>("ml_H1b", (size_t)B * HID, &e);
-  w.H2b = c->buf<__nv_bfloat16>("ml_H2b", (size_t)B * HID, &e);
-  w.dOb = c->buf<__nv_bfloat16>("ml_dOb", (size_t)B * (C + 1), &e);
-  w.dZ2b = c->buf<__nv_bfloat16>("ml_dZ2b", (size_t)B * HID, &e);
-  w.dZ1b = c->buf<__nv_bfloat16>("ml_dZ1b", (size_t)B * HID, &e);
-  w.H1 = c->buf<float>("ml_H1", (size_t)B * HID, &e);
-  w.H2 = c->buf<float>("ml_H2", (size_t)B * HID, &e);
-  w.O = c->buf<float>("ml_O", (size_t)B * (C + 1), &e);
-  w.dO = c->buf<float>("ml_dO", (size_t)B * (C + 1), &e);
-  w.dH2 = c->buf<float>("ml_dH2", (size_t)B * HID, &e);
-  w.dZ2 = c->buf<float>("ml_dZ2", (size_t)B * HID, &e);
-  w.dH1 = c->buf<float>("ml_dH1", (size_t)B * HID, &e);
-  w.dZ1 = c->buf<float>("ml_dZ1", (size_t)B * HID, &e);
+  auto nm = [&](const char *s) { return (pfx + s); };
+  w = Work{};
+  w.Xb = c->buf<__nv_bfloat16>(nm("Xb").c_str(), (size_t)B * D, &e);
+  w.H1b = c->buf<__nv_bfloat16>(nm("H1b").c_str(), (size_t)B * HID, &e);
+  w.H2b = c->buf<__nv_bfloat16>(nm("H2b").c_str(), (size_t)B * HID, &e);
+  w.H1 = c->buf<float>(nm("H1").c_str(), (size_t)B * HID, &e);
+  w.H2 = c->buf<float>(nm("H2").c_str(), (size_t)B * HID, &e);
+  w.O = c->buf<float>(nm("O").c_str(), (size_t)B * (C + 1), &e);
+  if (grads) {
+    w.dOb = c->buf<__nv_bfloat16>(nm("dOb").c_str(), (size_t)B * (C + 1), &e);
+    w.dZ2b = c->buf<__nv_bfloat16>(nm("dZ2b").c_str(), (size_t)B * HID, &e);
+    w.dZ1b = c->buf<__nv_bfloat16>(nm("dZ1b").c_str(), (size_t)B * HID, &e);
+    w.dO = c->buf<float>(nm("dO").c_str(), (size_t)B * (C + 1), &e);
+    w.dH2 = c->buf<float>(nm("dH2").c_str(), (size_t)B * HID, &e);
+    w.dZ2 = c->buf<float>(nm("dZ2").c_str(), (size_t)B * HID, &e);
+    w.dH1 = c->buf<float>(nm("dH1").c_str(), (size_t)B * HID, &e);
+    w.dZ1 = c->buf<float>(nm("dZ1").c_str(), (size_t)B * HID, &e);
+  }
   WV_CUDA(c, e);
   return WV_OK;
 }
@@ -494,12 +503,9 @@ int learn_fit(wv_ctx *c, const float *train_q, uint32_t nt, const LearnParams &p
   uint32_t *pans = c->buf<uint32_t>("ml_pans", (size_t)nt * 10, &e);
   WV_CUDA(c, e);
   WV_CUDA(c, cudaMemcpyAsync(dq, train_q, (size_t)nt * d * 4, cudaMemcpyHostToDevice, c->stream));
-  {
-    std::vector<uint32_t> hs((size_t)nt * p.L_trace);
-    draw_seeds_rand(c->rnd, nt, p.L_trace, n, hs.data(), p.L_trace);
-    WV_CUDA(c, cudaMemcpyAsync(pseeds, hs.data(), hs.size() * 4, cudaMemcpyHostToDevice, c->stream));
-  }
-  int rc = search_dev(c, dq, nt, pseeds, p.L_trace, nullptr, p.L_trace, p.L_trace, 10, pans, nullptr);
+  int rc = draw_seeds_rand_device(c, nt, nullptr, p.L_trace, p.L_trace, pseeds, p.L_trace);
+  if (rc) return rc;
+  rc = search_dev(c, dq, nt, pseeds, p.L_trace, nullptr, p.L_trace, p.L_trace, 10, pans, nullptr);
   if (rc) return rc;
   std::vector<uint32_t> hans((size_t)nt * 10);
   WV_CUDA(c, cudaMemcpyAsync(hans.data(), pans, hans.size() * 4, cudaMemcpyDeviceToHost, c->stream));
@@ -682,6 +688,60 @@ int learn_search(wv_ctx *c, const float *dq, uint32_t nq, uint32_t K, uint32_t *
   // without the fallback no query's beam exceeds Lmax: size the kernel for it
   const uint32_t Lcap = (d_plain_seeds && S.fallback_p > 0.f) ? stride : S.Lmax;
   return run_search_device(c, dq, nq, seeds, stride, Lq, nullptr, 0, K, Lcap, dout, ddist, K, counters);
+}
+
+int learn_prepare(wv_ctx *c, const char *pfx, uint32_t nq_max, uint32_t *Lcap, uint32_t *stride) {
+  WV_CHECK(c, c->learn && state(c).ready, WV_ERR_STATE, "no trained model (call wv_learn_fit)");
+  LearnState &S = state(c);
+  WV_CHECK(c, S.D == c->d, WV_ERR_STATE, "model trained for d=%u", S.D);
+  cudaError_t e = cudaSuccess;
+  const std::string p(pfx);
+  *stride = std::max(S.Lmax, S.L_plain);
+  c->buf<uint32_t>((p + "seeds").c_str(), (size_t)nq_max * *stride, &e);
+  c->buf<uint32_t>((p + "Lq").c_str(), nq_max, &e);
+  c->buf<uint32_t>((p + "fb").c_str(), 4, &e);
+  WV_CUDA(c, e);
+  Work w;
+  int rc = alloc_work(c, nq_max, S.D, S.C, w, p, false);
+  if (rc) return rc;
+  *Lcap = S.fallback_p > 0.f ? *stride : S.Lmax;
+  return WV_OK;
+}
+
+int learn_enqueue(wv_ctx *c, const char *pfx, const float *dq, uint32_t nq_max, const uint32_t *d_nq, uint32_t K,
+                  const uint32_t *d_K, uint32_t *dout, float *ddist, uint32_t out_stride,
+                  const uint32_t *d_plain_seeds, SearchShape shape, int blocks, const SearchScratch &scr,
+                  cudaEvent_t ev0, cudaEvent_t ev1) {
+  LearnState &S = state(c);
+  cudaError_t e = cudaSuccess;
+  const std::string p(pfx);
+  const uint32_t stride = std::max(S.Lmax, S.L_plain);
+  uint32_t *seeds = c->buf<uint32_t>((p + "seeds").c_str(), (size_t)nq_max * stride, &e);
+  uint32_t *Lq = c->buf<uint32_t>((p + "Lq").c_str(), nq_max, &e);
+  uint32_t *fb = c->buf<uint32_t>((p + "fb").c_str(), 4, &e);
+  WV_CUDA(c, e);
+  Work w;
+  int rc = alloc_work(c, nq_max, S.D, S.C, w, p, false);
+  if (rc) return rc;
+  rc = forward(c, S, dq, nullptr, nq_max, w);
+  if (rc) return rc;
+  WV_CUDA(c, cudaMemsetAsync(fb, 0, 4, c->stream));
+  k_learn_seeds<<<nblk(nq_max, 128), 128, 0, c->stream>>>(
+      w.O, nq_max, S.C, S.lists.as<uint32_t>(), S.SL, S.llen.as<uint32_t>(), S.margin, S.Lmin, S.Lmax, S.fallback_p,
+      S.L_plain, d_plain_seeds, seeds, stride, Lq, K, fb);
+  WV_CUDA(c, cudaGetLastError());
+  const uint32_t Lcap = S.fallback_p > 0.f ? stride : S.Lmax;
+  SearchArgs a = search_args(c, dq, nq_max, d_nq, seeds, stride, Lq, d_K, 0, K, Lcap, dout, ddist, out_stride);
+  if (scr.visited) {
+    a.visited = scr.visited;
+    a.touched = scr.touched;
+    a.words = scr.words;
+  }
+  if (ev0) WV_CUDA(c, cudaEventRecord(ev0, c->stream));
+  rc = search_enqueue(c, a, shape, blocks);
+  if (rc) return rc;
+  if (ev1) WV_CUDA(c, cudaEventRecord(ev1, c->stream));
+  return WV_OK;
 }
 
 int learn_grad(wv_ctx *c, const float *x, const uint32_t *yc, const float *yr, uint32_t B, uint32_t C,

@@ -10,10 +10,7 @@ struct LearnParams {
   uint32_t clusters = 64;      // entry clusters (k-means on the base)
   uint32_t kmeans_iters = 8;
   uint32_t list_len = 512;     // seeds kept per cluster
-  uint32_t L_trace = 512;      int learn_set_margin(wv_ctx *c, float margin);
-int learn_predict(wv_ctx *c, const float *q, uint32_t nq, uint32_t *cluster, float *prob, float *log2L);
-int learn_assign(wv_ctx *c, const uint32_t *ids, uint32_t n, uint32_t *cluster);
-// beam of the plain search that labels the traces
+  uint32_t L_trace = 512;      // beam of the plain search that labels the traces
   uint32_t epochs = 6, batch = 1024;
   float lr = 1e-3f, lam = 0.5f;  // Adam step, weight of the beam regressor
   uint32_t L_min = 16, L_max = 512;
@@ -32,6 +29,17 @@ int learn_fit(wv_ctx *c, const float *train_q, uint32_t nt, const LearnParams &p
 // (fallback and fill), or null
 int learn_search(wv_ctx *c, const float *dq, uint32_t nq, uint32_t K, uint32_t *dout, float *ddist,
                  wv_counters *counters, const uint32_t *d_plain_seeds, uint32_t *d_Lq_out);
+// the same without synchronizing, for a captured plan: work buffers named
+// with `pfx` for nq_max queries (learn_prepare, before the capture; *Lcap the
+// beam the search kernel is sized for, *stride the seed row stride), then
+// the forward pass, the seed kernel and the search of the first *d_nq
+// queries (per-query K optional, capped by K) on the caller's visited
+// scratch; ev0 / ev1 (nullable) are recorded around the search kernel
+int learn_prepare(wv_ctx *c, const char *pfx, uint32_t nq_max, uint32_t *Lcap, uint32_t *stride);
+int learn_enqueue(wv_ctx *c, const char *pfx, const float *dq, uint32_t nq_max, const uint32_t *d_nq, uint32_t K,
+                  const uint32_t *d_K, uint32_t *dout, float *ddist, uint32_t out_stride,
+                  const uint32_t *d_plain_seeds, SearchShape shape, int blocks, const SearchScratch &scr,
+                  cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
 // loss and gradients of a batch for given parameters (gradient check)
 int learn_grad(wv_ctx *c, const float *x, const uint32_t *yc, const float *yr, uint32_t B, uint32_t C,
                const float *params, float lam, float *grad, float *loss);

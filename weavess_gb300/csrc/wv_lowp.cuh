@@ -3,10 +3,10 @@
 //
 // A warp computes the distances of up to 32 rows at once.  Each row is read
 // in 16-byte chunks (8-byte or 4-byte when the row length is not a multiple
-// of 16 bytes; d is a multiple of 4) by a group of G lanes, G the power of two that covers the
-// row's chunks (at most 32), so 32 / G rows are read per pass; U passes are
-// issued before any of them is reduced, which keeps up to U chunk loads per
-// lane in flight.  The order of the additions depends only on d and the
+// of 16 bytes; d is a multiple of 4) by a group of G lanes, G the power of
+// two (4 to 32) that covers the row's chunks, so 32 / G rows are read per
+// pass; the loads of U passes are issued together, branch-free, before any
+// of them is used, which keeps U chunk loads per lane in flight.  The order of the additions depends only on d and the
 // storage, never on how many rows share the call, so the search kernel and
 // the diagnostic (wv_candidate_distances) return the same values.
 #pragma once
@@ -29,28 +29,38 @@ namespace lowp_detail {
 
 constexpr int U = 8;  // passes in flight
 
-// squared distance contribution of one chunk of CB bytes at element offset e0
+// the CB bytes of one chunk as 32-bit words
+template <int CB>
+struct Chunk {
+  uint32_t w[CB / 4];
+};
+template <int CB>
+__device__ __forceinline__ Chunk<CB> load_chunk(const uint8_t *p) {
+  Chunk<CB> c;
+  if (CB == 16) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
+    c.w[0] = v.x, c.w[1] = v.y, c.w[2] = v.z, c.w[3] = v.w;
+  } else if (CB == 8) {
+    const uint2 v = __ldg(reinterpret_cast<const uint2 *>(p));
+    c.w[0] = v.x, c.w[1] = v.y;
+  } else {
+    c.w[0] = __ldg(reinterpret_cast<const uint32_t *>(p));
+  }
+  return c;
+}
+
+// squared distance contribution of one loaded chunk at element offset e0
 template <int ST, int CB>
-__device__ __forceinline__ float chunk_sq(const uint8_t *p, const float *qv, uint32_t e0, float sc) {
+__device__ __forceinline__ float chunk_sq(const Chunk<CB> &c, const float *qv, uint32_t e0, float sc) {
   float acc = 0.f;
+  const float4 *q4 = reinterpret_cast<const float4 *>(qv + e0);
   if (ST == 1) {
     constexpr int E = CB / 2;  // bf16 values per chunk
-    uint32_t w[CB / 4];
-    if (CB == 16) {
-      const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
-      w[0] = v.x, w[1] = v.y, w[2] = v.z, w[3] = v.w;
-    } else if (CB == 8) {
-      const uint2 v = __ldg(reinterpret_cast<const uint2 *>(p));
-      w[0] = v.x, w[1] = v.y;
-    } else {
-      w[0] = __ldg(reinterpret_cast<const uint32_t *>(p));
-    }
-    const float4 *q4 = reinterpret_cast<const float4 *>(qv + e0);
 #pragma unroll
     for (int j = 0; j < E / 4; j++) {
       const float4 q = q4[j];
-      const float2 x0 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&w[2 * j]));
-      const float2 x1 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&w[2 * j + 1]));
+      const float2 x0 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&c.w[2 * j]));
+      const float2 x1 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&c.w[2 * j + 1]));
       const float a0 = q.x - x0.x, a1 = q.y - x0.y, a2 = q.z - x1.x, a3 = q.w - x1.y;
       acc = fmaf(a0, a0, acc);
       acc = fmaf(a1, a1, acc);
@@ -59,22 +69,11 @@ __device__ __forceinline__ float chunk_sq(const uint8_t *p, const float *qv, uin
     }
   } else {
     constexpr int E = CB;  // fp8 values per chunk
-    uint32_t w[CB / 4];
-    if (CB == 16) {
-      const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
-      w[0] = v.x, w[1] = v.y, w[2] = v.z, w[3] = v.w;
-    } else if (CB == 8) {
-      const uint2 v = __ldg(reinterpret_cast<const uint2 *>(p));
-      w[0] = v.x, w[1] = v.y;
-    } else {
-      w[0] = __ldg(reinterpret_cast<const uint32_t *>(p));
-    }
-    const float4 *q4 = reinterpret_cast<const float4 *>(qv + e0);
 #pragma unroll
     for (int j = 0; j < E / 4; j++) {
       const float4 q = q4[j];
-      const __half2_raw h0 = __nv_cvt_fp8x2_to_halfraw2((__nv_fp8x2_storage_t)(w[j] & 0xffffu), __NV_E4M3);
-      const __half2_raw h1 = __nv_cvt_fp8x2_to_halfraw2((__nv_fp8x2_storage_t)(w[j] >> 16), __NV_E4M3);
+      const __half2_raw h0 = __nv_cvt_fp8x2_to_halfraw2((__nv_fp8x2_storage_t)(c.w[j] & 0xffffu), __NV_E4M3);
+      const __half2_raw h1 = __nv_cvt_fp8x2_to_halfraw2((__nv_fp8x2_storage_t)(c.w[j] >> 16), __NV_E4M3);
       const float2 x0 = __half22float2(*reinterpret_cast<const __half2 *>(&h0));
       const float2 x1 = __half22float2(*reinterpret_cast<const __half2 *>(&h1));
       const float a0 = q.x - sc * x0.x, a1 = q.y - sc * x0.y, a2 = q.z - sc * x1.x, a3 = q.w - sc * x1.y;
@@ -87,37 +86,42 @@ __device__ __forceinline__ float chunk_sq(const uint8_t *p, const float *qv, uin
   return acc;
 }
 
-template <int ST, int CB>
+template <int ST, int CB, int G>
 __device__ __forceinline__ float rows_dist(const LowpRows &b, uint32_t my, int cnt, const float *qv, int lane) {
   constexpr int EPC = ST == 1 ? CB / 2 : CB;  // elements per chunk
+  constexpr int RPP = 32 / G;                 // rows per pass
   const uint32_t rb = ST == 1 ? b.d * 2 : b.d;
   const uint32_t ch = rb / CB;
-  int G = 1;
-  while (G < 32 && (uint32_t)G < ch) G <<= 1;
-  const int RPP = 32 / G;  // rows per pass
   const int sub = lane & (G - 1), grp = lane / G;
   const uint8_t *base = reinterpret_cast<const uint8_t *>(b.rows);
   float out = 0.f;
   for (int p0 = 0; p0 * RPP < cnt; p0 += U) {
     float part[U], sc[U];
     const uint8_t *row[U];
+    bool live[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
       const int r = (p0 + u) * RPP + grp;
       const uint32_t id = __shfl_sync(FULL, my, r & 31);
+      live[u] = r < cnt;
       part[u] = 0.f;
-      row[u] = r < cnt ? base + (size_t)id * rb : nullptr;
-      sc[u] = (ST == 2 && r < cnt) ? __ldg(b.scale + id) : 1.f;
+      // dead rows read row 0 (in bounds) and are ignored: no branch keeps the
+      // U loads from issuing together
+      row[u] = base + (size_t)(live[u] ? id : 0u) * rb;
+      sc[u] = ST == 2 ? __ldg(b.scale + (live[u] ? id : 0u)) : 1.f;
     }
-    // chunk-major: the U rows' loads of one chunk step are independent
+    // chunk-major: all U rows' loads of one step are issued before any math
     for (uint32_t k = sub; k < ch; k += G) {
+      Chunk<CB> c[U];
 #pragma unroll
-      for (int u = 0; u < U; u++)
-        if (row[u]) part[u] += chunk_sq<ST, CB>(row[u] + (size_t)k * CB, qv, k * EPC, sc[u]);
+      for (int u = 0; u < U; u++) c[u] = load_chunk<CB>(row[u] + (size_t)k * CB);
+#pragma unroll
+      for (int u = 0; u < U; u++) part[u] += chunk_sq<ST, CB>(c[u], qv, k * EPC, sc[u]);
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      float v = part[u];
+      float v = live[u] ? part[u] : 0.f;
+#pragma unroll
       for (int o = G >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
       // row `lane` sits in pass lane / RPP, group lane % RPP
       const float t = __shfl_sync(FULL, v, (lane % RPP) * G);
@@ -125,6 +129,15 @@ __device__ __forceinline__ float rows_dist(const LowpRows &b, uint32_t my, int c
     }
   }
   return out;
+}
+
+template <int ST, int CB>
+__device__ __forceinline__ float rows_dist_g(const LowpRows &b, uint32_t my, int cnt, const float *qv, int lane) {
+  const uint32_t ch = (ST == 1 ? b.d * 2 : b.d) / CB;
+  if (ch <= 4) return rows_dist<ST, CB, 4>(b, my, cnt, qv, lane);
+  if (ch <= 8) return rows_dist<ST, CB, 8>(b, my, cnt, qv, lane);
+  if (ch <= 16) return rows_dist<ST, CB, 16>(b, my, cnt, qv, lane);
+  return rows_dist<ST, CB, 32>(b, my, cnt, qv, lane);
 }
 
 }  // namespace lowp_detail
@@ -135,12 +148,12 @@ __device__ __forceinline__ float rows_dist(const LowpRows &b, uint32_t my, int c
 __device__ __forceinline__ float lowp_rows_dist(const LowpRows &b, uint32_t my, int cnt, const float *qv, int lane) {
   const uint32_t rb = b.storage == 1 ? b.d * 2 : b.d;
   if (b.storage == 1) {
-    if (rb % 16 == 0) return lowp_detail::rows_dist<1, 16>(b, my, cnt, qv, lane);
-    return lowp_detail::rows_dist<1, 8>(b, my, cnt, qv, lane);  // d % 4 == 0: rows are 8-byte multiples
+    if (rb % 16 == 0) return lowp_detail::rows_dist_g<1, 16>(b, my, cnt, qv, lane);
+    return lowp_detail::rows_dist_g<1, 8>(b, my, cnt, qv, lane);  // d % 4 == 0: rows are 8-byte multiples
   }
-  if (rb % 16 == 0) return lowp_detail::rows_dist<2, 16>(b, my, cnt, qv, lane);
-  if (rb % 8 == 0) return lowp_detail::rows_dist<2, 8>(b, my, cnt, qv, lane);
-  return lowp_detail::rows_dist<2, 4>(b, my, cnt, qv, lane);
+  if (rb % 16 == 0) return lowp_detail::rows_dist_g<2, 16>(b, my, cnt, qv, lane);
+  if (rb % 8 == 0) return lowp_detail::rows_dist_g<2, 8>(b, my, cnt, qv, lane);
+  return lowp_detail::rows_dist_g<2, 4>(b, my, cnt, qv, lane);
 }
 
 }  // namespace wv

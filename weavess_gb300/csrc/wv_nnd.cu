@@ -36,6 +36,7 @@
 #include <vector>
 
 #include "wv_common.cuh"
+#include "wv_mt.cuh"
 #include "wv_nnd.h"
 #include "wv_scan.h"
 
@@ -51,26 +52,13 @@ struct EntLess {
 };
 
 // ---------------------------------------------------------------- mt19937
-// std::mt19937 (Matsumoto & Nishimura): seeding recurrence, the in-place twist
-// run as four dependency-ordered phases, and tempering.
-__device__ __forceinline__ uint32_t mt_temper(uint32_t y) {
-  y ^= y >> 11;
-  y ^= (y << 7) & 0x9d2c5680u;
-  y ^= (y << 15) & 0xefc60000u;
-  y ^= y >> 18;
-  return y;
-}
-__device__ __forceinline__ uint32_t mt_mix(uint32_t cur, uint32_t next, uint32_t far) {
-  uint32_t y = (cur & 0x80000000u) | (next & 0x7fffffffu);
-  return far ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
-}
-
+// std::mt19937 stream of one seed (wv_mt.cuh), twisted by a block.
 __global__ void __launch_bounds__(256) k_mt19937(uint32_t seed, uint32_t *out, size_t count) {
   __shared__ uint32_t mt[624];
   const int t = threadIdx.x;
   if (t == 0) {
     mt[0] = seed;
-    for (int i = 1; i < 624; i++) mt[i] = 1812433253u * (mt[i - 1] ^ (mt[i - 1] >> 30)) + (uint32_t)i;
+    for (int i = 1; i < 624; i++) mt[i] = mt_seed_next(mt[i - 1], (uint32_t)i);
   }
   __syncthreads();
   for (size_t base = 0; base < count; base += 624) {

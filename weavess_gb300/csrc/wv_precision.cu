@@ -83,6 +83,7 @@ int wv_set_search_precision(wv_ctx *c, int storage, uint32_t rerank) {
   }
   WV_CUDA(c, cudaGetLastError());
   WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->generation++;
   c->storage = storage;
   c->rerank = rerank;
   return WV_OK;

@@ -36,6 +36,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp8.h>
 
+#include <algorithm>
 #include <cstdio>
 
 #include "warp_sort.cuh"
@@ -47,7 +48,7 @@ namespace wv {
 
 namespace {
 
-constexpr int WARPS = 4;  // warps per block
+constexpr int WARPS = 4;  // warps per block of the default shape
 constexpr uint32_t EMPTY = 0xffffffffu;
 // a visited-hash entry of an unexpanded seed: route mode does not mark seeds
 // visited, so the first time a seed comes back as a neighbour it is still
@@ -66,6 +67,11 @@ __host__ __device__ inline uint32_t pool_cap(uint32_t Lmax) { return (Lmax + 3) 
 // (the bitonic keys 2 * pow2(L) <= pow2(2L + 256), the introsort's
 // 2L + 256 words, the rerank's 2L words)
 __host__ __device__ inline uint32_t hash_cap(uint32_t Lmax) { return pow2_at_least(max(2048u, 2 * Lmax + 256)); }
+// the slots a launch uses: the default, or a larger power of two asked for
+__host__ __device__ inline uint32_t hash_slots(uint32_t Lmax, uint32_t want) {
+  const uint32_t h = hash_cap(Lmax);
+  return want > h ? pow2_at_least(want) : h;
+}
 
 struct WarpSmem {
   uint32_t *hash;  // hcap words: visited set; scratch of the seed sort and the rerank
@@ -78,20 +84,20 @@ struct WarpSmem {
   uint32_t *si;    //   (before that: the expansion's fresh ids)
 };
 
-__host__ __device__ inline size_t warp_smem_bytes(uint32_t d, uint32_t Lmax, uint32_t cap) {
+__host__ __device__ inline size_t warp_smem_bytes(uint32_t d, uint32_t Lmax, uint32_t cap, uint32_t hcap) {
   size_t b = 0;
-  b += align16((size_t)hash_cap(Lmax) * 4);
+  b += align16((size_t)hash_slots(Lmax, hcap) * 4);
   b += align16(((d + 3) & ~3u) * 4);
   b += 2 * align16((size_t)pool_cap(Lmax) * 4);
   b += 4 * align16(cap * 4);
   return b;
 }
 
-__device__ inline WarpSmem carve(uint8_t *p, uint32_t d, uint32_t Lmax, uint32_t cap) {
+__device__ inline WarpSmem carve(uint8_t *p, uint32_t d, uint32_t Lmax, uint32_t cap, uint32_t hcap) {
   WarpSmem s;
   const uint32_t pc = pool_cap(Lmax);
   s.hash = (uint32_t *)p;
-  p += align16((size_t)hash_cap(Lmax) * 4);
+  p += align16((size_t)hash_slots(Lmax, hcap) * 4);
   s.qv = (float *)p;
   p += align16(((d + 3) & ~3u) * 4);
   s.pd = (float *)p;
@@ -307,21 +313,43 @@ __device__ __forceinline__ float batch_dist(const float *__restrict__ base, uint
         const int c = c0 + g;
         const uint32_t id = __shfl_sync(FULL, my, c & 31);
         part[g] = 0.f;
-        row[g] = c < cnt ? reinterpret_cast<const float4 *>(base + (size_t)id * d) : nullptr;
+        // rows past cnt read row 0 (in bounds) and are ignored: no branch
+        // keeps the G loads from issuing together
+        row[g] = reinterpret_cast<const float4 *>(base + (size_t)(c < cnt ? id : 0u) * d);
       }
-      // chunk-major: the G rows' loads of one step are independent
+      // chunk-major: all G rows' loads of one step are issued before any math
       for (uint32_t k = lane; k < d4; k += 32) {
         const float4 qk = q4[k];
+        float4 x[G];
 #pragma unroll
-        for (int g = 0; g < G; g++)
-          if (row[g]) part[g] += group4(__ldg(row[g] + k), qk);
-      }
+        for (int g = 0; g < G; g++) x[g] = __ldg(row[g] + k);
 #pragma unroll
-      for (int g = 0; g < G; g++) {
-        float v = part[g];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
-        if (lane == c0 + g) out = v;
+        for (int g = 0; g < G; g++) part[g] += group4(x[g], qk);
       }
+      // transpose-reduce the 8 rows over the warp (10 shuffles, not 40):
+      // lanes exchange halves at distances 16, 8, 4 so that each lane keeps
+      // one row, then finish over distances 2, 1.  Lane l ends with row
+      // 4*bit4(l) + 2*bit3(l) + bit2(l).  (Integer sums: any order is exact.)
+      const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
+      float w[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const float send = b16 ? part[j] : part[j + 4];
+        w[j] = (b16 ? part[j + 4] : part[j]) + __shfl_xor_sync(FULL, send, 16);
+      }
+      float x2[2];
+#pragma unroll
+      for (int j = 0; j < 2; j++) {
+        const float send = b8 ? w[j] : w[j + 2];
+        x2[j] = (b8 ? w[j + 2] : w[j]) + __shfl_xor_sync(FULL, send, 8);
+      }
+      float y = (b4 ? x2[1] : x2[0]) + __shfl_xor_sync(FULL, b4 ? x2[0] : x2[1], 4);
+      y += __shfl_xor_sync(FULL, y, 2);
+      y += __shfl_xor_sync(FULL, y, 1);
+      // lane c0 + g takes row g from a lane that holds it
+      const int g = (lane - c0) & 7;
+      const float t = __shfl_sync(FULL, y, ((g >> 2) << 4) | (((g >> 1) & 1) << 3) | ((g & 1) << 2));
+      if (lane >= c0 && lane < c0 + G) out = t;
     }
   } else if (lane < cnt) {
     const float4 *row = reinterpret_cast<const float4 *>(base + (size_t)my * d);
@@ -344,17 +372,19 @@ __device__ __forceinline__ float cand_dist(const SearchArgs &a, bool ints, uint3
 //   marked visited, and every visited (id, dist) -- the seeds in drawn order,
 //   then each newly visited id in visit order -- is appended to the query's
 //   visit list (vis, vcap apart, vlimit entries kept, count in vcnt).
-template <bool BUILD>
-__global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
+template <bool BUILD, int W>
+__global__ void __maxnreg__(96) k_search(SearchArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const size_t wbytes = warp_smem_bytes(a.d, a.Lmax, a.cap);
-  WarpSmem s = carve(smem + warp * wbytes, a.d, a.Lmax, a.cap);
-  const uint32_t slot = blockIdx.x * WARPS + warp;
+  const size_t wbytes = warp_smem_bytes(a.d, a.Lmax, a.cap, a.hcap);
+  WarpSmem s = carve(smem + warp * wbytes, a.d, a.Lmax, a.cap, a.hcap);
+  const uint32_t slot = blockIdx.x * W + warp;
+  const uint32_t hs = hash_slots(a.Lmax, a.hcap);
+  const uint32_t nq = a.nq_dev ? *a.nq_dev : a.nq;
   Visited vis;
   vis.hash = s.hash;
-  vis.mask = hash_cap(a.Lmax) - 1;
-  vis.limit = hash_cap(a.Lmax) / 2;
+  vis.mask = hs - 1;
+  vis.limit = hs / 2;
   vis.bits = a.visited + (size_t)slot * a.words;
   vis.touched = a.touched + (size_t)slot * a.words;
   vis.ntouch = 0;
@@ -369,9 +399,14 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
     uint32_t q = 0;
     if (lane == 0) q = atomicAdd(a.next_query, 1u);
     q = __shfl_sync(FULL, q, 0);
-    if (q >= a.nq) break;
+    if (q >= nq) break;
     const int L = (int)(a.Lq ? a.Lq[q] : a.L);
     const int K = (int)(a.Kq ? a.Kq[q] : a.K);
+    // per-query sizes may come from device memory the host never checked
+    if (L < 1 || L > (int)a.Lmax || K < 1 || K > L || (uint32_t)L >= a.n || (a.out_ids && (uint32_t)K > a.out_stride)) {
+      if (lane == 0) set_err(a.status, DEV_OVERFLOW);
+      continue;
+    }
     const float *qsrc = a.queries + (size_t)q * a.d;
     bool qint = true;
     for (uint32_t i = lane; i < a.d; i += 32) {
@@ -440,6 +475,17 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
         deg = a.gw;
       }
       const float thr = pd[L - 1];
+      // the row most likely expanded next (the next unexpanded pool entry,
+      // unless this expansion inserts a closer one) is fetched toward L2
+      // while this one is processed
+      {
+        const int g = first_flag(pi, k + 1, L, lane);
+        if (g < L && lane == 0) {
+          const uint32_t nx = pi[g] & ID_MASK;
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(a.gids + (size_t)nx * a.gw));
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(a.gdeg + nx));
+        }
+      }
       // 1) the fresh neighbours, in adjacency order (a seed marked SEEDBIT)
       uint32_t nfresh = 0;
       for (uint32_t m0 = 0; m0 < deg; m0 += 32) {
@@ -592,35 +638,75 @@ __global__ void __launch_bounds__(WARPS * 32) k_search(SearchArgs a) {
   }
 }
 
-template <bool B>
-void set_attr(size_t smem) {
-  cudaFuncSetAttribute(k_search<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <bool B, int W>
+cudaError_t launch_w(const SearchArgs &a, int blocks, size_t smem, cudaStream_t stream) {
+  k_search<B, W><<<blocks, W * 32, smem, stream>>>(a);
+  return cudaGetLastError();
 }
+
+template <bool B, int W>
+int max_blocks_w(size_t smem) {
+  if (cudaFuncSetAttribute(k_search<B, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return -1;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<B, W>, W * 32, smem) != cudaSuccess) return -1;
+  return per_sm;
+}
+
+bool shape_ok(const SearchShape &sh) { return sh.wpb == 1 || sh.wpb == 2 || sh.wpb == 4 || sh.wpb == 8; }
 
 }  // namespace
 
-size_t search_block_smem(uint32_t d, uint32_t Lmax, uint32_t cap) { return WARPS * warp_smem_bytes(d, Lmax, cap); }
+size_t search_block_smem(uint32_t d, uint32_t Lmax, uint32_t cap, SearchShape sh) {
+  return (size_t)sh.wpb * warp_smem_bytes(d, Lmax, cap, sh.hcap);
+}
+size_t search_block_smem(uint32_t d, uint32_t Lmax, uint32_t cap) {
+  return search_block_smem(d, Lmax, cap, SearchShape{});
+}
 
 int search_warps_per_block() { return WARPS; }
 
-int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device) {
-  const size_t smem = search_block_smem(d, Lmax, cap);
+uint32_t search_hash_slots(uint32_t Lmax, uint32_t want) { return hash_slots(Lmax, want); }
+
+int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device, SearchShape sh) {
+  if (!shape_ok(sh)) return 0;
+  const size_t smem = search_block_smem(d, Lmax, cap, sh);
   if (smem > 227 * 1024) return 0;
-  set_attr<false>(smem);
-  set_attr<true>(smem);
-  if (cudaGetLastError() != cudaSuccess) return 0;
-  int per_sm = 0, sms = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search<true>, WARPS * 32, smem) != cudaSuccess)
+  int per_sm = -1;
+  // (the build variant exists in the default shape only)
+  switch (sh.wpb) {
+    case 1: per_sm = max_blocks_w<false, 1>(smem); break;
+    case 2: per_sm = max_blocks_w<false, 2>(smem); break;
+    case 4: per_sm = std::min(max_blocks_w<false, 4>(smem), max_blocks_w<true, 4>(smem)); break;
+    default: per_sm = max_blocks_w<false, 8>(smem); break;
+  }
+  if (per_sm <= 0) {
+    cudaGetLastError();
     return 0;
+  }
+  int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
   return per_sm * sms;
 }
+int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device) {
+  return search_grid(d, Lmax, cap, device, SearchShape{});
+}
 
+cudaError_t launch_search(const SearchArgs &a, SearchShape sh, int blocks, cudaStream_t stream) {
+  if (!shape_ok(sh)) return cudaErrorInvalidValue;
+  SearchArgs b = a;
+  b.hcap = sh.hcap;
+  const size_t smem = search_block_smem(a.d, a.Lmax, a.cap, sh);
+  if (a.vis) return sh.wpb == WARPS ? launch_w<true, WARPS>(b, blocks, smem, stream) : cudaErrorInvalidValue;
+  switch (sh.wpb) {
+    case 1: return launch_w<false, 1>(b, blocks, smem, stream);
+    case 2: return launch_w<false, 2>(b, blocks, smem, stream);
+    case 4: return launch_w<false, 4>(b, blocks, smem, stream);
+    default: return launch_w<false, 8>(b, blocks, smem, stream);
+  }
+}
 cudaError_t launch_search_exact(const SearchArgs &a, int blocks, cudaStream_t stream) {
-  const size_t smem = search_block_smem(a.d, a.Lmax, a.cap);
-  if (a.vis) k_search<true><<<blocks, WARPS * 32, smem, stream>>>(a);
-  else k_search<false><<<blocks, WARPS * 32, smem, stream>>>(a);
-  return cudaGetLastError();
+  return launch_search(a, SearchShape{}, blocks, stream);
 }
 
 }  // namespace wv

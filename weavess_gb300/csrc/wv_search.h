@@ -16,6 +16,7 @@ struct SearchArgs {
   uint32_t gw;
   const float *queries;  // nq x d
   uint32_t nq;
+  const uint32_t *nq_dev;  // if set, the query count is read from here (captured launches)
   const uint32_t *seeds;  // nq x seed_stride
   uint32_t seed_stride;
   const uint32_t *Lq;  // per-query beam width (or null: L)
@@ -28,7 +29,8 @@ struct SearchArgs {
   uint32_t *visited;             // slots x words bitsets, all zero between queries
   uint32_t *touched;             // slots x words
   uint32_t words;
-  uint32_t cap;  // candidate buffer entries per warp (graph width + 32)
+  uint32_t cap;   // candidate buffer entries per warp (graph width + 32)
+  uint32_t hcap;  // visited-hash slots per warp (0: the default for Lmax); set by launch_search
   unsigned *next_query;
   int *status;
   // candidate-search (build) mode: visit lists, vcap entries per query
@@ -52,11 +54,25 @@ struct SearchArgs {
 constexpr uint32_t SEARCH_MAX_WIDTH = 256;  // graph row width the kernel accepts
 constexpr uint32_t SEARCH_MAX_L = 1536;  // exact seed sort scratch: 2L + 256 words of stage
 
+// the tunable launch shape of the route kernel: warps per block (1, 2, 4 or
+// 8; one warp serves one query at a time) and visited-hash slots per warp (0:
+// the default, 2L + 256 rounded up to a power of two, at least 2048; more
+// slots keep longer searches off the global bitset but cost occupancy).
+// The build (candidate-search) variant runs in the default shape only.
+struct SearchShape {
+  int wpb = 4;
+  uint32_t hcap = 0;
+};
+
 // bytes of dynamic shared memory per block and warps per block
+size_t search_block_smem(uint32_t d, uint32_t Lmax, uint32_t cap, SearchShape sh);
 size_t search_block_smem(uint32_t d, uint32_t Lmax, uint32_t cap);
 int search_warps_per_block();
+uint32_t search_hash_slots(uint32_t Lmax, uint32_t want);
 // blocks to launch for one persistent wave on this device (0 if it cannot run)
+int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device, SearchShape sh);
 int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device);
+cudaError_t launch_search(const SearchArgs &a, SearchShape sh, int blocks, cudaStream_t stream);
 cudaError_t launch_search_exact(const SearchArgs &a, int blocks, cudaStream_t stream);
 
 }  // namespace wv

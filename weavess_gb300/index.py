@@ -217,6 +217,16 @@ class Context:
         self._check(self.L.wv_draw_seeds(self.h, nq, ENTRY[entry], L, out))
         return out
 
+    def plan(self, nq_max: int, K_max: int, d_queries: int, d_out_ids: int, L_max: int = 0, mode: str = "rand",
+             d_L: int = 0, d_K: int = 0, d_seeds: int = 0, d_out_dist: int = 0, out_stride: int = 0):
+        """A captured batch search on device buffers (pointers); see Plan."""
+        return Plan(self, nq_max, K_max, d_queries, d_out_ids, L_max, mode, d_L, d_K, d_seeds, d_out_dist,
+                    out_stride)
+
+    def draw_seeds_device(self, nq: int, L: int, d_seeds_ptr: int, stride: int = 0):
+        """SEARCH_ENTRY_RAND seeds into device memory (asynchronous)."""
+        self._check(self.L.wv_draw_seeds_device(self.h, nq, L, C.c_void_p(d_seeds_ptr), stride or L))
+
     def search_device(self, d_queries_ptr: int, nq: int, L: int, K: int, d_seeds_ptr: int, d_out_ptr: int,
                       d_dist_ptr: int = 0, counters: bool = False):
         cnt = _lib.Counters() if counters else None
@@ -224,3 +234,60 @@ class Context:
                                             C.c_void_p(d_out_ptr), C.c_void_p(d_dist_ptr or None),
                                             C.byref(cnt) if counters else None))
         return (int(cnt.dist_count), int(cnt.hop_count)) if counters else None
+
+
+PLAN_MODE = {"rand": 0, "seeds": 1, "learned": 2}
+
+
+class Plan:
+    """wv_plan_*: one batch layout (queries, per-query L and K, results) on
+    caller-owned device buffers, captured as a CUDA graph; `run(nq)` replays it
+    for the first nq queries, `wait()` returns (dist_count, hop_count), `tune(nq)`
+    picks the launch shape by timing the current inputs."""
+
+    def __init__(self, ctx, nq_max, K_max, d_queries, d_out_ids, L_max=0, mode="rand", d_L=0, d_K=0, d_seeds=0,
+                 d_out_dist=0, out_stride=0):
+        self.ctx, self.L = ctx, ctx.L
+        p = _lib.PlanParams(nq_max, L_max, K_max, out_stride or K_max, PLAN_MODE[mode])
+        h = C.c_void_p()
+        vp = lambda x: C.c_void_p(x or None)
+        ctx._check(self.L.wv_plan_create(ctx.h, C.byref(p), vp(d_queries), vp(d_L), vp(d_K), vp(d_seeds),
+                                         vp(d_out_ids), vp(d_out_dist), C.byref(h)))
+        self.h = h
+
+    def run(self, nq: int):
+        self.ctx._check(self.L.wv_plan_run(self.h, nq))
+
+    def wait(self):
+        cnt = _lib.Counters()
+        self.ctx._check(self.L.wv_plan_wait(self.h, C.byref(cnt)))
+        return int(cnt.dist_count), int(cnt.hop_count)
+
+    def tune(self, nq: int):
+        r = _lib.TuneReport()
+        self.ctx._check(self.L.wv_plan_tune(self.h, nq, C.byref(r)))
+        tried = [{"warps_per_block": t.warps_per_block, "hash_slots": t.hash_slots, "blocks": t.blocks,
+                  "ms": round(t.ms, 4)} for t in r.tried[:r.n]]
+        return {"tried": tried, "chosen": tried[r.chosen] if r.chosen >= 0 else None}
+
+    def search_ms(self) -> float:
+        """Device time of the search kernel in the last replay (waits for it)."""
+        v = C.c_float()
+        self.ctx._check(self.L.wv_plan_search_ms(self.h, C.byref(v)))
+        return float(v.value)
+
+    def shape(self):
+        sh = _lib.PlanShape()
+        self.ctx._check(self.L.wv_plan_shape_of(self.h, C.byref(sh)))
+        return {"warps_per_block": sh.warps_per_block, "hash_slots": sh.hash_slots, "blocks": sh.blocks}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.wv_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
