@@ -240,11 +240,12 @@ typedef struct {
 } wv_plan_params;
 typedef struct {
   int warps_per_block;
-  uint32_t hash_slots; /* visited-hash slots per warp */
+  uint32_t hash_words; /* visited-hash area per warp (32-bit words) */
+  int wide_hash;       /* 1: 32-bit entries; 0: 16-bit entries where n allows (twice the slots) */
   int blocks;
   float ms; /* measured search time (tuning) */
 } wv_plan_shape;
-#define WV_TUNE_MAX 16
+#define WV_TUNE_MAX 32
 typedef struct {
   int n, chosen;
   wv_plan_shape tried[WV_TUNE_MAX];
@@ -263,6 +264,10 @@ int wv_plan_wait(wv_plan *plan, wv_counters *counters);
  * draws.  The report lists every shape tried. */
 int wv_plan_tune(wv_plan *plan, uint32_t nq, wv_tune_report *report);
 int wv_plan_shape_of(wv_plan *plan, wv_plan_shape *shape);
+/* Pins a launch shape (warps_per_block 1/2/4/8, hash_words 0 for the default
+ * or a power of two, wide_hash) and recaptures, e.g. one found by an earlier
+ * wv_plan_tune; blocks and ms are ignored. */
+int wv_plan_set_shape(wv_plan *plan, const wv_plan_shape *shape);
 /* Device time of the search kernel in the last replay (CUDA events captured
  * around it in the graph); waits for the replay. */
 int wv_plan_search_ms(wv_plan *plan, float *ms);

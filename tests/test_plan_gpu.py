@@ -86,9 +86,30 @@ def test_plan_tune_keeps_results(setup):
     assert len(rep["tried"]) >= 4 and rep["chosen"] is not None
     assert {s["warps_per_block"] for s in rep["tried"]} >= {1, 2, 4, 8}
     assert plan.shape()["warps_per_block"] == rep["chosen"]["warps_per_block"]
+    assert plan.shape()["hash_words"] == rep["chosen"]["hash_words"]
     ctx.srand(12)
     ref, dc, hc = ctx.search_batch(query, L, K)
     ctx.srand(12)
+    plan.run(nq)
+    assert plan.wait() == (dc, hc)
+    check_rows(t["out"].cpu().numpy().view(np.uint32), ref, K, nq)
+    plan.close()
+
+
+@pytest.mark.parametrize("shape", [dict(warps_per_block=1, wide_hash=True), dict(warps_per_block=8, wide_hash=False),
+                                   dict(warps_per_block=2, hash_words=4096, wide_hash=True)])
+def test_plan_shapes_agree(setup, shape):
+    """Pinned launch shapes, 16-bit and 32-bit visited-hash entries included,
+    give the per-call results and counters."""
+    ctx, base, query, L, K, t = setup
+    nq = query.shape[0]
+    plan = rand_plan(ctx, t, nq)
+    plan.set_shape(**shape)
+    got = plan.shape()
+    assert got["warps_per_block"] == shape["warps_per_block"] and got["wide_hash"] == int(shape["wide_hash"])
+    ctx.srand(17)
+    ref, dc, hc = ctx.search_batch(query, L, K)
+    ctx.srand(17)
     plan.run(nq)
     assert plan.wait() == (dc, hc)
     check_rows(t["out"].cpu().numpy().view(np.uint32), ref, K, nq)

@@ -43,11 +43,12 @@ class PlanParams(C.Structure):
 
 
 class PlanShape(C.Structure):
-    _fields_ = [("warps_per_block", C.c_int), ("hash_slots", C.c_uint32), ("blocks", C.c_int), ("ms", C.c_float)]
+    _fields_ = [("warps_per_block", C.c_int), ("hash_words", C.c_uint32), ("wide_hash", C.c_int), ("blocks", C.c_int),
+                ("ms", C.c_float)]
 
 
 class TuneReport(C.Structure):
-    _fields_ = [("n", C.c_int), ("chosen", C.c_int), ("tried", PlanShape * 16)]
+    _fields_ = [("n", C.c_int), ("chosen", C.c_int), ("tried", PlanShape * 32)]
 
 
 class LearnReport(C.Structure):
@@ -133,6 +134,7 @@ def load(build_if_needed: bool = True):
     L.wv_plan_tune.argtypes = [vp, C.c_uint32, C.POINTER(TuneReport)]
     L.wv_plan_shape_of.argtypes = [vp, C.POINTER(PlanShape)]
     L.wv_plan_search_ms.argtypes = [vp, C.POINTER(C.c_float)]
+    L.wv_plan_set_shape.argtypes = [vp, C.POINTER(PlanShape)]
     L.wv_plan_destroy.argtypes = [vp]
     _lib = L
     return L

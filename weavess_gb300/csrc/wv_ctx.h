@@ -148,6 +148,16 @@ SearchArgs search_args(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t 
 // (capturable once search_prepare ran)
 int search_enqueue(wv_ctx *c, const SearchArgs &a, SearchShape shape, int blocks);
 
+// records `ev` on `s`; inside a stream capture as an event node of the graph
+// (so that replays time it), outside as a plain record
+inline cudaError_t record_event(cudaEvent_t ev, cudaStream_t s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &st);
+  if (e != cudaSuccess) return e;
+  return st == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal)
+                                             : cudaEventRecord(ev, s);
+}
+
 // visited-set scratch owned by someone other than the context (a plan)
 struct SearchScratch {
   uint32_t *visited = nullptr, *touched = nullptr;

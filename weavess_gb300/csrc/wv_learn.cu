@@ -737,10 +737,10 @@ int learn_enqueue(wv_ctx *c, const char *pfx, const float *dq, uint32_t nq_max, 
     a.touched = scr.touched;
     a.words = scr.words;
   }
-  if (ev0) WV_CUDA(c, cudaEventRecord(ev0, c->stream));
+  if (ev0) WV_CUDA(c, record_event(ev0, c->stream));
   rc = search_enqueue(c, a, shape, blocks);
   if (rc) return rc;
-  if (ev1) WV_CUDA(c, cudaEventRecord(ev1, c->stream));
+  if (ev1) WV_CUDA(c, record_event(ev1, c->stream));
   return WV_OK;
 }
 

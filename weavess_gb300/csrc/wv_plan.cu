@@ -128,10 +128,10 @@ int enqueue(wv_plan *p) {
   int rc = WV_OK;
   const SearchArgs a = plan_args(p, nqm, nq_dev, &rc);
   if (rc) return rc;
-  WV_CUDA(c, cudaEventRecord(p->s0, c->stream));
+  WV_CUDA(c, record_event(p->s0, c->stream));
   rc = search_enqueue(c, a, p->shape, p->blocks);
   if (rc) return rc;
-  WV_CUDA(c, cudaEventRecord(p->s1, c->stream));
+  WV_CUDA(c, record_event(p->s1, c->stream));
   return WV_OK;
 }
 
@@ -331,10 +331,16 @@ int wv_plan_tune(wv_plan *p, uint32_t nq, wv_tune_report *rep) {
   if (rc) return rc;
   rc = wv_plan_wait(p, nullptr);
   if (rc) return rc;
-  const uint32_t h0 = search_hash_slots(p->Lcap, 0);
+  // areas: the least the beam allows, the default, twice the default
+  const uint32_t h0 = search_hash_slots(p->Lcap, 0), hmin = search_hash_min(p->Lcap, c->n);
+  std::vector<uint32_t> areas;
+  if (hmin < h0) areas.push_back(hmin);
+  if (hmin < h0 / 2) areas.push_back(h0 / 2);
+  areas.push_back(0u);
+  areas.push_back(2 * h0);
   std::vector<SearchShape> cand;
   for (int w : {1, 2, 4, 8})
-    for (uint32_t h : {0u, 2 * h0}) cand.push_back(SearchShape{w, h});
+    for (uint32_t h : areas) cand.push_back(SearchShape{w, h});
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   WV_CUDA(c, cudaEventCreate(&e0));
   WV_CUDA(c, cudaEventCreate(&e1));
@@ -355,7 +361,7 @@ int wv_plan_tune(wv_plan *p, uint32_t nq, wv_tune_report *rep) {
       break;
     }
     if (r.n < WV_TUNE_MAX) {
-      r.tried[r.n] = wv_plan_shape{sh.wpb, search_hash_slots(p->Lcap, sh.hcap), blocks, ms};
+      r.tried[r.n] = wv_plan_shape{sh.wpb, search_hash_slots(p->Lcap, sh.hcap), sh.wide ? 1 : 0, blocks, ms};
       if (ms < best) {
         best = ms;
         chosen = sh;
@@ -389,8 +395,36 @@ int wv_plan_search_ms(wv_plan *p, float *ms) {
 
 int wv_plan_shape_of(wv_plan *p, wv_plan_shape *out) {
   if (!p || !out) return WV_ERR_ARG;
-  *out = wv_plan_shape{p->shape.wpb, search_hash_slots(p->Lcap, p->shape.hcap), p->blocks, 0.f};
+  *out = wv_plan_shape{p->shape.wpb, search_hash_slots(p->Lcap, p->shape.hcap), p->shape.wide ? 1 : 0, p->blocks,
+                       0.f};
   return WV_OK;
+}
+
+int wv_plan_set_shape(wv_plan *p, const wv_plan_shape *sh) {
+  if (!p || !sh) return WV_ERR_ARG;
+  wv_ctx *c = p->c;
+  int rc = check_usable(p);
+  if (rc) return rc;
+  WV_CHECK(c, sh->warps_per_block == 1 || sh->warps_per_block == 2 || sh->warps_per_block == 4 ||
+                  sh->warps_per_block == 8,
+           WV_ERR_ARG, "warps_per_block must be 1, 2, 4 or 8");
+  WV_CHECK(c, sh->hash_words == 0 || (sh->hash_words & (sh->hash_words - 1)) == 0, WV_ERR_ARG,
+           "hash_words must be 0 or a power of two");
+  WV_CHECK(c, sh->hash_words == 0 || sh->hash_words >= search_hash_min(p->Lcap, c->n), WV_ERR_ARG,
+           "hash_words=%u below the least area %u for L=%u, n=%u", sh->hash_words, search_hash_min(p->Lcap, c->n),
+           p->Lcap, c->n);
+  rc = wait_pending(p);
+  if (rc) return rc;
+  const SearchShape old = p->shape;
+  p->shape = SearchShape{sh->warps_per_block, sh->hash_words, sh->wide_hash != 0};
+  rc = capture(p);
+  if (rc) {
+    const std::string msg = c->err;
+    p->shape = old;
+    capture(p);
+    c->err = msg;
+  }
+  return rc;
 }
 
 int wv_plan_destroy(wv_plan *p) {

@@ -63,14 +63,20 @@ __host__ __device__ inline uint32_t pow2_at_least(uint32_t x) {
 }
 // pool: L entries, merged in place
 __host__ __device__ inline uint32_t pool_cap(uint32_t Lmax) { return (Lmax + 3) & ~3u; }
-// hash slots (a power of two): >= 2048, and room for the seed sort's scratch
-// (the bitonic keys 2 * pow2(L) <= pow2(2L + 256), the introsort's
-// 2L + 256 words, the rerank's 2L words)
+// hash area (32-bit words, a power of two), also the scratch of the seed
+// sort and the rerank.  Default: >= 2048 and room for the bitonic keys
+// (2 * pow2(L) <= pow2(2L + 256)), the introsort's 2L + 256 words and the
+// rerank's 2L words.  The least area a launch may ask for holds the bitonic
+// keys and the rerank (2 * pow2(L)); the introsort then works in the warp's
+// global scratch (the host allows that area only when the scratch is big
+// enough).
 __host__ __device__ inline uint32_t hash_cap(uint32_t Lmax) { return pow2_at_least(max(2048u, 2 * Lmax + 256)); }
-// the slots a launch uses: the default, or a larger power of two asked for
+__host__ __device__ inline uint32_t hash_min(uint32_t Lmax) { return max(512u, 2 * pow2_at_least(Lmax)); }
+// the area a launch uses: the default, or the power of two asked for (not
+// below the least)
 __host__ __device__ inline uint32_t hash_slots(uint32_t Lmax, uint32_t want) {
-  const uint32_t h = hash_cap(Lmax);
-  return want > h ? pow2_at_least(want) : h;
+  if (want == 0) return hash_cap(Lmax);
+  return max(pow2_at_least(want), hash_min(Lmax));
 }
 
 struct WarpSmem {
@@ -124,6 +130,18 @@ __device__ inline int first_flag(const uint32_t *pi, int from, int L, int lane) 
   return L;
 }
 
+// number of entries of the sorted array a[0..n) with a[i] < x (lower bound)
+template <class T>
+__device__ inline int lower_bound_of(const T *a, int n, T x) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
 // number of entries of the sorted array a[0..n) with a[i] <= x (upper bound)
 template <class T>
 __device__ inline int upper_bound_of(const T *a, int n, T x) {
@@ -138,39 +156,153 @@ __device__ inline int upper_bound_of(const T *a, int n, T x) {
 
 __device__ __forceinline__ uint32_t hslot(uint32_t id, uint32_t mask) { return (id * 2654435761u) & mask; }
 
-// visited test-and-set over a shared-memory hash that spills to a bitset
+// Visited set: an open-addressing hash in shared memory while it is at most
+// half full, then the warp's own n-bit bitset in global memory for ids the
+// hash does not hold.  Exact either way.
+//
+// Narrow form (whenever n is small enough): 16-bit entries, twice the slots
+// of the wide form in the same bytes.  An id is mapped by a bijection y of
+// its B-bit value (B = bits of n - 1, at least log2(slots) + 1); the low
+// log2(slots) bits of y are its home slot and the rest its quotient q.  An
+// entry stores q and the probe distance t of its slot from home (linear
+// probing, no deletions), so (slot - t, q) gives y back: an entry matches an
+// id exactly.  A probe longer than the distance field holds sends that id
+// to the bitset (and the hash to its spill mode).  Bit 15 marks a seed.
+// Wide form: the ids themselves (32-bit), bit 31 marking a seed.
 struct Visited {
   uint32_t *hash, mask, inserted, limit;
-  bool spill;  // the hash reached its limit: new ids go to the global bitset
+  bool spill;      // the hash is full (or an id overflowed): new ids go to the bitset
+  bool seed_over;  // a seed did not fit (narrow form): candidates are checked against the pool
+  bool narrow;
+  uint32_t nbits, shift, cbits, qbits, dmax;  // narrow form: B, B - log2(slots), log2(slots), quotient bits, longest probe
   uint32_t *bits, *touched, ntouch;
 
+  // slots: a power of two (the number of 32-bit words of the area)
+  __device__ void init(uint32_t *area, uint32_t words, uint32_t n, bool force_wide) {
+    hash = area;
+    uint32_t lg = 0;
+    while ((2u << lg) <= words) lg++;  // words = 2^lg
+    uint32_t B = 1;
+    while (B < 32 && (n - 1) >> B) B++;
+    const uint32_t c = lg + 1;  // narrow slots = 2 * words
+    if (B < c + 1) B = c + 1;
+    const uint32_t qb = B - c;
+    narrow = !force_wide && qb + 1 + 4 <= 16;  // room for a probe distance of at least 4 bits
+    if (narrow) {
+      mask = 2 * words - 1;
+      nbits = B;
+      cbits = c;
+      shift = B - c;
+      qbits = qb;
+      dmax = (1u << (15 - qb)) - 2;  // the all-ones entry stays EMPTY
+    } else {
+      mask = words - 1;
+    }
+    limit = (mask + 1) / 2;
+    inserted = 0;
+    spill = seed_over = false;
+    ntouch = 0;
+  }
   __device__ void clear(int lane) {
-    for (uint32_t i = lane; i <= mask; i += 32) hash[i] = EMPTY;
+    const uint32_t words = narrow ? (mask + 1) / 2 : mask + 1;
+    for (uint32_t i = lane; i < words; i += 32) hash[i] = EMPTY;
     __syncwarp();
     for (uint32_t i = lane; i < ntouch; i += 32) bits[touched[i]] = 0u;
     __syncwarp();
     inserted = 0;
-    spill = false;
+    spill = seed_over = false;
     ntouch = 0;
   }
+  __device__ __forceinline__ uint32_t mixed(uint32_t id) const {
+    const uint32_t m = nbits >= 32 ? 0xffffffffu : ((1u << nbits) - 1u);
+    uint32_t y = (id * 0x9E3779B1u) & m;
+    return y ^ (y >> shift);
+  }
+  __device__ __forceinline__ uint16_t *h16() const { return reinterpret_cast<uint16_t *>(hash); }
+
+  // insert `id` (seed: marked); returns 1 inserted, 0 present, -1 no room
+  // within the probe limit (narrow form)
+  __device__ int insert(uint32_t id, bool seed, bool &was_seed) {
+    was_seed = false;
+    if (narrow) {
+      const uint32_t y = mixed(id), home = y & mask, q = y >> cbits;
+      for (uint32_t t = 0; t <= dmax; t++) {
+        const uint32_t h = (home + t) & mask;
+        const uint16_t e = (uint16_t)(q | (t << qbits));
+        const uint16_t old = atomicCAS(h16() + h, (uint16_t)0xffff, (uint16_t)(seed ? (e | 0x8000) : e));
+        if (old == 0xffff) return 1;
+        if (old == e) return 0;
+        if (old == (e | 0x8000)) {
+          if (!seed) {
+            h16()[h] = e;
+            was_seed = true;
+            return 1;  // fresh: the first time a seed is met as a neighbour
+          }
+          return 0;
+        }
+      }
+      return -1;
+    }
+    uint32_t h = hslot(id, mask);
+    while (true) {
+      const uint32_t old = atomicCAS(&hash[h], EMPTY, seed ? (id | SEEDBIT) : id);
+      if (old == EMPTY) return 1;
+      if (old == id) return 0;
+      if (old == (id | SEEDBIT)) {
+        if (!seed) {
+          hash[h] = id;
+          was_seed = true;
+          return 1;
+        }
+        return 0;
+      }
+      h = (h + 1) & mask;
+    }
+  }
+  // spill mode: 1 found (was_seed: a seed, now converted), 0 absent
+  __device__ int find(uint32_t id, bool &was_seed) {
+    was_seed = false;
+    if (narrow) {
+      const uint32_t y = mixed(id), home = y & mask, q = y >> cbits;
+      for (uint32_t t = 0; t <= dmax; t++) {
+        const uint32_t h = (home + t) & mask;
+        const uint16_t e = (uint16_t)(q | (t << qbits));
+        const uint16_t v = h16()[h];
+        if (v == 0xffff) return 0;
+        if (v == e) return 1;
+        if (v == (e | 0x8000)) {
+          h16()[h] = e;
+          was_seed = true;
+          return 1;
+        }
+      }
+      return 0;
+    }
+    uint32_t h = hslot(id, mask);
+    while (true) {
+      const uint32_t v = hash[h];
+      if (v == id) return 1;
+      if (v == (id | SEEDBIT)) {
+        hash[h] = id;
+        was_seed = true;
+        return 1;
+      }
+      if (v == EMPTY) return 0;
+      h = (h + 1) & mask;
+    }
+  }
+
   // route mode: records the seeds (not visited) so that a seed met again is
   // known; warp-uniform call, ids distinct among the `want` lanes; the hash
   // has room for every seed (limit >= SEARCH_MAX_L + 128)
   __device__ void add_seed(bool want, uint32_t id) {
-    bool added = false;
+    int r = 0;
     if (want) {
-      uint32_t h = hslot(id, mask);
-      while (true) {
-        const uint32_t old = atomicCAS(&hash[h], EMPTY, id | SEEDBIT);
-        if (old == EMPTY) {
-          added = true;
-          break;
-        }
-        if (old == (id | SEEDBIT)) break;
-        h = (h + 1) & mask;
-      }
+      bool ws;
+      r = insert(id, true, ws);
     }
-    inserted += __popc(__ballot_sync(FULL, added));
+    inserted += __popc(__ballot_sync(FULL, r == 1));
+    if (__any_sync(FULL, r < 0)) seed_over = true;
   }
   // warp-uniform call; `want` lanes test `id` (ids distinct among lanes);
   // returns true for lanes whose id was not visited before; `seed` is set
@@ -178,50 +310,27 @@ struct Visited {
   __device__ bool test_and_set(bool want, uint32_t id, int lane, bool &seed) {
     const unsigned wm = __ballot_sync(FULL, want);
     if (!spill && inserted + __popc(wm) > limit) spill = true;
-    bool fresh = false, newword = false, added = false;
+    bool fresh = false, newword = false, added = false, to_bits = false;
     seed = false;
     if (want) {
-      uint32_t h = hslot(id, mask);
       if (!spill) {
-        while (true) {
-          const uint32_t old = atomicCAS(&hash[h], EMPTY, id);
-          if (old == EMPTY) {
-            fresh = added = true;
-            break;
-          }
-          if (old == id) break;
-          if (old == (id | SEEDBIT)) {  // only this lane holds this id
-            hash[h] = id;
-            fresh = seed = true;
-            break;
-          }
-          h = (h + 1) & mask;
-        }
+        const int r = insert(id, false, seed);
+        fresh = r == 1;
+        added = r == 1 && !seed;
+        to_bits = r < 0;
       } else {
-        bool in_hash = false;
-        while (true) {
-          const uint32_t v = hash[h];
-          if (v == id) {
-            in_hash = true;
-            break;
-          }
-          if (v == (id | SEEDBIT)) {
-            hash[h] = id;
-            in_hash = fresh = seed = true;
-            break;
-          }
-          if (v == EMPTY) break;
-          h = (h + 1) & mask;
-        }
-        if (!in_hash) {
-          const uint32_t bit = 1u << (id & 31);
-          const uint32_t old = atomicOr(bits + (id >> 5), bit);
-          fresh = (old & bit) == 0;
-          newword = old == 0;
-        }
+        to_bits = find(id, seed) == 0;
+        fresh = seed;
+      }
+      if (to_bits) {
+        const uint32_t bit = 1u << (id & 31);
+        const uint32_t old = atomicOr(bits + (id >> 5), bit);
+        fresh = (old & bit) == 0;
+        newword = old == 0;
       }
     }
-    if (!spill) inserted += __popc(__ballot_sync(FULL, added));
+    if (__any_sync(FULL, to_bits)) spill = true;  // an overflow keeps later lookups exact
+    inserted += __popc(__ballot_sync(FULL, added));
     const unsigned nwm = __ballot_sync(FULL, newword);
     if (newword) touched[ntouch + __popc(nwm & ((1u << lane) - 1u))] = id >> 5;
     ntouch += __popc(nwm);
@@ -235,7 +344,7 @@ struct Visited {
 // std::sort's whenever L <= 16 or no two seed distances tie; otherwise the
 // warp replays libstdc++'s introsort (warp_sort.cuh) on the drawn order.  The
 // hash area is the scratch (the caller clears it afterwards).
-__device__ void sort_seeds(WarpSmem &s, int L, int lane) {
+__device__ void sort_seeds(WarpSmem &s, int L, uint32_t hwords, uint32_t *gscratch, int lane) {
   const int P = (int)pow2_at_least((uint32_t)L);
   const DI *dv = reinterpret_cast<const DI *>(s.pd);
   float *kd = reinterpret_cast<float *>(s.hash);
@@ -278,12 +387,15 @@ __device__ void sort_seeds(WarpSmem &s, int L, int lane) {
   } else {
     // ties and L > 16: libstdc++ introsort on the drawn order, in place over
     // the pool region (pd and pi are contiguous, 2 * pcap >= 2L words), the
-    // partition scratch in the hash area; unpacked through the hash area
+    // partition scratch (2L + 256 words) in the hash area when it fits, else
+    // in the warp's global scratch; unpacked through the same place
     __syncwarp();
     DI *tmp = reinterpret_cast<DI *>(s.pd);
-    int *scr = reinterpret_cast<int *>(s.hash);
+    uint32_t *area = hwords >= (uint32_t)(2 * L + 256) ? s.hash : gscratch;
+    int *scr = reinterpret_cast<int *>(area);
     warp_std_sort(tmp, L, DILess(), WarpSortScratch{scr, scr + L, scr + 2 * L, scr + 2 * L + 192}, lane);
-    DI *cp = reinterpret_cast<DI *>(s.hash);
+    __syncwarp();
+    DI *cp = reinterpret_cast<DI *>(area);
     for (int i = lane; i < L; i += 32) cp[i] = tmp[i];
     __syncwarp();
     for (int i = lane; i < L; i += 32) {
@@ -382,14 +494,9 @@ __global__ void __maxnreg__(96) k_search(SearchArgs a) {
   const uint32_t hs = hash_slots(a.Lmax, a.hcap);
   const uint32_t nq = a.nq_dev ? *a.nq_dev : a.nq;
   Visited vis;
-  vis.hash = s.hash;
-  vis.mask = hs - 1;
-  vis.limit = hs / 2;
+  vis.init(s.hash, hs, a.n, a.wide_hash != 0);
   vis.bits = a.visited + (size_t)slot * a.words;
   vis.touched = a.touched + (size_t)slot * a.words;
-  vis.ntouch = 0;
-  vis.inserted = 0;
-  vis.spill = false;
   unsigned long long dcount = 0, hcount = 0;
   const unsigned lt = (1u << lane) - 1u;
   float *pd = s.pd;
@@ -439,7 +546,7 @@ __global__ void __maxnreg__(96) k_search(SearchArgs a) {
     }
     dcount += L;
     __syncwarp();
-    sort_seeds(s, L, lane);
+    sort_seeds(s, L, hs, vis.touched, lane);  // (the touched list is empty between queries)
     vis.clear(lane);  // the seed sort used the hash as scratch
     // CandidateNSG flags its seeds (component_candidate.cpp:21-29); the route
     // leaves them unvisited and records them as seeds
@@ -518,7 +625,14 @@ __global__ void __maxnreg__(96) k_search(SearchArgs a) {
           if (lane < cnt && nvis + lane < a.vlimit) vis_out[nvis + lane] = DI{dist, my};
           nvis += cnt;
         }
-        const bool acc = lane < cnt && dist < thr && !(raw & SEEDBIT);
+        bool acc = lane < cnt && dist < thr && !(raw & SEEDBIT);
+        if (acc && vis.seed_over) {
+          // a seed the hash could not record: look for the id in the pool
+          // (same id, same distance: inside the run of equal distances)
+          const int lo = lower_bound_of(pd, L, dist), hi = upper_bound_of(pd, L, dist);
+          for (int t = lo; t < hi && acc; t++)
+            if ((pi[t] & ID_MASK) == my) acc = false;
+        }
         const unsigned am = __ballot_sync(FULL, acc);
         if (acc) {
           const int r = ncand + __popc(am & lt);
@@ -667,6 +781,10 @@ size_t search_block_smem(uint32_t d, uint32_t Lmax, uint32_t cap) {
 int search_warps_per_block() { return WARPS; }
 
 uint32_t search_hash_slots(uint32_t Lmax, uint32_t want) { return hash_slots(Lmax, want); }
+uint32_t search_hash_min(uint32_t Lmax, uint32_t n) {
+  const size_t words = ((size_t)n + 31) / 32;
+  return words >= 2 * (size_t)Lmax + 256 ? hash_min(Lmax) : hash_cap(Lmax);
+}
 
 int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device, SearchShape sh) {
   if (!shape_ok(sh)) return 0;
@@ -696,6 +814,7 @@ cudaError_t launch_search(const SearchArgs &a, SearchShape sh, int blocks, cudaS
   if (!shape_ok(sh)) return cudaErrorInvalidValue;
   SearchArgs b = a;
   b.hcap = sh.hcap;
+  b.wide_hash = sh.wide ? 1 : 0;
   const size_t smem = search_block_smem(a.d, a.Lmax, a.cap, sh);
   if (a.vis) return sh.wpb == WARPS ? launch_w<true, WARPS>(b, blocks, smem, stream) : cudaErrorInvalidValue;
   switch (sh.wpb) {

@@ -30,7 +30,8 @@ struct SearchArgs {
   uint32_t *touched;             // slots x words
   uint32_t words;
   uint32_t cap;   // candidate buffer entries per warp (graph width + 32)
-  uint32_t hcap;  // visited-hash slots per warp (0: the default for Lmax); set by launch_search
+  uint32_t hcap;  // visited-hash area per warp, 32-bit words (0: the default for Lmax); set by launch_search
+  int wide_hash;  // 32-bit hash entries only (set by launch_search)
   unsigned *next_query;
   int *status;
   // candidate-search (build) mode: visit lists, vcap entries per query
@@ -55,13 +56,15 @@ constexpr uint32_t SEARCH_MAX_WIDTH = 256;  // graph row width the kernel accept
 constexpr uint32_t SEARCH_MAX_L = 1536;  // exact seed sort scratch: 2L + 256 words of stage
 
 // the tunable launch shape of the route kernel: warps per block (1, 2, 4 or
-// 8; one warp serves one query at a time) and visited-hash slots per warp (0:
-// the default, 2L + 256 rounded up to a power of two, at least 2048; more
-// slots keep longer searches off the global bitset but cost occupancy).
+// 8; one warp serves one query at a time) and the visited-hash area per warp
+// in 32-bit words (0: the default, 2L + 256 rounded up to a power of two, at
+// least 2048; a larger area keeps longer searches off the global bitset but
+// costs occupancy), holding twice as many 16-bit entries unless `wide`.
 // The build (candidate-search) variant runs in the default shape only.
 struct SearchShape {
   int wpb = 4;
   uint32_t hcap = 0;
+  bool wide = false;  // 32-bit visited-hash entries even where 16-bit ones would do
 };
 
 // bytes of dynamic shared memory per block and warps per block
@@ -69,6 +72,10 @@ size_t search_block_smem(uint32_t d, uint32_t Lmax, uint32_t cap, SearchShape sh
 size_t search_block_smem(uint32_t d, uint32_t Lmax, uint32_t cap);
 int search_warps_per_block();
 uint32_t search_hash_slots(uint32_t Lmax, uint32_t want);
+// the least hash area (words) a launch at beams up to Lmax may ask for; it
+// needs n >= 32 * (2 Lmax + 256) (the introsort scratch then lives in the
+// warp's global scratch of ceil(n / 32) words)
+uint32_t search_hash_min(uint32_t Lmax, uint32_t n);
 // blocks to launch for one persistent wave on this device (0 if it cannot run)
 int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device, SearchShape sh);
 int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device);
