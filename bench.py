@@ -502,6 +502,199 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ the other configurations
+# Informational lines (one JSON line each, its own metric); the default run
+# measures the 1M x 128 configuration above.
+
+def _setup(cfg, ds_fn, nq):
+    import torch
+    from weavess_gb300 import Context
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    t = time.time()
+    base, query = ds_fn(cfg["n"], cfg["d"], n_query=nq)
+    log(f"data {base.shape} {query.shape} in {time.time() - t:.1f}s")
+    ctx = Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    build_s, stages = build_index(ctx, base, cfg)
+    log(f"build {build_s:.2f}s")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    return torch, dev, base, query, ctx, stream, flush, build_s, stages
+
+
+def _timed_plan(torch, plan, nq, args, stream, flush):
+    plan.run(nq)
+    counters = plan.wait()
+    for _ in range(args.warmup):
+        plan.run(nq)
+        plan.wait()
+    kms = []
+    with Clocks() as clk:
+        step_ms = timed_steps(lambda: plan.run(nq), args.steps, stream, flush, clk,
+                              after=lambda i: kms.append(plan.search_ms()))
+    plan.wait()
+    return float(np.mean(step_ms)), float(np.mean(kms)), counters, clk.summary()
+
+
+def run_precision96(args):
+    """1M x 96 unit-norm vectors (isotropic part + 1,000 directions, cosine
+    ~0.7), NN-Descent -> NSG R=32; the plain search with FP32, bf16 and fp8
+    e4m3 (per-row scale) candidate distances, each with the exact FP32 rerank
+    of the final pool: QPS at recall@10 >= 0.95 per precision, and the
+    candidate-distance error against FP64."""
+    from weavess_gb300.groundtruth import knn_fp64
+    cfg = dict(CFG)
+    cfg.update(n=args.n or 1_000_000, d=96, nq=args.nq or 10_000)
+    torch, dev, base, query, ctx, stream, flush, build_s, _ = _setup(
+        cfg, lambda n, d, n_query: ds.unit_mixture(n, d, 1000, seed=11, n_query=n_query), cfg["nq"])
+    gt = knn_fp64(base, query, 100)
+    nq, K = query.shape[0], cfg["k"]
+    # candidate-distance error vs FP64: each of 1,000 queries against its
+    # true 100 nearest and 100 random rows
+    rng = np.random.default_rng(3)
+    qs = query[:1000]
+    ids = np.concatenate([gt[:1000, :100], rng.integers(0, base.shape[0], size=(1000, 100))], 1).astype(np.uint32)
+    exact = ((qs[:, None, :].astype(np.float64) - base[ids].astype(np.float64)) ** 2).sum(2)
+    out = {}
+    dq = torch.from_numpy(query).to(dev)
+    dout = torch.empty((nq, K), dtype=torch.int32, device=dev)
+    for storage in ("fp32", "bf16", "fp8"):
+        ctx.set_precision(storage, rerank=0)
+        got = ctx.candidate_distances(qs, ids).astype(np.float64)
+        err = np.abs(got - exact)
+        sweep, Lsel = {}, cfg["L_grid"][-1]
+        for L in cfg["L_grid"]:
+            ctx.srand(12345)
+            res, _, _ = ctx.search(query, L, K)
+            sweep[L] = round(recall(res, gt, K), 4)
+            if sweep[L] >= cfg["target_recall"]:
+                Lsel = L
+                break
+        ctx.srand(777)
+        seeds = torch.from_numpy(ctx.draw_seeds(nq, Lsel, "rand").astype(np.int32)).to(dev)
+        plan = ctx.plan(nq, K, dq.data_ptr(), dout.data_ptr(), L_max=Lsel, mode="seeds", d_seeds=seeds.data_ptr())
+        tune = plan.tune(nq)
+        ms, kms, (dc, hc), clk = _timed_plan(torch, plan, nq, args, stream, flush)
+        plan.close()
+        r = recall(dout.cpu().numpy().astype(np.uint32), gt, K)
+        out[storage] = {"qps": round(nq / (ms / 1e3), 1), "L_search": Lsel, "recall@10": round(r, 4),
+                        "recall_sweep": sweep, "search_kernel_ms": round(kms, 4), "dist_count": dc,
+                        "tuned_shape": tune["chosen"], "clocks": clk,
+                        "err_vs_fp64": {"max_abs": float(err.max()), "mean_abs": float(err.mean()),
+                                        "max_rel_to_mean_dist": float(err.max() / exact.mean()),
+                                        "mean_rel": float((err / np.maximum(exact, 1e-12)).mean())}}
+        log(f"{storage}: {out[storage]}")
+    ctx.set_precision("fp32")
+    best = max(out, key=lambda k: out[k]["qps"])
+    line = {"metric": "QPS at recall@10>=0.95 per candidate precision (1M x 96 unit vectors)",
+            "value": out[best]["qps"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": best, "data": "synthetic (seeded unit-norm mixture)",
+            "config": {"workload": f"{cfg['n']}x96 unit-mixture, {nq} queries, top-10, NN-Descent S=20 K=64 L=80 "
+                                   f"ITER=8 R=100 -> NSG R=32 L_refine=64 C_refine=500, exact FP32 rerank of "
+                                   f"the whole pool", "build_s": round(build_s, 2), "by_precision": out}}
+    print(json.dumps(line), flush=True)
+
+
+def run_batch960(args):
+    """1M x 960 non-negative vectors summing to 1 (512-component mixture),
+    NN-Descent -> NSG R=48; one launch serves 20,000 queries with k drawn
+    from {1, 10, 50, 100} and L uniform on [10, 500] (L >= k): a tuned,
+    captured plan; QPS and recall@k per k."""
+    from weavess_gb300.groundtruth import knn_fp64
+    cfg = dict(CFG)
+    cfg.update(n=args.n or 1_000_000, d=960, nq=args.nq or 20_000, R_refine=48)
+    torch, dev, base, query, ctx, stream, flush, build_s, stages = _setup(
+        cfg, lambda n, d, n_query: ds.simplex_mixture(n, d, 512, seed=13, n_query=n_query), cfg["nq"])
+    gt = knn_fp64(base, query, 100)
+    nq = query.shape[0]
+    rng = np.random.default_rng(4)
+    K = rng.choice([1, 10, 50, 100], size=nq).astype(np.int32)
+    L = np.maximum(K, rng.integers(10, 501, size=nq)).astype(np.int32)
+    dq = torch.from_numpy(query).to(dev)
+    dL, dK = torch.from_numpy(L).to(dev), torch.from_numpy(K).to(dev)
+    dout = torch.full((nq, 100), -1, dtype=torch.int32, device=dev)
+    plan = ctx.plan(nq, 100, dq.data_ptr(), dout.data_ptr(), L_max=500, mode="rand", d_L=dL.data_ptr(),
+                    d_K=dK.data_ptr(), out_stride=100)
+    tune = plan.tune(nq)
+    log(f"tuning {tune}")
+    ms, kms, (dc, hc), clk = _timed_plan(torch, plan, nq, args, stream, flush)
+    plan.close()
+    out = dout.cpu().numpy()
+    rec = {}
+    for k in (1, 10, 50, 100):
+        sel = np.nonzero(K == k)[0]
+        hit = sum(len(set(out[i, :k].tolist()) & set(gt[i, :k].tolist())) for i in sel)
+        rec[k] = round(hit / max(1, len(sel) * k), 4)
+    line = {"metric": "QPS, one launch of 20,000 queries with mixed k and L (1M x 960)",
+            "value": round(nq / (ms / 1e3), 1), "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded simplex mixture)",
+            "config": {"workload": f"{cfg['n']}x960 simplex-mixture(512), {nq} queries, k in {{1,10,50,100}}, "
+                                   f"L~U[10,500], NN-Descent S=20 K=64 L=80 ITER=8 R=100 -> NSG R=48 "
+                                   f"L_refine=64 C_refine=500", "build_s": round(build_s, 2),
+                       "build_stages": {k: {kk: (round(vv, 2) if isinstance(vv, float) else vv)
+                                            for kk, vv in v.items()} for k, v in stages.items()},
+                       "recall_at_k": rec, "search_kernel_ms": round(kms, 4), "dist_count": dc, "hop_count": hc,
+                       "tuned_shape": tune["chosen"], "tune": tune["tried"]},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
+def run_learned10m(args):
+    """10M x 128 integer mixture (1,024 centres), NN-Descent -> NSG R=32; the
+    learned entry / beam (64 clusters, trained on 200,000 plain-search traces)
+    with bf16 candidates against the plain FP32 search, 10,000 held-out
+    queries; QPS at recall@10 >= 0.95 (or the best recall the beam cap
+    reaches)."""
+    from weavess_gb300.groundtruth import knn_fp64
+    cfg = dict(CFG)
+    cfg.update(n=args.n or 10_000_000, centers=1024, nq=args.nq or 10_000)
+    torch, dev, base, query, ctx, stream, flush, build_s, stages = _setup(
+        cfg, lambda n, d, n_query: ds.int_mixture(n, d, cfg["centers"], seed=cfg["seed"], n_query=n_query),
+        cfg["nq"])
+    gt = knn_fp64(base, query, 100)
+    nq, K = query.shape[0], cfg["k"]
+    sweep, Lsel = {}, cfg["L_grid"][-1]
+    for L in cfg["L_grid"]:
+        ctx.srand(12345)
+        res, _, _ = ctx.search(query, L, K)
+        sweep[L] = round(recall(res, gt, K), 4)
+        log(f"plain L={L} recall={sweep[L]}")
+        if sweep[L] >= cfg["target_recall"]:
+            Lsel = L
+            break
+    dq = torch.from_numpy(query).to(dev)
+    dout = torch.empty((nq, K), dtype=torch.int32, device=dev)
+    ctx.srand(777)
+    seeds = torch.from_numpy(ctx.draw_seeds(nq, Lsel, "rand").astype(np.int32)).to(dev)
+    plan = ctx.plan(nq, K, dq.data_ptr(), dout.data_ptr(), L_max=Lsel, mode="seeds", d_seeds=seeds.data_ptr())
+    plan.tune(nq)
+    ms_p, kms_p, _, _ = _timed_plan(torch, plan, nq, args, stream, flush)
+    plan.close()
+    r_p = recall(dout.cpu().numpy().astype(np.uint32), gt, K)
+    learned = run_learned(ctx, cfg, base, query, gt, args, dev, stream, flush)
+    line = {"metric": "QPS at recall@10>=0.95 (learned+BF16 vs plain FP32, 10M x 128)",
+            "value": round(learned["qps"], 1), "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(learned["ms"], 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 candidates, f32 rerank",
+            "data": "synthetic (seeded integer Gaussian mixture)",
+            "config": {"workload": f"{cfg['n']}x128 int-mixture(1024), {nq} held-out queries, top-10, NN-Descent "
+                                   f"S=20 K=64 L=80 ITER=8 R=100 -> NSG R=32 L_refine=64 C_refine=500",
+                       "build_s": round(build_s, 2),
+                       "build_stages": {k: {kk: (round(vv, 2) if isinstance(vv, float) else vv)
+                                            for kk, vv in v.items()} for k, v in stages.items()},
+                       "learned": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in learned.items()},
+                       "plain_fp32": {"qps": round(nq / (ms_p / 1e3), 1), "L_search": Lsel,
+                                      "recall@10": round(r_p, 4), "recall_sweep": sweep,
+                                      "search_kernel_ms": round(kms_p, 4)},
+                       "speedup_vs_plain": round(learned["qps"] / (nq / (ms_p / 1e3)), 3)},
+            "e2e": {"value": round(learned["e2e_qps"], 1), "unit": "queries/s"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -512,6 +705,8 @@ def main():
     ap.add_argument("--nq", type=int, default=0, help="override the number of queries")
     ap.add_argument("--n", type=int, default=0, help="override the number of base vectors")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned + bf16 leg")
+    ap.add_argument("--workload", default="int128", choices=["int128", "precision96", "batch960", "learned10m"],
+                    help="int128: the 1M x 128 measurement (default); the others print informational lines")
     ap.add_argument("--profile-region", choices=["search", "build"], default="search",
                     help="region bracketed by cudaProfilerStart/Stop (ncu --profile-from-start off)")
     args = ap.parse_args()
@@ -526,7 +721,8 @@ def main():
         # search shards by query; this build measures one GPU (replicas only)
         if rank != 0:
             return
-    run_ours(args)
+    {"int128": run_ours, "precision96": run_precision96, "batch960": run_batch960,
+     "learned10m": run_learned10m}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -299,6 +299,11 @@ int wv_search_noalloc(const float *d_base, uint32_t n, uint32_t d, const uint32_
  * warp-parallel, mode 1: one thread), in place, so a test can compare the
  * order of tied keys with the host's std::sort.  Arrays of up to 4096. */
 int wv_debug_sort(wv_ctx *ctx, float *keys, uint32_t *vals, const uint32_t *offsets, uint32_t narr, int mode);
+/* C (M x N, FP32, row-major) = A B with bf16 operands (bit patterns) at
+ * element strides A(m, k) = A[m * sam + k * sak], B(k, n) = B[k * sbk + n * sbn];
+ * impl 0: the mma.sync kernel, 1: the tcgen05 kernel (the MLP's GEMMs). */
+int wv_debug_gemm(wv_ctx *ctx, int impl, uint32_t M, uint32_t N, uint32_t K, const uint16_t *A, long long sam,
+                  long long sak, const uint16_t *B, long long sbk, long long sbn, float *C);
 
 #ifdef __cplusplus
 }

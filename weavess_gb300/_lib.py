@@ -126,6 +126,9 @@ def load(build_if_needed: bool = True):
     L.wv_learn_param_count.argtypes = [C.c_uint32, C.c_uint32, C.POINTER(C.c_ulonglong)]
     L.wv_learn_grad.argtypes = [vp, f32p, u32p, f32p, C.c_uint32, C.c_uint32, f32p, C.c_float, f32p, f32p]
     L.wv_debug_sort.argtypes = [vp, f32p, u32p, u32p, C.c_uint32, C.c_int]
+    u16p = np.ctypeslib.ndpointer(np.uint16, flags="C_CONTIGUOUS")
+    L.wv_debug_gemm.argtypes = [vp, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32, u16p, C.c_longlong, C.c_longlong,
+                                u16p, C.c_longlong, C.c_longlong, f32p]
     L.wv_search_noalloc.argtypes = [vp, C.c_uint32, C.c_uint32, vp, vp, C.c_uint32, vp, C.c_uint32, vp, C.c_uint32,
                                     C.c_uint32, vp, vp, vp]
     L.wv_plan_create.argtypes = [vp, C.POINTER(PlanParams), vp, vp, vp, vp, vp, vp, C.POINTER(vp)]

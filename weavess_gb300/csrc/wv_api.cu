@@ -40,6 +40,18 @@ __global__ void k_check_int(const float *x, size_t count, int *ok) {
 }
 
 // status code; *out_blocks = the persistent grid of the shape
+// squared norm of every row (warp per row; on integer data any order is exact)
+__global__ void k_row_norms(const float *x, uint32_t n, uint32_t d, float *out) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t r = w; r < n; r += nw) {
+    float a = 0.f;
+    for (uint32_t k = lane; k < d; k += 32) a = fmaf(x[(size_t)r * d + k], x[(size_t)r * d + k], a);
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(FULL, a, o);
+    if (lane == 0) out[r] = a;
+  }
+}
+
 int ensure_search_scratch(wv_ctx *c, uint32_t Lmax, SearchShape sh, int *out_blocks) {
   const uint32_t cap = c->gw + 32;
   int blocks = search_grid(c->d, Lmax, cap, c->device, sh);
@@ -97,9 +109,11 @@ SearchArgs wv::search_args(wv_ctx *c, const float *d_q, uint32_t nq, const uint3
   a.next_query = c->d_next();
   a.status = c->d_status();
   a.int_exact = c->base_int;
+  a.xnorm = c->xnorm.as<float>();
   a.storage = c->storage;
   a.qbase = c->qbase.p;
   a.qscale = c->qscale.as<float>();
+  a.qnorm = c->qnorm.as<float>();
   a.rerank = c->rerank == 0 ? Lmax : c->rerank;
   return a;
 }
@@ -252,6 +266,13 @@ int wv_upload_base(wv_ctx *c, const float *base, uint32_t n, uint32_t d) {
   WV_CUDA(c, cudaMemcpyAsync(&hok, ok, 4, cudaMemcpyDeviceToHost, c->stream));
   WV_CUDA(c, cudaStreamSynchronize(c->stream));
   c->base_int = hok == 1;
+  if (c->base_int) {
+    // the distance kernels use |q|^2 + |x|^2 - 2 q.x on integer data (exact)
+    WV_CUDA(c, c->xnorm.ensure((size_t)n * 4));
+    k_row_norms<<<c->sms * 8, 256, 0, c->stream>>>(c->base.as<float>(), n, d, c->xnorm.as<float>());
+    WV_CUDA(c, cudaGetLastError());
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
   return WV_OK;
 }
 

@@ -53,10 +53,11 @@ struct wv_ctx {
   wv::DevBuf base;
   uint32_t n = 0, d = 0;
   bool base_int = false;  // every value an integer in [0, 255]
+  wv::DevBuf xnorm;       // squared norm of every base row (when base_int: exact)
   // low-precision copy of the base for candidate distances
   int storage = 0;
   uint32_t rerank = 0;
-  wv::DevBuf qbase, qscale;
+  wv::DevBuf qbase, qscale, qnorm;  // qnorm: squared norms of the low-precision rows
 
   // search graph (load_graph_)
   wv::DevBuf gids, gdeg;

@@ -1,8 +1,11 @@
 // Diagnostic entry point: runs the device sort replicas on caller arrays so
 // tests can compare them with the host's std::sort.
+#include <cuda_bf16.h>
+
 #include "warp_sort.cuh"
 #include "wv_common.cuh"
 #include "wv_ctx.h"
+#include "wv_mlp.cuh"
 
 using namespace wv;
 
@@ -61,4 +64,39 @@ extern "C" int wv_debug_sort(wv_ctx *c, float *keys, uint32_t *vals, const uint3
     vals[i] = h[i].i;
   }
   return WV_OK;
+}
+
+// C (M x N, FP32) = A (M x K) B (K x N), bf16 operands given as their bit
+// patterns with element strides; impl 0: mma.sync kernel, 1: tcgen05 kernel
+extern "C" int wv_debug_gemm(wv_ctx *c, int impl, uint32_t M, uint32_t N, uint32_t K, const uint16_t *A,
+                             long long sam, long long sak, const uint16_t *B, long long sbk, long long sbn,
+                             float *C) {
+  if (!c || !A || !B || !C || M == 0 || N == 0 || K == 0) return WV_ERR_ARG;
+  WV_CHECK(c, impl == 0 || impl == 1, WV_ERR_ARG, "impl must be 0 or 1");
+  WV_CUDA(c, cudaSetDevice(c->device));
+  // extents of the strided operands
+  const size_t na = (size_t)((M - 1) * sam + (K - 1) * sak + 1), nb = (size_t)((K - 1) * sbk + (N - 1) * sbn + 1);
+  cudaError_t e = cudaSuccess;
+  uint16_t *dA = c->buf<uint16_t>("dbg_gA", na, &e);
+  uint16_t *dB = c->buf<uint16_t>("dbg_gB", nb, &e);
+  float *dC = c->buf<float>("dbg_gC", (size_t)M * N, &e);
+  WV_CUDA(c, e);
+  WV_CUDA(c, cudaMemcpyAsync(dA, A, na * 2, cudaMemcpyHostToDevice, c->stream));
+  WV_CUDA(c, cudaMemcpyAsync(dB, B, nb * 2, cudaMemcpyHostToDevice, c->stream));
+  GemmArgs g{};
+  g.A = reinterpret_cast<const __nv_bfloat16 *>(dA);
+  g.sam = sam;
+  g.sak = sak;
+  g.B = reinterpret_cast<const __nv_bfloat16 *>(dB);
+  g.sbk = sbk;
+  g.sbn = sbn;
+  g.C = dC;
+  g.ldc = N;
+  g.M = (int)M;
+  g.N = (int)N;
+  g.K = (int)K;
+  WV_CUDA(c, impl == 0 ? gemm_bf16(g, c->stream) : gemm_bf16_umma(g, c->d_status(), c->stream));
+  WV_CUDA(c, cudaMemcpyAsync(C, dC, (size_t)M * N * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  return check_device_status(c, "gemm");
 }

@@ -1,4 +1,5 @@
-// BF16 tensor-core GEMM for the learned entry/beam MLP (see wv_mlp.cuh).
+// BF16 GEMM on the warp-level tensor-core instruction (mma.sync), the
+// cross-check of the tcgen05 GEMM the MLP runs (see wv_mlp.cuh).
 // 64 x 64 output tile per block, K in steps of 32, four warps of 32 x 32,
 // each issuing m16n8k16 MMAs from shared-memory fragments.
 #include "wv_common.cuh"

@@ -11,7 +11,7 @@
 //    cluster's list, matches the plain answer in >= 9 of 10 ids is the
 //    beam label (as log2 L);
 //  * model: x -> 256 -> 256 (ReLU) -> C entry logits + 1 beam regressor, BF16
-//    operands with FP32 accumulation on the tensor cores (wv_gemm.cu),
+//    operands with FP32 accumulation in tensor memory (tcgen05, wv_umma.cu),
 //    softmax cross-entropy + squared error, Adam; every forward, backward and
 //    update step is a kernel of this file;
 //  * inference: one forward pass per query batch picks the entry cluster(s)
@@ -347,10 +347,10 @@ int forward(wv_ctx *c, LearnState &S, const float *x, const uint32_t *rows, uint
   const __nv_bfloat16 *Pb = S.Pb.as<__nv_bfloat16>();
   k_gather_norm<<<nblk((size_t)B * S.D), 256, 0, c->stream>>>(x, rows, B, S.D, S.mu.as<float>(), S.sg.as<float>(),
                                                               w.Xb);
-  WV_CUDA(c, gemm_bf16(gm(w.Xb, S.D, 1, Pb + S.oW1, HID, 1, w.H1, w.H1b, HID, P + S.ob1, 1, B, HID, S.D), c->stream));
-  WV_CUDA(c, gemm_bf16(gm(w.H1b, HID, 1, Pb + S.oW2, HID, 1, w.H2, w.H2b, HID, P + S.ob2, 1, B, HID, HID), c->stream));
-  WV_CUDA(c, gemm_bf16(gm(w.H2b, HID, 1, Pb + S.oW3, S.C + 1, 1, w.O, nullptr, S.C + 1, P + S.ob3, 0, B, S.C + 1, HID),
-                       c->stream));
+  WV_CUDA(c, gemm_bf16_umma(gm(w.Xb, S.D, 1, Pb + S.oW1, HID, 1, w.H1, w.H1b, HID, P + S.ob1, 1, B, HID, S.D), c->d_status(), c->stream));
+  WV_CUDA(c, gemm_bf16_umma(gm(w.H1b, HID, 1, Pb + S.oW2, HID, 1, w.H2, w.H2b, HID, P + S.ob2, 1, B, HID, HID), c->d_status(), c->stream));
+  WV_CUDA(c, gemm_bf16_umma(gm(w.H2b, HID, 1, Pb + S.oW3, S.C + 1, 1, w.O, nullptr, S.C + 1, P + S.ob3, 0, B, S.C + 1, HID),
+                            c->d_status(), c->stream));
   return WV_OK;
 }
 
@@ -362,17 +362,17 @@ int backward(wv_ctx *c, LearnState &S, const uint32_t *yc, const float *yr, cons
   const uint32_t W = S.C + 1;
   k_loss_grad<<<nblk((size_t)B * 32), 256, 0, c->stream>>>(w.O, B, S.C, yc, yr, rows, lam, w.dO, w.dOb, loss);
   // layer 3
-  WV_CUDA(c, gemm_bf16(gm(w.H2b, 1, HID, w.dOb, W, 1, G + S.oW3, nullptr, W, nullptr, 0, HID, W, B), c->stream));
+  WV_CUDA(c, gemm_bf16_umma(gm(w.H2b, 1, HID, w.dOb, W, 1, G + S.oW3, nullptr, W, nullptr, 0, HID, W, B), c->d_status(), c->stream));
   k_colsum<<<nblk(W), 256, 0, c->stream>>>(w.dO, B, W, G + S.ob3);
-  WV_CUDA(c, gemm_bf16(gm(w.dOb, W, 1, Pb + S.oW3, 1, W, w.dH2, nullptr, HID, nullptr, 0, B, HID, W), c->stream));
+  WV_CUDA(c, gemm_bf16_umma(gm(w.dOb, W, 1, Pb + S.oW3, 1, W, w.dH2, nullptr, HID, nullptr, 0, B, HID, W), c->d_status(), c->stream));
   k_relu_bwd<<<nblk((size_t)B * HID), 256, 0, c->stream>>>(w.dH2, w.H2, (size_t)B * HID, w.dZ2, w.dZ2b);
   // layer 2
-  WV_CUDA(c, gemm_bf16(gm(w.H1b, 1, HID, w.dZ2b, HID, 1, G + S.oW2, nullptr, HID, nullptr, 0, HID, HID, B), c->stream));
+  WV_CUDA(c, gemm_bf16_umma(gm(w.H1b, 1, HID, w.dZ2b, HID, 1, G + S.oW2, nullptr, HID, nullptr, 0, HID, HID, B), c->d_status(), c->stream));
   k_colsum<<<nblk(HID), 256, 0, c->stream>>>(w.dZ2, B, HID, G + S.ob2);
-  WV_CUDA(c, gemm_bf16(gm(w.dZ2b, HID, 1, Pb + S.oW2, 1, HID, w.dH1, nullptr, HID, nullptr, 0, B, HID, HID), c->stream));
+  WV_CUDA(c, gemm_bf16_umma(gm(w.dZ2b, HID, 1, Pb + S.oW2, 1, HID, w.dH1, nullptr, HID, nullptr, 0, B, HID, HID), c->d_status(), c->stream));
   k_relu_bwd<<<nblk((size_t)B * HID), 256, 0, c->stream>>>(w.dH1, w.H1, (size_t)B * HID, w.dZ1, w.dZ1b);
   // layer 1
-  WV_CUDA(c, gemm_bf16(gm(w.Xb, 1, S.D, w.dZ1b, HID, 1, G + S.oW1, nullptr, HID, nullptr, 0, S.D, HID, B), c->stream));
+  WV_CUDA(c, gemm_bf16_umma(gm(w.Xb, 1, S.D, w.dZ1b, HID, 1, G + S.oW1, nullptr, HID, nullptr, 0, S.D, HID, B), c->d_status(), c->stream));
   k_colsum<<<nblk(HID), 256, 0, c->stream>>>(w.dZ1, B, HID, G + S.ob1);
   WV_CUDA(c, cudaGetLastError());
   return WV_OK;

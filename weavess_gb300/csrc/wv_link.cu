@@ -627,6 +627,7 @@ int run_build_search(wv_ctx *c, const float *d_queries, uint32_t nq, const uint3
   a.vcap = vcap;
   a.vlimit = vlimit;
   a.int_exact = c->base_int;
+  a.xnorm = c->xnorm.as<float>();
   int nb = (int)std::min<size_t>((size_t)blocks, ((size_t)nq + search_warps_per_block() - 1) / search_warps_per_block());
   WV_CUDA(c, launch_search_exact(a, std::max(nb, 1), c->stream));
   return WV_OK;

@@ -384,7 +384,7 @@ struct Offers {
 
 constexpr int J_THREADS = 256;
 constexpr int J_TI = 16;  // new rows per i tile
-constexpr int J_TJ = 64;  // rows per j tile (new ++ old)
+constexpr int J_TJ = 64;  // rows per j tile (new ++ old); fewer for long rows (the tile must fit shared memory)
 
 __device__ __forceinline__ void emit(const Offers &o, bool ok, uint32_t t, unsigned long long key, uint32_t c,
                                      float d, int lane, int *status) {
@@ -410,7 +410,7 @@ __device__ __forceinline__ void emit(const Offers &o, bool ok, uint32_t t, unsig
 
 // local join of nodes [n0, n1): one block per node
 __global__ void __launch_bounds__(J_THREADS) k_join(Nnd s, uint32_t n0, Offers of, unsigned long long *pairs,
-                                                     int *status) {
+                                                     int *status, uint32_t tjc) {
   extern __shared__ __align__(16) uint8_t smem[];
   const uint32_t n = n0 + blockIdx.x;
   const uint32_t a = s.lnew[n], b = s.lold[n];
@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(J_THREADS) k_join(Nnd s, uint32_t n0, Offers o
   const uint32_t stride = ((s.d + 3) & ~3u) + 4;
   float *ri = (float *)smem;                     // J_TI rows
   float *rj = ri + (size_t)J_TI * stride;        // J_TJ rows
-  uint32_t *ids = (uint32_t *)(rj + (size_t)J_TJ * stride);  // tot ids: new ++ old
+  uint32_t *ids = (uint32_t *)(rj + (size_t)tjc * stride);  // tot ids: new ++ old
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (uint32_t t = threadIdx.x; t < tot; t += J_THREADS)
     ids[t] = t < a ? s.nnew[(size_t)n * s.capn + t] : s.nold[(size_t)n * s.capo + (t - a)];
@@ -428,8 +428,8 @@ __global__ void __launch_bounds__(J_THREADS) k_join(Nnd s, uint32_t n0, Offers o
   unsigned long long npairs = 0;
   for (uint32_t i0 = 0; i0 < a; i0 += J_TI) {
     const uint32_t ti = min((uint32_t)J_TI, a - i0);
-    for (uint32_t j0 = 0; j0 < tot; j0 += J_TJ) {
-      const uint32_t tj = min((uint32_t)J_TJ, tot - j0);
+    for (uint32_t j0 = 0; j0 < tot; j0 += tjc) {
+      const uint32_t tj = min(tjc, tot - j0);
       __syncthreads();
       // stage rows (coalesced 16-byte copies, one row per warp step)
       for (uint32_t r = warp; r < ti + tj; r += J_THREADS / 32) {
@@ -754,7 +754,10 @@ int nndescent_gpu(wv_ctx *c, const NndParams &p, NndStats *st) {
   WV_CUDA(c, cudaGetLastError());
 
   const uint32_t stride = ((c->d + 3) & ~3u) + 4;
-  const size_t join_smem = (size_t)(J_TI + J_TJ) * stride * 4 + (size_t)(s.capn + s.capo) * 4 + 16;
+  uint32_t tjc = J_TJ;
+  while (tjc > 32 && (size_t)(J_TI + tjc) * stride * 4 > 200 * 1024) tjc -= 32;
+  const size_t join_smem = (size_t)(J_TI + tjc) * stride * 4 + (size_t)(s.capn + s.capo) * 4 + 16;
+  WV_CHECK(c, join_smem <= 227 * 1024, WV_ERR_LIMIT, "dimension %u too large for the local-join tile", c->d);
   WV_CUDA(c, cudaFuncSetAttribute(k_join, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)join_smem));
   const size_t apw_smem = (size_t)AP_WARPS * AP_WARP_CAP * sizeof(Grouped) + (size_t)AP_WARPS * (p.L + 1) * sizeof(Ent);
   WV_CUDA(c, cudaFuncSetAttribute(k_apply_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)apw_smem));
@@ -787,7 +790,7 @@ int nndescent_gpu(wv_ctx *c, const NndParams &p, NndStats *st) {
         while (true) {
           WV_CUDA(c, cudaMemsetAsync(tcnt, 0, (size_t)n * 4, c->stream));
           WV_CUDA(c, cudaMemsetAsync(small, 0, 16, c->stream));
-          k_join<<<n1 - n0, J_THREADS, join_smem, c->stream>>>(s, n0, of, pairs, c->d_status());
+          k_join<<<n1 - n0, J_THREADS, join_smem, c->stream>>>(s, n0, of, pairs, c->d_status(), tjc);
           WV_CUDA(c, cudaGetLastError());
           k_active<<<nb, NODE_THREADS, 0, c->stream>>>(n, tcnt, act, small, big, small + 1, AP_WARP_CAP, small + 2);
           uint32_t hs[4];

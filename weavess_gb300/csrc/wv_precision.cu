@@ -34,11 +34,33 @@ __global__ void k_to_fp8(const float *x, uint32_t n, uint32_t d, __nv_fp8_storag
   }
 }
 
+// squared norms of the stored low-precision rows, dequantised (warp per row)
+__global__ void k_lowp_norms(const void *rows, const float *scale, int storage, uint32_t n, uint32_t d, float *out) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t r = w; r < n; r += nw) {
+    float a = 0.f;
+    for (uint32_t k = lane; k < d; k += 32) {
+      float x;
+      if (storage == 1) {
+        x = __bfloat162float(reinterpret_cast<const __nv_bfloat16 *>(rows)[(size_t)r * d + k]);
+      } else {
+        const __half_raw h =
+            __nv_cvt_fp8_to_halfraw(reinterpret_cast<const __nv_fp8_storage_t *>(rows)[(size_t)r * d + k], __NV_E4M3);
+        x = scale[r] * __half2float(*reinterpret_cast<const __half *>(&h));
+      }
+      a = fmaf(x, x, a);
+    }
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(FULL, a, o);
+    if (lane == 0) out[r] = a;
+  }
+}
+
 // out[q, j] = candidate distance of query q to base id ids[q, j]: fp32 in the
 // reference's order, or the search kernel's low-precision distance (one warp
 // per query and 32 ids, the same lowp_rows_dist the search calls)
-__global__ void k_cand_dist(const float *base, LowpRows lp, uint32_t d, const float *queries, const uint32_t *ids,
-                            uint32_t nq, uint32_t m, float *out) {
+__global__ void k_cand_dist(const float *base, LowpRows lp, int base_int, uint32_t d, const float *queries,
+                            const uint32_t *ids, uint32_t nq, uint32_t m, float *out) {
   const int lane = threadIdx.x & 31;
   const size_t w = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
   const uint32_t chunks = (m + 31) / 32;
@@ -47,6 +69,15 @@ __global__ void k_cand_dist(const float *base, LowpRows lp, uint32_t d, const fl
   const int cnt = (int)min(32u, m - j0);
   const float *qv = queries + (size_t)q * d;
   const uint32_t my = lane < cnt ? ids[(size_t)q * m + j0 + lane] : 0u;
+  float qn = 0.f;
+  bool qint = true;
+  for (uint32_t k = lane; k < d; k += 32) {
+    qn = fmaf(qv[k], qv[k], qn);
+    qint &= qv[k] >= 0.f && qv[k] <= 255.f && qv[k] == rintf(qv[k]);
+  }
+  for (int o = 16; o > 0; o >>= 1) qn += __shfl_xor_sync(FULL, qn, o);
+  // as the search: the difference form for integer data at d > 128
+  if (lp.norm && base_int && d > 128 && __all_sync(FULL, qint)) lp.norm = nullptr;
   float v;
   if (lp.storage == 0) {
     v = 0.f;
@@ -56,7 +87,7 @@ __global__ void k_cand_dist(const float *base, LowpRows lp, uint32_t d, const fl
       for (uint32_t g = 0; g < d / 4; g++) v = __fadd_rn(v, group4(row[g], q4[g]));
     }
   } else {
-    v = lowp_rows_dist(lp, my, cnt, qv, lane);
+    v = lowp_rows_dist(lp, my, cnt, qv, qn, lane);
   }
   if (lane < cnt) out[(size_t)q * m + j0 + lane] = v;
 }
@@ -82,6 +113,12 @@ int wv_set_search_precision(wv_ctx *c, int storage, uint32_t rerank) {
                                                  c->qbase.as<__nv_fp8_storage_t>(), c->qscale.as<float>());
   }
   WV_CUDA(c, cudaGetLastError());
+  if (storage != 0) {
+    WV_CUDA(c, c->qnorm.ensure((size_t)c->n * 4));
+    k_lowp_norms<<<c->sms * 8, 256, 0, c->stream>>>(c->qbase.p, c->qscale.as<float>(), storage, c->n, c->d,
+                                                    c->qnorm.as<float>());
+    WV_CUDA(c, cudaGetLastError());
+  }
   WV_CUDA(c, cudaStreamSynchronize(c->stream));
   c->generation++;
   c->storage = storage;
@@ -105,7 +142,8 @@ int wv_candidate_distances(wv_ctx *c, const float *queries, uint32_t nq, const u
   WV_CUDA(c, cudaMemcpyAsync(di, ids, (size_t)nq * m * 4, cudaMemcpyHostToDevice, c->stream));
   const size_t warps = (size_t)nq * ((m + 31) / 32);
   k_cand_dist<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, c->stream>>>(
-      c->base.as<float>(), LowpRows{c->qbase.p, c->qscale.as<float>(), c->storage, c->d}, c->d, dq, di, nq, m, dout);
+      c->base.as<float>(), LowpRows{c->qbase.p, c->qscale.as<float>(), c->qnorm.as<float>(), c->storage, c->d},
+      c->base_int ? 1 : 0, c->d, dq, di, nq, m, dout);
   WV_CUDA(c, cudaGetLastError());
   WV_CUDA(c, cudaMemcpyAsync(out, dout, (size_t)nq * m * 4, cudaMemcpyDeviceToHost, c->stream));
   WV_CUDA(c, cudaStreamSynchronize(c->stream));

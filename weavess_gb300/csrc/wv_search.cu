@@ -411,10 +411,16 @@ __device__ void sort_seeds(WarpSmem &s, int L, uint32_t hwords, uint32_t *gscrat
 // else one lane per row in the reference's order.
 template <bool INTS>
 __device__ __forceinline__ float batch_dist(const float *__restrict__ base, uint32_t d, uint32_t my, int cnt,
-                                            const float *qv, int lane) {
+                                            const float *qv, int lane, float qn = 0.f,
+                                            const float *__restrict__ xnorm = nullptr) {
   float out = 0.f;
   const uint32_t d4 = d >> 2;
   if (INTS) {
+    // with row norms (d <= 128): |q|^2 + |x|^2 - 2 q.x, integers below 2^24
+    // throughout (|q|^2 + |x|^2 <= 2 * 128 * 255^2), so exact; else the
+    // difference form, exact in any order for d <= 256
+    const bool dot = xnorm != nullptr;
+    const float xn = (dot && lane < cnt) ? __ldg(xnorm + my) : 0.f;
     const float4 *q4 = reinterpret_cast<const float4 *>(qv);
     constexpr int G = 8;
     for (int c0 = 0; c0 < cnt; c0 += G) {
@@ -435,13 +441,23 @@ __device__ __forceinline__ float batch_dist(const float *__restrict__ base, uint
         float4 x[G];
 #pragma unroll
         for (int g = 0; g < G; g++) x[g] = __ldg(row[g] + k);
+        if (dot) {
 #pragma unroll
-        for (int g = 0; g < G; g++) part[g] += group4(x[g], qk);
+          for (int g = 0; g < G; g++) {
+            part[g] = fmaf(x[g].x, qk.x, part[g]);
+            part[g] = fmaf(x[g].y, qk.y, part[g]);
+            part[g] = fmaf(x[g].z, qk.z, part[g]);
+            part[g] = fmaf(x[g].w, qk.w, part[g]);
+          }
+        } else {
+#pragma unroll
+          for (int g = 0; g < G; g++) part[g] += group4(x[g], qk);
+        }
       }
-      // transpose-reduce the 8 rows over the warp (10 shuffles, not 40):
-      // lanes exchange halves at distances 16, 8, 4 so that each lane keeps
-      // one row, then finish over distances 2, 1.  Lane l ends with row
-      // 4*bit4(l) + 2*bit3(l) + bit2(l).  (Integer sums: any order is exact.)
+      // transpose-reduce the 8 rows' dot products over the warp (10
+      // shuffles, not 40): lanes exchange halves at distances 16, 8, 4 so
+      // that each lane keeps one row, then finish over distances 2, 1.  Lane
+      // l ends with row 4*bit4(l) + 2*bit3(l) + bit2(l).
       const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
       float w[4];
 #pragma unroll
@@ -461,7 +477,7 @@ __device__ __forceinline__ float batch_dist(const float *__restrict__ base, uint
       // lane c0 + g takes row g from a lane that holds it
       const int g = (lane - c0) & 7;
       const float t = __shfl_sync(FULL, y, ((g >> 2) << 4) | (((g >> 1) & 1) << 3) | ((g & 1) << 2));
-      if (lane >= c0 && lane < c0 + G) out = t;
+      if (lane >= c0 && lane < c0 + G) out = dot ? qn + xn - 2.f * t : t;
     }
   } else if (lane < cnt) {
     const float4 *row = reinterpret_cast<const float4 *>(base + (size_t)my * d);
@@ -473,9 +489,14 @@ __device__ __forceinline__ float batch_dist(const float *__restrict__ base, uint
 }
 
 __device__ __forceinline__ float cand_dist(const SearchArgs &a, bool ints, uint32_t my, int cnt, const float *qv,
-                                           int lane) {
-  if (a.storage != 0) return lowp_rows_dist(LowpRows{a.qbase, a.qscale, a.storage, a.d}, my, cnt, qv, lane);
-  return ints ? batch_dist<true>(a.base, a.d, my, cnt, qv, lane) : batch_dist<false>(a.base, a.d, my, cnt, qv, lane);
+                                           int lane, float qn) {
+  if (a.storage != 0)
+    // the norm form unless integer data at d > 128 (where only the
+    // difference form stays exact)
+    return lowp_rows_dist(LowpRows{a.qbase, a.qscale, (ints && a.d > 128) ? nullptr : a.qnorm, a.storage, a.d}, my,
+                          cnt, qv, qn, lane);
+  return ints ? batch_dist<true>(a.base, a.d, my, cnt, qv, lane, qn, a.d <= 128 ? a.xnorm : nullptr)
+              : batch_dist<false>(a.base, a.d, my, cnt, qv, lane);
 }
 
 // BUILD = false: SearchEntry* + ROUTER_GREEDY (seeds not marked visited,
@@ -516,11 +537,14 @@ __global__ void __maxnreg__(96) k_search(SearchArgs a) {
     }
     const float *qsrc = a.queries + (size_t)q * a.d;
     bool qint = true;
+    float qn = 0.f;  // |q|^2 (exact on integer data)
     for (uint32_t i = lane; i < a.d; i += 32) {
       const float v = qsrc[i];
       s.qv[i] = v;
+      qn = fmaf(v, v, qn);
       qint &= v >= 0.f && v <= 255.f && v == rintf(v);
     }
+    for (int o = 16; o > 0; o >>= 1) qn += __shfl_xor_sync(FULL, qn, o);
     // integer base and query: any summation order gives the reference's value
     const bool ints = a.int_exact && a.d <= 256 && __all_sync(FULL, qint);
     // ---- seeds (SearchEntryInner): distances in drawn order, as (dist, id)
@@ -537,7 +561,7 @@ __global__ void __maxnreg__(96) k_search(SearchArgs a) {
         set_err(a.status, DEV_BAD_ID);
         id = 0;
       }
-      const float dist = cand_dist(a, ints, id, cnt, s.qv, lane);
+      const float dist = cand_dist(a, ints, id, cnt, s.qv, lane, qn);
       if (lane < cnt) {
         drawn[b + lane] = DI{dist, id};
         if (BUILD && nvis + lane < a.vlimit) vis_out[nvis + lane] = DI{dist, id};
@@ -620,7 +644,7 @@ __global__ void __maxnreg__(96) k_search(SearchArgs a) {
         const int cnt = (int)min(32u, nfresh - b);
         const uint32_t raw = lane < cnt ? s.si[b + lane] : 0u;
         const uint32_t my = raw & ID_MASK;
-        const float dist = cand_dist(a, ints, my, cnt, s.qv, lane);
+        const float dist = cand_dist(a, ints, my, cnt, s.qv, lane, qn);
         if (BUILD) {
           if (lane < cnt && nvis + lane < a.vlimit) vis_out[nvis + lane] = DI{dist, my};
           nvis += cnt;
@@ -711,7 +735,7 @@ __global__ void __maxnreg__(96) k_search(SearchArgs a) {
       for (int b = 0; b < R; b += 32) {
         const int cnt = min(32, R - b);
         const uint32_t id = lane < cnt ? (pi[b + lane] & ID_MASK) : 0u;
-        const float ex = ints ? batch_dist<true>(a.base, a.d, id, cnt, s.qv, lane)
+        const float ex = ints ? batch_dist<true>(a.base, a.d, id, cnt, s.qv, lane, qn, a.d <= 128 ? a.xnorm : nullptr)
                               : batch_dist<false>(a.base, a.d, id, cnt, s.qv, lane);
         if (lane < cnt) {
           xd[b + lane] = ex;

@@ -42,6 +42,7 @@ struct SearchArgs {
   // every base value is an integer in [0, 255]: queries that are too get
   // their distances by a warp reduction (exact in any order)
   int int_exact;
+  const float *xnorm;  // squared norms of the base rows (set when int_exact)
   // candidate distances from a low-precision copy of the base (0: the FP32
   // base; 1: bf16 rows; 2: fp8 e4m3 rows with a per-row FP32 scale), FP32
   // accumulation; the first `rerank` pool entries are then re-scored exactly
@@ -49,6 +50,7 @@ struct SearchArgs {
   int storage;
   const void *qbase;
   const float *qscale;
+  const float *qnorm;  // squared norms of the low-precision rows
   uint32_t rerank;
 };
 
