@@ -41,6 +41,9 @@ CFG = dict(n=1_000_000, d=128, centers=256, nq=10_000, seed=7, S=20, K=64, L=80,
            L_grid=[16, 24, 32, 48, 64, 96, 128, 160, 192, 256, 320, 384, 448, 512, 640, 768, 896, 1024, 1280,
                    1536])
 METRIC = "QPS at recall@10>=0.95 (learned+BF16 vs plain FP32, 1 GB300); build sec"
+# DRAM bytes (read + write) of one learned-plan search launch on the 1M x 128
+# workload, from an ncu capture of this command (profiles/)
+TRAFFIC_LEARNED_1M = 3089417984 + 4369664
 
 
 def log(*a):
@@ -392,7 +395,9 @@ def run_ours(args):
         alg = ldc * d * 2 + lhc * (avg_deg * 4 + 4) + nq * d * 4
         l_achieved = alg / (learned["search_kernel_ms"] / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": round(l_achieved, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(l_achieved / hbm, 4), "traffic": None, "peak_kind": peak_kind,
+                "frac": round(l_achieved / hbm, 4), "traffic": TRAFFIC_LEARNED_1M if cfg["n"] == 1_000_000 else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this launch, "
+                                  "profiles/dram_k_search_learned_1M.md", "peak_kind": peak_kind,
                 "alg_bytes_per_launch": int(alg), "dist_count": ldc, "hop_count": lhc,
                 "kernel": "k_search (learned seeds, per-query L, bf16 candidate rows)",
                 "kernel_ms": round(learned["search_kernel_ms"], 4),
