@@ -218,6 +218,29 @@ int wv_draw_seeds(wv_ctx *ctx, uint32_t nq, int entry, uint32_t L, uint32_t *see
  * GenRandom draws on the device; asynchronous on the context's stream. */
 int wv_draw_seeds_device(wv_ctx *ctx, uint32_t nq, uint32_t L, uint32_t *d_seeds, uint32_t stride);
 
+/* ---- graph files and index statistics ------------------------------------ */
+/* The per-node graph file of IndexBuilder::save_graph / load_graph
+ * (src/builder.cpp:918-1089): [entry point u32 (NSG, Vamana)] then, per node,
+ * its degree and ids (u32 each).  Save writes the built graph
+ * (final_graph_); load reads into the search graph (load_graph_) and must
+ * hold exactly n rows for the uploaded base. */
+int wv_save_graph(wv_ctx *ctx, const char *path, int with_ep);
+int wv_load_graph(wv_ctx *ctx, const char *path, int with_ep);
+/* IndexBuilder::print_index_info (builder.cpp:501-600, 714-780) on the search
+ * graph: out-degree statistics, conn (depth-first traversals from the entry
+ * point -- or node 0 when use_ep is 0 -- restarting at the smallest unreached
+ * id, until every node is reached) and, given an exact KNN graph (n rows of
+ * exact_width ids, exact_deg valid), the mean share of each node's first 10
+ * exact neighbours in its row (-1 when no exact graph is given). */
+typedef struct {
+  uint32_t max_out, min_out;
+  double avg_out;
+  uint32_t conn;
+  double quality;
+} wv_index_stats;
+int wv_index_info(wv_ctx *ctx, int use_ep, const uint32_t *exact_ids, const uint32_t *exact_deg,
+                  uint32_t exact_width, wv_index_stats *out);
+
 /* ---- batched search plans (CUDA graphs, tuned launch shape) -------------- */
 /* No counterpart in the reference (IndexBuilder::search loops over queries,
  * src/builder.cpp:445-454).  A plan binds one batch layout to caller-owned

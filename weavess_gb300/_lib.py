@@ -51,6 +51,11 @@ class TuneReport(C.Structure):
     _fields_ = [("n", C.c_int), ("chosen", C.c_int), ("tried", PlanShape * 32)]
 
 
+class IndexInfo(C.Structure):
+    _fields_ = [("max_out", C.c_uint32), ("min_out", C.c_uint32), ("avg_out", C.c_double), ("conn", C.c_uint32),
+                ("quality", C.c_double)]
+
+
 class LearnReport(C.Structure):
     _fields_ = [("loss_ce", C.c_float), ("loss_mse", C.c_float), ("margin", C.c_float),
                 ("val_agreement", C.c_float), ("ms", C.c_float), ("mean_label_L", C.c_float),
@@ -131,6 +136,9 @@ def load(build_if_needed: bool = True):
                                 u16p, C.c_longlong, C.c_longlong, f32p]
     L.wv_search_noalloc.argtypes = [vp, C.c_uint32, C.c_uint32, vp, vp, C.c_uint32, vp, C.c_uint32, vp, C.c_uint32,
                                     C.c_uint32, vp, vp, vp]
+    L.wv_save_graph.argtypes = [vp, C.c_char_p, C.c_int]
+    L.wv_load_graph.argtypes = [vp, C.c_char_p, C.c_int]
+    L.wv_index_info.argtypes = [vp, C.c_int, vp, vp, C.c_uint32, C.POINTER(IndexInfo)]
     L.wv_plan_create.argtypes = [vp, C.POINTER(PlanParams), vp, vp, vp, vp, vp, vp, C.POINTER(vp)]
     L.wv_plan_run.argtypes = [vp, C.c_uint32]
     L.wv_plan_wait.argtypes = [vp, C.POINTER(Counters)]

@@ -43,6 +43,19 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // One group of four in WEAVESS's distance order (distance.h:20-25):
 // ((d0*d0 + d1*d1) + d2*d2) + d3*d3, every operation rounded separately
 // (no FMA), so the FP32 result equals the reference's for any input.
+// packed FP32 (two independent round-to-nearest FMAs per instruction):
+// acc.{lo,hi} += a.{0,1} * b.{0,1}
+__device__ __forceinline__ void fma2(unsigned long long &acc, float a0, float a1, float b0, float b1) {
+  asm("{\n .reg .b64 pa, pb;\n mov.b64 pa, {%1, %2};\n mov.b64 pb, {%3, %4};\n fma.rn.f32x2 %0, pa, pb, %0;\n}"
+      : "+l"(acc)
+      : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
+}
+__device__ __forceinline__ float sum2(unsigned long long acc) {
+  float lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(acc));
+  return lo + hi;
+}
+
 __device__ __forceinline__ float group4(float4 a, float4 b) {
   float d0 = __fsub_rn(a.x, b.x), d1 = __fsub_rn(a.y, b.y), d2 = __fsub_rn(a.z, b.z), d3 = __fsub_rn(a.w, b.w);
   float s = __fadd_rn(__fmul_rn(d0, d0), __fmul_rn(d1, d1));

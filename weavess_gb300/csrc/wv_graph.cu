@@ -1,0 +1,234 @@
+// Graph files and index statistics.
+//
+// Files: the per-node form of IndexBuilder::save_graph / load_graph
+// (src/builder.cpp:918-1089, the branch every KNN-graph index falls through
+// to, and INDEX_EXACT_KNNG): an optional entry point (one u32, NSG and
+// Vamana), then for every node its degree GK (u32) and GK ids (u32), native
+// byte order.  Byte-compatible with the reference in both directions.
+//
+// Statistics: IndexBuilder::print_index_info (builder.cpp:501-600, 714-780)
+//  * degree: max / min / mean out-degree;
+//  * conn: the number of depth-first traversals needed to reach every node,
+//    starting at the entry point (or node 0) and restarting at the smallest
+//    unreached id.  A traversal's reach does not depend on its order, so the
+//    GPU runs it as a level-synchronous BFS (frontier kernels) and counts the
+//    same restarts;
+//  * quality: the mean, over nodes, of the share of the node's first 10 exact
+//    neighbours (itself skipped) found in its row, the share taken over
+//    min(10, degree, exact-list length) as the reference divides.
+#include <algorithm>
+#include <cstdio>
+#include <utility>
+#include <vector>
+
+#include "wv_common.cuh"
+#include "wv_ctx.h"
+
+using namespace wv;
+
+namespace {
+
+__global__ void k_bfs_level(const uint32_t *ids, const uint32_t *deg, uint32_t w, uint32_t n, const uint32_t *front,
+                            uint32_t nfront, uint32_t *bits, uint32_t *next, uint32_t *nnext, int *status) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t f = wid; f < nfront; f += nw) {
+    const uint32_t u = front[f];
+    uint32_t dg = deg[u];
+    if (dg > w) {
+      if (lane == 0) set_err(status, DEV_BAD_ID);
+      dg = w;
+    }
+    for (uint32_t j = lane; j < dg; j += 32) {
+      const uint32_t v = ids[(size_t)u * w + j];
+      if (v >= n) {
+        set_err(status, DEV_BAD_ID);
+        continue;
+      }
+      const uint32_t bit = 1u << (v & 31);
+      if (!(atomicOr(bits + (v >> 5), bit) & bit)) next[atomicAdd(nnext, 1u)] = v;
+    }
+  }
+}
+
+// first node id whose bit is clear (n if none): one block
+__global__ void k_first_unreached(const uint32_t *bits, uint32_t n, uint32_t *out) {
+  __shared__ uint32_t best;
+  if (threadIdx.x == 0) best = n;
+  __syncthreads();
+  const uint32_t words = (n + 31) / 32;
+  for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) {
+    uint32_t free = ~bits[i];
+    if (i == words - 1 && (n & 31)) free &= (1u << (n & 31)) - 1u;
+    if (free) atomicMin(&best, i * 32 + (uint32_t)(__ffs(free) - 1));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *out = best;
+}
+
+// per node: share of its first 10 exact neighbours (itself skipped) in its row
+__global__ void k_quality(const uint32_t *ids, const uint32_t *deg, uint32_t w, const uint32_t *ex,
+                          const uint32_t *exdeg, uint32_t ew, uint32_t n, float *q) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = wid; i < n; i += nw) {
+    const uint32_t *v = ex + (size_t)i * ew;
+    uint32_t vl = min(exdeg[i], ew);
+    uint32_t v0 = 0;
+    if (vl > 0 && v[0] == i) {
+      v0 = 1;
+      vl--;
+    }
+    const uint32_t dg = min(deg[i], w);
+    uint32_t hits = 0;
+    for (uint32_t j = 0; j < 10 && j < vl; j++) {
+      const uint32_t target = v[v0 + j];
+      bool found = false;
+      for (uint32_t k = lane; k < dg && !found; k += 32) found = ids[(size_t)i * w + k] == target;
+      hits += __any_sync(FULL, found) ? 1u : 0u;
+    }
+    if (lane == 0) {
+      const uint32_t den = min(min(10u, dg), vl);
+      q[i] = den ? (float)hits / (float)den : __int_as_float(0x7fc00000);  // 0/0 as the reference's float division
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int wv_save_graph(wv_ctx *c, const char *path, int with_ep) {
+  if (!c || !path) return WV_ERR_ARG;
+  WV_CHECK(c, c->fg_n > 0, WV_ERR_STATE, "no built graph");
+  const size_t n = c->fg_n, w = c->fg_w;
+  std::vector<uint32_t> ids(n * w), deg(n);
+  WV_CUDA(c, cudaSetDevice(c->device));
+  WV_CUDA(c, cudaMemcpyAsync(ids.data(), c->fg_ids.p, n * w * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaMemcpyAsync(deg.data(), c->fg_deg.p, n * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  FILE *f = fopen(path, "wb");
+  WV_CHECK(c, f, WV_ERR_ARG, "cannot open %s for writing", path);
+  bool ok = true;
+  if (with_ep) ok = fwrite(&c->fg_ep, 4, 1, f) == 1;
+  for (size_t i = 0; i < n && ok; i++) {
+    const uint32_t gk = deg[i] <= w ? deg[i] : (uint32_t)w;
+    ok = fwrite(&gk, 4, 1, f) == 1 && fwrite(ids.data() + i * w, 4, gk, f) == gk;
+  }
+  ok = (fclose(f) == 0) && ok;
+  WV_CHECK(c, ok, WV_ERR_ARG, "writing %s failed", path);
+  return WV_OK;
+}
+
+int wv_load_graph(wv_ctx *c, const char *path, int with_ep) {
+  if (!c || !path) return WV_ERR_ARG;
+  WV_CHECK(c, c->n > 0, WV_ERR_STATE, "upload the base first (the graph's node count must match it)");
+  FILE *f = fopen(path, "rb");
+  WV_CHECK(c, f, WV_ERR_ARG, "cannot open %s", path);
+  uint32_t ep = 0;
+  if (with_ep && fread(&ep, 4, 1, f) != 1) {
+    fclose(f);
+    return fail(c, WV_ERR_ARG, "%s: no entry point", path);
+  }
+  std::vector<std::vector<uint32_t>> rows;
+  uint32_t w = 0;
+  for (;;) {
+    uint32_t gk;
+    if (fread(&gk, 4, 1, f) != 1) break;  // end of file, as the reference's loop
+    std::vector<uint32_t> r(gk);
+    if (gk && fread(r.data(), 4, gk, f) != gk) {
+      fclose(f);
+      return fail(c, WV_ERR_ARG, "%s: truncated row %zu", path, rows.size());
+    }
+    w = gk > w ? gk : w;
+    rows.push_back(std::move(r));
+  }
+  fclose(f);
+  WV_CHECK(c, rows.size() == c->n, WV_ERR_ARG, "%s holds %zu rows, the base %u", path, rows.size(), c->n);
+  w = w ? w : 1;
+  std::vector<uint32_t> ids((size_t)c->n * w, 0u), deg(c->n);
+  for (size_t i = 0; i < rows.size(); i++) {
+    deg[i] = (uint32_t)rows[i].size();
+    for (size_t j = 0; j < rows[i].size(); j++) ids[i * w + j] = rows[i][j];
+  }
+  return wv_upload_graph(c, ids.data(), deg.data(), c->n, w, with_ep ? ep : 0);
+}
+
+int wv_index_info(wv_ctx *c, int use_ep, const uint32_t *exact_ids, const uint32_t *exact_deg, uint32_t exact_width,
+                  wv_index_stats *out) {
+  if (!c || !out) return WV_ERR_ARG;
+  WV_CHECK(c, c->gn == c->n && c->n > 0, WV_ERR_STATE, "no search graph");
+  WV_CUDA(c, cudaSetDevice(c->device));
+  const uint32_t n = c->n, w = c->gw;
+  std::vector<uint32_t> deg(n);
+  WV_CUDA(c, cudaMemcpyAsync(deg.data(), c->gdeg.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  wv_index_stats r{};
+  r.min_out = 1000000u;
+  double sum = 0.0;
+  for (uint32_t i = 0; i < n; i++) {
+    r.max_out = deg[i] > r.max_out ? deg[i] : r.max_out;
+    r.min_out = deg[i] < r.min_out ? deg[i] : r.min_out;
+    sum += deg[i];
+  }
+  r.avg_out = sum / n;
+  // connectivity: BFS reach from the root, restarts at the smallest unreached id
+  cudaError_t e = cudaSuccess;
+  uint32_t *bits = c->buf<uint32_t>("gi_bits", (n + 31) / 32, &e);
+  uint32_t *fa = c->buf<uint32_t>("gi_fa", n, &e);
+  uint32_t *fb = c->buf<uint32_t>("gi_fb", n, &e);
+  uint32_t *cnt = c->buf<uint32_t>("gi_cnt", 4, &e);
+  WV_CUDA(c, e);
+  WV_CUDA(c, cudaMemsetAsync(bits, 0, (size_t)(n + 31) / 32 * 4, c->stream));
+  uint32_t root = use_ep ? c->ep : 0u, conn = 0;
+  WV_CHECK(c, root < n, WV_ERR_ARG, "entry point %u >= n", root);
+  for (;;) {
+    conn++;
+    const uint32_t word = root >> 5, bit = 1u << (root & 31);
+    uint32_t wv_ = 0;
+    WV_CUDA(c, cudaMemcpyAsync(&wv_, bits + word, 4, cudaMemcpyDeviceToHost, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    wv_ |= bit;
+    WV_CUDA(c, cudaMemcpyAsync(bits + word, &wv_, 4, cudaMemcpyHostToDevice, c->stream));
+    WV_CUDA(c, cudaMemcpyAsync(fa, &root, 4, cudaMemcpyHostToDevice, c->stream));
+    uint32_t nf = 1;
+    while (nf) {
+      WV_CUDA(c, cudaMemsetAsync(cnt, 0, 4, c->stream));
+      const uint32_t blocks = std::min<uint32_t>((nf + 7) / 8, (uint32_t)c->sms * 32);
+      k_bfs_level<<<blocks, 256, 0, c->stream>>>(c->gids.as<uint32_t>(), c->gdeg.as<uint32_t>(), w, n, fa, nf, bits, fb,
+                                                cnt, c->d_status());
+      WV_CUDA(c, cudaGetLastError());
+      WV_CUDA(c, cudaMemcpyAsync(&nf, cnt, 4, cudaMemcpyDeviceToHost, c->stream));
+      WV_CUDA(c, cudaStreamSynchronize(c->stream));
+      std::swap(fa, fb);
+    }
+    k_first_unreached<<<1, 1024, 0, c->stream>>>(bits, n, cnt);
+    WV_CUDA(c, cudaGetLastError());
+    WV_CUDA(c, cudaMemcpyAsync(&root, cnt, 4, cudaMemcpyDeviceToHost, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (root >= n) break;
+  }
+  r.conn = conn;
+  r.quality = -1.0;
+  if (exact_ids && exact_deg && exact_width) {
+    uint32_t *dex = c->buf<uint32_t>("gi_ex", (size_t)n * exact_width, &e);
+    uint32_t *dexd = c->buf<uint32_t>("gi_exd", n, &e);
+    float *q = c->buf<float>("gi_q", n, &e);
+    WV_CUDA(c, e);
+    WV_CUDA(c, cudaMemcpyAsync(dex, exact_ids, (size_t)n * exact_width * 4, cudaMemcpyHostToDevice, c->stream));
+    WV_CUDA(c, cudaMemcpyAsync(dexd, exact_deg, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+    k_quality<<<c->sms * 8, 256, 0, c->stream>>>(c->gids.as<uint32_t>(), c->gdeg.as<uint32_t>(), w, dex, dexd,
+                                                 exact_width, n, q);
+    WV_CUDA(c, cudaGetLastError());
+    std::vector<float> hq(n);
+    WV_CUDA(c, cudaMemcpyAsync(hq.data(), q, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    double s = 0.0;
+    for (float x : hq) s += x;
+    r.quality = s / n;
+  }
+  *out = r;
+  return check_device_status(c, "index info");
+}
+
+}  // extern "C"

@@ -160,6 +160,14 @@ __global__ void k_adam(float *p, const float *g, float *m, float *v, size_t coun
   p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
+// out (cols x rows) = x (rows x cols)^T, rounded to bf16
+__global__ void k_transpose_bf16(const float *x, uint32_t rows, uint32_t cols, __nv_bfloat16 *out) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)rows * cols) return;
+  const uint32_t r = (uint32_t)(i / cols), cc = (uint32_t)(i % cols);
+  out[(size_t)cc * rows + r] = __float2bfloat16_rn(x[i]);
+}
+
 __global__ void k_to_bf16(const float *x, size_t count, __nv_bfloat16 *out) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i < count) out[i] = __float2bfloat16_rn(x[i]);
@@ -248,6 +256,8 @@ struct LearnState {
   // parameter block (FP32 master): W1 D x H, b1 H, W2 H x H, b2 H, W3 H x (C+1), b3 C+1
   size_t oW1, ob1, oW2, ob2, oW3, ob3, np;
   DevBuf P, G, M, V, Pb;  // Pb: bf16 copies of the weights (same offsets)
+  DevBuf PbT;             // bf16 weights transposed (out x in per layer, same offsets): the forward pass's B
+                          // operand with K contiguous
   DevBuf mu, sg;
   DevBuf lists, llen, cent;
   std::vector<uint32_t> h_entry;
@@ -280,7 +290,8 @@ struct LearnState {
 void learn_free(wv_ctx *c) {
   if (!c->learn) return;
   LearnState *L = static_cast<LearnState *>(c->learn);
-  for (DevBuf *b : {&L->P, &L->G, &L->M, &L->V, &L->Pb, &L->mu, &L->sg, &L->lists, &L->llen, &L->cent}) b->release();
+  for (DevBuf *b : {&L->P, &L->G, &L->M, &L->V, &L->Pb, &L->PbT, &L->mu, &L->sg, &L->lists, &L->llen, &L->cent})
+    b->release();
   delete L;
   c->learn = nullptr;
 }
@@ -344,12 +355,14 @@ inline unsigned nblk(size_t n, unsigned t = 256) { return (unsigned)((n + t - 1)
 // forward pass of B rows of x (rows: optional gather list); O = outputs
 int forward(wv_ctx *c, LearnState &S, const float *x, const uint32_t *rows, uint32_t B, Work &w) {
   const float *P = S.P.as<float>();
-  const __nv_bfloat16 *Pb = S.Pb.as<__nv_bfloat16>();
+  const __nv_bfloat16 *Pt = S.PbT.as<__nv_bfloat16>();  // W^T: B(k, n) = Pt[n * K + k]
   k_gather_norm<<<nblk((size_t)B * S.D), 256, 0, c->stream>>>(x, rows, B, S.D, S.mu.as<float>(), S.sg.as<float>(),
                                                               w.Xb);
-  WV_CUDA(c, gemm_bf16_umma(gm(w.Xb, S.D, 1, Pb + S.oW1, HID, 1, w.H1, w.H1b, HID, P + S.ob1, 1, B, HID, S.D), c->d_status(), c->stream));
-  WV_CUDA(c, gemm_bf16_umma(gm(w.H1b, HID, 1, Pb + S.oW2, HID, 1, w.H2, w.H2b, HID, P + S.ob2, 1, B, HID, HID), c->d_status(), c->stream));
-  WV_CUDA(c, gemm_bf16_umma(gm(w.H2b, HID, 1, Pb + S.oW3, S.C + 1, 1, w.O, nullptr, S.C + 1, P + S.ob3, 0, B, S.C + 1, HID),
+  WV_CUDA(c, gemm_bf16_umma(gm(w.Xb, S.D, 1, Pt + S.oW1, 1, S.D, w.H1, w.H1b, HID, P + S.ob1, 1, B, HID, S.D),
+                            c->d_status(), c->stream));
+  WV_CUDA(c, gemm_bf16_umma(gm(w.H1b, HID, 1, Pt + S.oW2, 1, HID, w.H2, w.H2b, HID, P + S.ob2, 1, B, HID, HID),
+                            c->d_status(), c->stream));
+  WV_CUDA(c, gemm_bf16_umma(gm(w.H2b, HID, 1, Pt + S.oW3, 1, HID, w.O, nullptr, S.C + 1, P + S.ob3, 0, B, S.C + 1, HID),
                             c->d_status(), c->stream));
   return WV_OK;
 }
@@ -381,6 +394,15 @@ int backward(wv_ctx *c, LearnState &S, const uint32_t *yc, const float *yr, cons
 int refresh_bf16(wv_ctx *c, LearnState &S) {
   k_to_bf16<<<nblk(S.np), 256, 0, c->stream>>>(S.P.as<float>(), S.np, S.Pb.as<__nv_bfloat16>());
   WV_CUDA(c, cudaGetLastError());
+  const float *P = S.P.as<float>();
+  __nv_bfloat16 *T = S.PbT.as<__nv_bfloat16>();
+  const size_t offs[3] = {S.oW1, S.oW2, S.oW3};
+  const uint32_t rows[3] = {S.D, HID, HID}, cols[3] = {HID, HID, S.C + 1};
+  for (int l = 0; l < 3; l++) {
+    k_transpose_bf16<<<nblk((size_t)rows[l] * cols[l]), 256, 0, c->stream>>>(P + offs[l], rows[l], cols[l],
+                                                                             T + offs[l]);
+    WV_CUDA(c, cudaGetLastError());
+  }
   return WV_OK;
 }
 
@@ -390,6 +412,7 @@ int ensure_params(wv_ctx *c, LearnState &S) {
   WV_CUDA(c, S.M.ensure(S.np * 4));
   WV_CUDA(c, S.V.ensure(S.np * 4));
   WV_CUDA(c, S.Pb.ensure(S.np * 2));
+  WV_CUDA(c, S.PbT.ensure(S.np * 2));
   return WV_OK;
 }
 

@@ -114,6 +114,8 @@ __device__ __forceinline__ float rows_dist(const LowpRows &b, uint32_t my, int c
   const uint32_t ch = rb / CB;
   const int sub = lane & (G - 1), grp = lane / G;
   const uint8_t *base = reinterpret_cast<const uint8_t *>(b.rows);
+  const float xn = (DOT && lane < cnt) ? __ldg(b.norm + my) : 0.f;
+  const float xs = (DOT && ST == 2 && lane < cnt) ? __ldg(b.scale + my) : 1.f;
   float out = 0.f;
   for (int p0 = 0; p0 * RPP < cnt; p0 += U) {
     float part[U], sc[U];
@@ -128,7 +130,7 @@ __device__ __forceinline__ float rows_dist(const LowpRows &b, uint32_t my, int c
       // dead rows read row 0 (in bounds) and are ignored: no branch keeps the
       // U loads from issuing together
       row[u] = base + (size_t)(live[u] ? id : 0u) * rb;
-      sc[u] = ST == 2 ? __ldg(b.scale + (live[u] ? id : 0u)) : 1.f;
+      sc[u] = (ST == 2 && !DOT) ? __ldg(b.scale + (live[u] ? id : 0u)) : 1.f;
     }
     // chunk-major: all U rows' loads of one step are issued before any math
     for (uint32_t k = sub; k < ch; k += G) {
@@ -148,12 +150,24 @@ __device__ __forceinline__ float rows_dist(const LowpRows &b, uint32_t my, int c
       if (lane / RPP == p0 + u) out = t;
     }
   }
-  if (DOT && lane < cnt) {
-    // |q|^2 + |x|^2 - 2 q.x with the stored row's norm (fp8: q.x = scale * q.h)
-    const float s2 = ST == 2 ? 2.f * __ldg(b.scale + my) : 2.f;
-    out = fmaxf(qn + __ldg(b.norm + my) - s2 * out, 0.f);
-  }
+  // |q|^2 + |x|^2 - 2 q.x with the stored row's norm (fp8: q.x = scale * q.h)
+  if (DOT && lane < cnt) out = fmaxf(qn + xn - 2.f * xs * out, 0.f);
   return out;
+}
+
+// the dot product of one loaded bf16 chunk with the query, added to a packed
+// pair of accumulators (two values per FMA instruction)
+template <int CB>
+__device__ __forceinline__ void chunk_dot2_bf16(const Chunk<CB> &c, const float *qv, uint32_t e0,
+                                                unsigned long long &acc) {
+  const float4 *q4 = reinterpret_cast<const float4 *>(qv + e0);
+#pragma unroll
+  for (int j = 0; j < CB / 8; j++) {
+    const float4 q = q4[j];
+    const uint32_t w0 = c.w[2 * j], w1 = c.w[2 * j + 1];
+    fma2(acc, q.x, q.y, __uint_as_float(w0 << 16), __uint_as_float(w0 & 0xffff0000u));
+    fma2(acc, q.z, q.w, __uint_as_float(w1 << 16), __uint_as_float(w1 & 0xffff0000u));
+  }
 }
 
 // a warp per row (rows of at least 24 chunks): 8 rows per batch, their loads
@@ -167,6 +181,9 @@ __device__ __forceinline__ float rows_dist_w(const LowpRows &b, uint32_t my, int
   const uint32_t rb = ST == 1 ? b.d * 2 : b.d;
   const uint32_t ch = rb / CB;
   const uint8_t *base = reinterpret_cast<const uint8_t *>(b.rows);
+  // the lane's own row norm (and fp8 scale), loaded before the rows
+  const float xn = (DOT && lane < cnt) ? __ldg(b.norm + my) : 0.f;
+  const float xs = (DOT && ST == 2 && lane < cnt) ? __ldg(b.scale + my) : 1.f;
   float out = 0.f;
   for (int c0 = 0; c0 < cnt; c0 += 8) {
     float part[8], sc[8];
@@ -180,12 +197,24 @@ __device__ __forceinline__ float rows_dist_w(const LowpRows &b, uint32_t my, int
       row[g] = base + (size_t)(live ? id : 0u) * rb;  // dead rows read row 0 (in bounds), ignored
       sc[g] = (ST == 2 && !DOT) ? __ldg(b.scale + (live ? id : 0u)) : 1.f;
     }
+    unsigned long long pacc[8];  // bf16 dot form: packed accumulators
+#pragma unroll
+    for (int g = 0; g < 8; g++) pacc[g] = 0ull;
     for (uint32_t k = lane; k < ch; k += 32) {
       Chunk<CB> c[8];
 #pragma unroll
       for (int g = 0; g < 8; g++) c[g] = load_chunk<CB>(row[g] + (size_t)k * CB);
+      if (ST == 1 && DOT && CB >= 8) {
 #pragma unroll
-      for (int g = 0; g < 8; g++) part[g] += chunk_sq<ST, CB, DOT>(c[g], qv, k * EPC, sc[g]);
+        for (int g = 0; g < 8; g++) chunk_dot2_bf16<CB>(c[g], qv, k * EPC, pacc[g]);
+      } else {
+#pragma unroll
+        for (int g = 0; g < 8; g++) part[g] += chunk_sq<ST, CB, DOT>(c[g], qv, k * EPC, sc[g]);
+      }
+    }
+    if (ST == 1 && DOT && CB >= 8) {
+#pragma unroll
+      for (int g = 0; g < 8; g++) part[g] = sum2(pacc[g]);
     }
     const bool b16 = lane & 16, b8 = lane & 8, b4 = lane & 4;
     float w[4];
@@ -207,10 +236,7 @@ __device__ __forceinline__ float rows_dist_w(const LowpRows &b, uint32_t my, int
     const float t = __shfl_sync(FULL, y, ((g >> 2) << 4) | (((g >> 1) & 1) << 3) | ((g & 1) << 2));
     if (lane >= c0 && lane < c0 + 8) out = t;
   }
-  if (DOT && lane < cnt) {
-    const float s2 = ST == 2 ? 2.f * __ldg(b.scale + my) : 2.f;
-    out = fmaxf(qn + __ldg(b.norm + my) - s2 * out, 0.f);
-  }
+  if (DOT && lane < cnt) out = fmaxf(qn + xn - 2.f * xs * out, 0.f);
   return out;
 }
 

@@ -425,12 +425,14 @@ __device__ __forceinline__ float batch_dist(const float *__restrict__ base, uint
     constexpr int G = 8;
     for (int c0 = 0; c0 < cnt; c0 += G) {
       float part[G];
+      unsigned long long pacc[G];  // packed accumulators of the dot form
       const float4 *row[G];
 #pragma unroll
       for (int g = 0; g < G; g++) {
         const int c = c0 + g;
         const uint32_t id = __shfl_sync(FULL, my, c & 31);
         part[g] = 0.f;
+        pacc[g] = 0ull;
         // rows past cnt read row 0 (in bounds) and are ignored: no branch
         // keeps the G loads from issuing together
         row[g] = reinterpret_cast<const float4 *>(base + (size_t)(c < cnt ? id : 0u) * d);
@@ -442,17 +444,20 @@ __device__ __forceinline__ float batch_dist(const float *__restrict__ base, uint
 #pragma unroll
         for (int g = 0; g < G; g++) x[g] = __ldg(row[g] + k);
         if (dot) {
+          // packed FMAs: two dimensions per instruction (integer sums: exact)
 #pragma unroll
           for (int g = 0; g < G; g++) {
-            part[g] = fmaf(x[g].x, qk.x, part[g]);
-            part[g] = fmaf(x[g].y, qk.y, part[g]);
-            part[g] = fmaf(x[g].z, qk.z, part[g]);
-            part[g] = fmaf(x[g].w, qk.w, part[g]);
+            fma2(pacc[g], x[g].x, x[g].y, qk.x, qk.y);
+            fma2(pacc[g], x[g].z, x[g].w, qk.z, qk.w);
           }
         } else {
 #pragma unroll
           for (int g = 0; g < G; g++) part[g] += group4(x[g], qk);
         }
+      }
+      if (dot) {
+#pragma unroll
+        for (int g = 0; g < G; g++) part[g] = sum2(pacc[g]);
       }
       // transpose-reduce the 8 rows' dot products over the warp (10
       // shuffles, not 40): lanes exchange halves at distances 16, 8, 4 so
@@ -506,7 +511,7 @@ __device__ __forceinline__ float cand_dist(const SearchArgs &a, bool ints, uint3
 //   then each newly visited id in visit order -- is appended to the query's
 //   visit list (vis, vcap apart, vlimit entries kept, count in vcnt).
 template <bool BUILD, int W>
-__global__ void __maxnreg__(96) k_search(SearchArgs a) {
+__global__ void __maxnreg__(128) k_search(SearchArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t wbytes = warp_smem_bytes(a.d, a.Lmax, a.cap, a.hcap);

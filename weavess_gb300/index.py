@@ -217,6 +217,25 @@ class Context:
         self._check(self.L.wv_draw_seeds(self.h, nq, ENTRY[entry], L, out))
         return out
 
+    # -- graph files and statistics (IndexBuilder::save_graph / load_graph / print_index_info)
+    def save_graph(self, path: str, with_ep: bool = False):
+        self._check(self.L.wv_save_graph(self.h, path.encode(), 1 if with_ep else 0))
+
+    def load_graph(self, path: str, with_ep: bool = False):
+        self._check(self.L.wv_load_graph(self.h, path.encode(), 1 if with_ep else 0))
+
+    def index_info(self, use_ep: bool = False, exact_ids=None, exact_deg=None):
+        r = _lib.IndexInfo()
+        if exact_ids is not None:
+            ex = _u32(exact_ids)
+            exd = _u32(exact_deg if exact_deg is not None else np.full(ex.shape[0], ex.shape[1], np.uint32))
+            self._check(self.L.wv_index_info(self.h, 1 if use_ep else 0, ex.ctypes.data, exd.ctypes.data, ex.shape[1],
+                                             C.byref(r)))
+        else:
+            self._check(self.L.wv_index_info(self.h, 1 if use_ep else 0, None, None, 0, C.byref(r)))
+        return {"max_out": r.max_out, "min_out": r.min_out, "avg_out": r.avg_out, "conn": r.conn,
+                "quality": r.quality}
+
     def plan(self, nq_max: int, K_max: int, d_queries: int, d_out_ids: int, L_max: int = 0, mode: str = "rand",
              d_L: int = 0, d_K: int = 0, d_seeds: int = 0, d_out_dist: int = 0, out_stride: int = 0):
         """A captured batch search on device buffers (pointers); see Plan."""
