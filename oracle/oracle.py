@@ -53,6 +53,8 @@ def lib():
                                  C.c_float, C.c_uint, C.c_void_p, C.c_int, u32p, f32p, u32p, u32p]
         L.orc_nsg.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint, C.c_uint, C.c_uint,
                               C.c_void_p, C.c_int, u32p, f32p, u32p, C.c_uint, u32p, u32p]
+        L.orc_ssg.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint, C.c_uint, C.c_float,
+                              C.c_uint, C.c_void_p, u32p, f32p, u32p, C.c_uint, u32p, u32p]
         L.orc_search.argtypes = [f32p, C.c_uint, C.c_uint, f32p, C.c_uint, u32p, u32p, C.c_uint, C.c_uint,
                                  C.c_int, C.c_uint, C.c_uint, C.c_void_p, C.c_int, u32p, u64p]
         L.orc_search_seeds.argtypes = [C.c_uint, C.c_uint, u32p, u32p, C.c_uint, C.c_uint, C.c_int, C.c_uint,
@@ -175,6 +177,25 @@ def nsg(base, g: Graph, L_refine, R_refine, C_refine, rnd: Rand, threads=1, out_
                          g.width, L_refine, R_refine, C_refine, rnd.h, threads, ids, dist, deg, out_w, ep,
                          added) == 0
     out = Graph(ids, dist, deg, int(ep[0]))
+    out.conn_added = int(added[0])
+    return out
+
+
+def ssg(base, g: Graph, L_refine, R_refine, A, n_try, rnd: Rand, out_w=None) -> Graph:
+    """REFINE_SSG: Propagation2 candidates, SSG prune, InterInsert, DFS-expand
+    conn; the returned graph carries `eps` (the n_try roots)."""
+    base = _c(base, np.float32)
+    n, d = base.shape
+    out_w = out_w or R_refine
+    ids = np.zeros((n, out_w), np.uint32)
+    dist = np.zeros((n, out_w), np.float32)
+    deg = np.zeros(n, np.uint32)
+    eps = np.zeros(max(1, n_try), np.uint32)
+    added = np.zeros(1, np.uint32)
+    assert lib().orc_ssg(base, n, d, _c(g.ids, np.uint32), _c(g.dist, np.float32), _c(g.deg, np.uint32), g.width,
+                         L_refine, R_refine, A, n_try, rnd.h, ids, dist, deg, out_w, eps, added) == 0
+    out = Graph(ids, dist, deg, None)
+    out.eps = eps[:n_try].copy()
     out.conn_added = int(added[0])
     return out
 

@@ -8,13 +8,14 @@
 //   Vamana link    src/component_refine.cpp:794-872 (alpha set on the index, as
 //                  the reference has no parameter for it, index.h:213-216)
 //   NSG link       src/component_refine.cpp:393-472
+//   SSG link       src/component_refine.cpp:550-720, component_conn.cpp:169-225
 //   search loop    src/builder.cpp:445-454 (L_SEARCH_ASSIGN, serial), with the
 //                  result ids kept instead of only the recall print.
 // One thread (IndexBuilder(1)), so the glibc rand() stream and every sort are
 // deterministic.
 //
 // usage: ref_driver base.fvecs query.fvecs gt.ivecs outprefix key=val ... -- step ...
-//   steps: init_random | init_rand | nndescent | vamana | nsg | load:<kgraph|vamana|nsg>
+//   steps: init_random | init_rand | nndescent | vamana | nsg | ssg | load:<kgraph|vamana|nsg|ssg>
 //          | search_rand:<L> | search_centroid:<L> | rand_probe
 #include <bits/stdc++.h>
 #include <omp.h>
@@ -101,8 +102,21 @@ int main(int argc, char **argv) {
     } else if (step == "nsg") {
       builder->refine(REFINE_NSG, false);
       write_final_graph(prefix + ".nsg.bin", idx, true);
+    } else if (step == "ssg") {
+      // REFINE_SSG (component_refine.cpp:550-582): Propagation2 candidates,
+      // SSG prune, InterInsert, DFS-expand conn from n_try shuffled roots
+      builder->refine(REFINE_SSG, false);
+      write_final_graph(prefix + ".ssg.bin", idx, false);
+      FILE *f = fopen((prefix + ".ssgeps.bin").c_str(), "wb");
+      unsigned ne = (unsigned)idx->eps_.size();
+      fwrite(&ne, 4, 1, f);
+      fwrite(idx->eps_.data(), 4, ne, f);
+      fclose(f);
     } else if (step == "load") {
-      TYPE t = arg == "kgraph" ? INDEX_KGRAPH : (arg == "vamana" ? INDEX_VAMANA : INDEX_NSG);
+      TYPE t = arg == "kgraph" ? INDEX_KGRAPH
+               : arg == "vamana" ? INDEX_VAMANA
+               : arg == "ssg"    ? INDEX_SSG
+                                 : INDEX_NSG;
       std::string gf = prefix + "." + arg + ".graph";
       builder->save_graph(t, &gf[0]);
       idx->getLoadGraph().clear();

@@ -721,6 +721,206 @@ void conn_dfs(const Data &D, FinalGraph &g, unsigned ep, unsigned Lr, GlibcRand 
 
 }  // namespace
 
+namespace {
+
+// ---------------------------------------------------------------- SSG
+// The angle test of ComponentPruneSSG::PruneInner (component_prune.cpp:96-104)
+// and ComponentRefineSSG::InterInsert (component_refine.cpp:685-693):
+// cos_ij = (p + r - djk) / 2 / sqrt(p * r) with the reference's operand
+// types -- float sums, a float quotient by 2, and the unqualified sqrt of the
+// float product resolving to ::sqrt(double) there -- so the quotient is
+// taken in double and stored to float.
+inline bool ssg_occludes(float pd, float rd, float djk, float threshold) {
+  const float num = (pd + rd - djk) / 2;
+  const float cos_ij = (float)((double)num / std::sqrt((double)(pd * rd)));
+  return cos_ij > threshold;
+}
+
+// float threshold = std::cos((float)A / 180 * kPi) (component_prune.cpp:92-93,
+// component_refine.cpp:640-641): float quotient, double product and cosine
+float ssg_threshold(float A) {
+  const double kPi = std::acos(-1.0);
+  return (float)std::cos(A / 180 * kPi);
+}
+
+// ComponentCandidatePropagation2::CandidateInner (component_candidate.cpp:90-109).
+// The reference takes `flags` by value, so every call starts from a clear copy.
+void candidate_prop2(const Data &D, const FinalGraph &g, unsigned query, unsigned Lr, std::vector<char> &flags,
+                     std::vector<SimpleNeighbor> &pool) {
+  std::fill(flags.begin(), flags.end(), 0);
+  flags[query] = 1;
+  for (unsigned i = 0; i < g[query].size(); i++) {
+    unsigned nid = g[query][i].id;
+    for (unsigned nn = 0; nn < g[nid].size(); nn++) {
+      unsigned nnid = g[nid][nn].id;
+      if (flags[nnid]) continue;
+      flags[nnid] = 1;
+      pool.emplace_back(nnid, l2(D.row(query), D.row(nnid), D.d));
+      if (pool.size() >= Lr) break;
+    }
+    if (pool.size() >= Lr) break;
+  }
+}
+
+// ComponentPruneSSG::PruneInner (component_prune.cpp:71-122); the flags it
+// receives are the caller's clear bitset (a by-value copy), so the node's
+// whole row joins the pool
+void prune_ssg(const Data &D, const FinalGraph &g, unsigned query, unsigned range, float threshold,
+               std::vector<SimpleNeighbor> &pool, SimpleNeighbor *cut_graph) {
+  unsigned start = 0;
+  for (unsigned nn = 0; nn < g[query].size(); nn++) {
+    unsigned id = g[query][nn].id;
+    pool.push_back(SimpleNeighbor(id, l2(D.row(query), D.row(id), D.d)));
+  }
+  std::sort(pool.begin(), pool.end());
+  std::vector<SimpleNeighbor> result;
+  if (pool[start].id == query) start++;
+  result.push_back(pool[start]);
+  while (result.size() < range && (++start) < pool.size()) {
+    auto &p = pool[start];
+    bool occlude = false;
+    for (unsigned t = 0; t < result.size(); t++) {
+      if (p.id == result[t].id) {
+        occlude = true;
+        break;
+      }
+      float djk = l2(D.row(result[t].id), D.row(p.id), D.d);
+      if (ssg_occludes(p.distance, result[t].distance, djk, threshold)) {
+        occlude = true;
+        break;
+      }
+    }
+    if (!occlude) result.push_back(p);
+  }
+  SimpleNeighbor *des_pool = cut_graph + (size_t)query * range;
+  for (size_t t = 0; t < result.size(); t++) des_pool[t] = result[t];
+  if (result.size() < range) des_pool[result.size()].distance = -1;
+}
+
+// ComponentRefineSSG::InterInsert (component_refine.cpp:647-720): NSG's
+// structure with the angle test, and a sentinel after a short re-prune
+void inter_insert_ssg(const Data &D, unsigned n, unsigned range, float threshold, SimpleNeighbor *cut_graph) {
+  SimpleNeighbor *src_pool = cut_graph + (size_t)n * range;
+  for (size_t i = 0; i < range; i++) {
+    if (src_pool[i].distance == -1) break;
+    SimpleNeighbor sn(n, src_pool[i].distance);
+    size_t des = src_pool[i].id;
+    SimpleNeighbor *des_pool = cut_graph + des * range;
+    std::vector<SimpleNeighbor> temp_pool;
+    int dup = 0;
+    for (size_t j = 0; j < range; j++) {
+      if (des_pool[j].distance == -1) break;
+      if (n == des_pool[j].id) {
+        dup = 1;
+        break;
+      }
+      temp_pool.push_back(des_pool[j]);
+    }
+    if (dup) continue;
+    temp_pool.push_back(sn);
+    if (temp_pool.size() > range) {
+      std::vector<SimpleNeighbor> result;
+      unsigned start = 0;
+      std::sort(temp_pool.begin(), temp_pool.end());
+      result.push_back(temp_pool[start]);
+      while (result.size() < range && (++start) < temp_pool.size()) {
+        auto &p = temp_pool[start];
+        bool occlude = false;
+        for (unsigned t = 0; t < result.size(); t++) {
+          if (p.id == result[t].id) {
+            occlude = true;
+            break;
+          }
+          float djk = l2(D.row(result[t].id), D.row(p.id), D.d);
+          if (ssg_occludes(p.distance, result[t].distance, djk, threshold)) {
+            occlude = true;
+            break;
+          }
+        }
+        if (!occlude) result.push_back(p);
+      }
+      for (unsigned t = 0; t < result.size(); t++) des_pool[t] = result[t];
+      if (result.size() < range) des_pool[result.size()].distance = -1;
+    } else {
+      for (unsigned t = 0; t < range; t++) {
+        if (des_pool[t].distance == -1) {
+          des_pool[t] = sn;
+          if (t + 1 < range) des_pool[t + 1].distance = -1;
+          break;
+        }
+      }
+    }
+  }
+}
+
+// ComponentConnSSGDFS::ConnInner (component_conn.cpp:169-225): n_try roots
+// from a std::random_shuffle of 0..n-1 (libstdc++: for i = 1..n-1 swap ids[i]
+// with ids[rand() % (i + 1)]); from each root a breadth-first walk, and while
+// nodes stay unreached the first reached node with a free slot gets an edge
+// to the smallest unreached id, which the walk continues from
+void conn_ssg(const Data &D, FinalGraph &g, unsigned n_try, unsigned range, GlibcRand &rnd,
+              std::vector<unsigned> &eps, unsigned *added) {
+  std::vector<unsigned> ids(D.n);
+  for (unsigned i = 0; i < D.n; i++) ids[i] = i;
+  for (unsigned i = 1; i < D.n; i++) {
+    unsigned j = (unsigned)((long)rnd.next() % (long)(i + 1));
+    if (i != j) std::swap(ids[i], ids[j]);
+  }
+  *added = 0;
+  for (unsigned i = 0; i < n_try; i++) eps.push_back(ids[i]);
+  for (unsigned i = 0; i < n_try; i++) {
+    unsigned rootid = eps[i];
+    std::vector<char> flags(D.n, 0);
+    std::vector<unsigned> queue;
+    size_t head = 0;
+    queue.push_back(rootid);
+    flags[rootid] = 1;
+    std::vector<unsigned> uncheck_set(1);
+    while (uncheck_set.size() > 0) {
+      while (head < queue.size()) {
+        unsigned q_front = queue[head++];
+        for (unsigned j = 0; j < g[q_front].size(); j++) {
+          unsigned child = g[q_front][j].id;
+          if (flags[child]) continue;
+          flags[child] = 1;
+          queue.push_back(child);
+        }
+      }
+      uncheck_set.clear();
+      for (unsigned j = 0; j < D.n; j++)
+        if (!flags[j]) uncheck_set.push_back(j);
+      if (uncheck_set.size() > 0) {
+        for (unsigned j = 0; j < D.n; j++) {
+          if (flags[j] && g[j].size() < range) {
+            g[j].push_back(SimpleNeighbor(uncheck_set[0], l2(D.row(j), D.row(uncheck_set[0]), D.d)));
+            (*added)++;
+            break;
+          }
+        }
+        queue.push_back(uncheck_set[0]);
+        flags[uncheck_set[0]] = 1;
+      }
+    }
+  }
+}
+
+// ComponentRefineSSG::RefineInner / Link (component_refine.cpp:550-645)
+FinalGraph link_ssg(const Data &D, const FinalGraph &g, unsigned Lr, unsigned Rr, float A) {
+  std::vector<SimpleNeighbor> cut((size_t)D.n * Rr);
+  std::vector<SimpleNeighbor> pool;
+  std::vector<char> flags(D.n);
+  const float threshold = ssg_threshold(A);
+  for (unsigned n = 0; n < D.n; ++n) {
+    pool.clear();
+    candidate_prop2(D, g, n, Lr, flags, pool);
+    prune_ssg(D, g, n, Rr, threshold, pool, cut.data());
+  }
+  for (unsigned n = 0; n < D.n; ++n) inter_insert_ssg(D, n, Rr, threshold, cut.data());
+  return cut_to_final(cut, D.n, Rr);
+}
+
+}  // namespace
+
 extern "C" {
 
 void *orc_rand_create(unsigned seed) { return new GlibcRand(seed); }
@@ -814,6 +1014,22 @@ int orc_nsg(const float *base, unsigned n, unsigned d, const unsigned *in_ids, c
   FinalGraph out = link(D, g, e, L_refine, R_refine, C_refine, false, 1.0f, r, threads < 1 ? 1 : threads);
   conn_dfs(D, out, e, L_refine, r, conn_added);
   *ep = e;
+  return graph_to_arrays(out, ids, dist, deg, out_w);
+}
+
+// REFINE_SSG (component_refine.cpp:550-582): link + DFS-expand conn; eps
+// receives the n_try roots
+int orc_ssg(const float *base, unsigned n, unsigned d, const unsigned *in_ids, const float *in_dist,
+            const unsigned *in_deg, unsigned in_w, unsigned L_refine, unsigned R_refine, float A, unsigned n_try,
+            void *rnd, unsigned *ids, float *dist, unsigned *deg, unsigned out_w, unsigned *eps,
+            unsigned *conn_added) {
+  Data D{base, n, d};
+  GlibcRand &r = *(GlibcRand *)rnd;
+  FinalGraph g = graph_from_arrays(in_ids, in_dist, in_deg, n, in_w);
+  FinalGraph out = link_ssg(D, g, L_refine, R_refine, A);
+  std::vector<unsigned> e;
+  conn_ssg(D, out, n_try, R_refine, r, e, conn_added);
+  for (unsigned i = 0; i < n_try; i++) eps[i] = e[i];
   return graph_to_arrays(out, ids, dist, deg, out_w);
 }
 

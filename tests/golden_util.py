@@ -78,6 +78,9 @@ def replay_oracle(f, pi, on_search=None, on_graph=None):
             g = O.nsg(base, g, p["L_refine"], p["R_refine"], p["C_refine"], rnd)
             entry_L = p["L_refine"]
             exp = key + "nsg"
+        elif kind == "ssg":
+            g = O.ssg(base, g, p["L_refine"], p["R_refine"], float(p["A"]), p["n_try"], rnd)
+            exp = key + "ssg"
         elif kind == "load":
             loaded = g
             continue

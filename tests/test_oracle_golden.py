@@ -51,6 +51,10 @@ def test_oracle_replays_reference(name):
                 g = O.nsg(base, g, p["L_refine"], p["R_refine"], p["C_refine"], rnd)
                 entry_L = p["L_refine"]
                 exp = graph_of(f, key + "nsg")
+            elif kind == "ssg":
+                g = O.ssg(base, g, p["L_refine"], p["R_refine"], float(p["A"]), p["n_try"], rnd)
+                exp = graph_of(f, key + "ssg")
+                assert np.array_equal(g.eps, f[key + "ssg.eps"]), (name, s)
             elif kind == "load":
                 loaded = g
                 continue
