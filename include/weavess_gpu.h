@@ -124,6 +124,17 @@ int wv_vamana_refine(wv_ctx *ctx, uint32_t L_refine, uint32_t R_refine, float al
  * ComponentConnNSGDFS.  Result: the current graph (rows may exceed R_refine
  * after the connectivity pass) with its entry point. */
 int wv_nsg_refine(wv_ctx *ctx, uint32_t L_refine, uint32_t R_refine, uint32_t C_refine, wv_build_stats *stats);
+/* ComponentRefineSSG::RefineInner (component_refine.cpp:550-720): candidates
+ * by ComponentCandidatePropagation2 (component_candidate.cpp:90-109, the
+ * first L_refine unseen neighbours of neighbours), ComponentPruneSSG's angle
+ * rule (component_prune.cpp:71-122, angle A in degrees, rows of at most
+ * R_refine), InterInsert with the same rule, then ComponentConnSSGDFS
+ * (component_conn.cpp:169-225): n_try roots from std::random_shuffle on the
+ * rand stream, every node linked from them.  eps (nullable) receives the
+ * n_try roots; the built graph keeps them for save / load.  Bit-exact with
+ * the reference run on one thread. */
+int wv_ssg_refine(wv_ctx *ctx, uint32_t L_refine, uint32_t R_refine, float A, uint32_t n_try, uint32_t *eps,
+                  wv_build_stats *stats);
 
 /* ---- search ------------------------------------------------------------- */
 /* Replaces the query loop of IndexBuilder::search with L_SEARCH_ASSIGN
@@ -219,17 +230,22 @@ int wv_draw_seeds(wv_ctx *ctx, uint32_t nq, int entry, uint32_t L, uint32_t *see
 int wv_draw_seeds_device(wv_ctx *ctx, uint32_t nq, uint32_t L, uint32_t *d_seeds, uint32_t stride);
 
 /* ---- graph files and index statistics ------------------------------------ */
+/* Header forms of a graph file (the `with_ep` / `use_ep` arguments below) */
+#define WV_GRAPH_PLAIN 0 /* no header (KGraph, ...) */
+#define WV_GRAPH_EP 1    /* one entry point ep_ (INDEX_NSG, INDEX_VAMANA) */
+#define WV_GRAPH_EPS 2   /* root count, then the roots eps_ (INDEX_SSG) */
 /* The per-node graph file of IndexBuilder::save_graph / load_graph
- * (src/builder.cpp:918-1089): [entry point u32 (NSG, Vamana)] then, per node,
- * its degree and ids (u32 each).  Save writes the built graph
- * (final_graph_); load reads into the search graph (load_graph_) and must
- * hold exactly n rows for the uploaded base. */
+ * (src/builder.cpp:918-1095): the header (WV_GRAPH_*), then, per node, its
+ * degree and ids (u32 each).  Save writes the built graph (final_graph_);
+ * load reads into the search graph (load_graph_) and must hold exactly n rows
+ * for the uploaded base. */
 int wv_save_graph(wv_ctx *ctx, const char *path, int with_ep);
 int wv_load_graph(wv_ctx *ctx, const char *path, int with_ep);
 /* IndexBuilder::print_index_info (builder.cpp:501-600, 714-780) on the search
- * graph: out-degree statistics, conn (depth-first traversals from the entry
- * point -- or node 0 when use_ep is 0 -- restarting at the smallest unreached
- * id, until every node is reached) and, given an exact KNN graph (n rows of
+ * graph: out-degree statistics, conn (traversal passes: the first from the
+ * roots -- the entry point (WV_GRAPH_EP), the SSG roots (WV_GRAPH_EPS) or
+ * node 0 (WV_GRAPH_PLAIN) -- then each from the smallest unreached id, until
+ * every node is reached) and, given an exact KNN graph (n rows of
  * exact_width ids, exact_deg valid), the mean share of each node's first 10
  * exact neighbours in its row (-1 when no exact graph is given). */
 typedef struct {

@@ -1,6 +1,6 @@
-"""GPU Vamana / NSG link (candidate search, prune, InterInsert, entry point,
-connectivity) against the reference: every row, the entry point and the
-searches that follow must be identical."""
+"""GPU Vamana / NSG / SSG link (candidates, prune, InterInsert, entry point,
+connectivity) against the reference: every row, the entry point (the SSG
+roots) and the searches that follow must be identical."""
 import numpy as np
 import pytest
 
@@ -47,6 +47,10 @@ def _replay(ctx, f, pi):
             ctx.nsg_refine(p["L_refine"], p["R_refine"], p["C_refine"])
             entry_L = p["L_refine"]
             exp = key + "nsg"
+        elif kind == "ssg":
+            st = ctx.ssg_refine(p["L_refine"], p["R_refine"], float(p["A"]), p["n_try"])
+            exp = key + "ssg"
+            assert np.array_equal(st["eps"], f[exp + ".eps"]), s
         elif kind == "load":
             ctx.load_built_graph()
             continue
@@ -111,3 +115,42 @@ def test_nsg_matches_oracle_20k(ctx, mix20k):
     assert ep == gn.ep
     assert st["conn_added"] == gn.conn_added
     assert rows_equal(ids, dist, deg, gn.ids, gn.dist, gn.deg) == 0, st
+
+
+@pytest.mark.parametrize("L_refine,R_refine,A,n_try", [(100, 50, 60.0, 10), (200, 32, 30.0, 4), (40, 24, 75.0, 1)])
+def test_ssg_matches_oracle_20k(ctx, mix20k, L_refine, R_refine, A, n_try):
+    base, query, g = mix20k
+    ctx.upload_base(base)
+    ctx.srand(1)
+    ctx.init_random(10)
+    ctx.nnd_refine(10, 24, 40, 6, 50)
+    ro = O.Rand(1)
+    go = O.nndescent(base, O.init_random(base, 10, ro), 10, 24, 40, 6, 50, ro)
+    gs = O.ssg(base, go, L_refine, R_refine, A, n_try, ro)
+    st = ctx.ssg_refine(L_refine, R_refine, A, n_try)
+    assert np.array_equal(st["eps"], gs.eps)
+    assert st["conn_added"] == gs.conn_added
+    ids, dist, deg, _ = ctx.get_graph()
+    assert rows_equal(ids, dist, deg, gs.ids, gs.dist, gs.deg) == 0, st
+    # the rand stream continues where the reference's would
+    assert ctx.rand() == ro.next()
+
+
+def test_ssg_graph_file_and_conn(ctx, mix20k, tmp_path):
+    """The INDEX_SSG file (root count, roots, rows) round-trips, and
+    print_index_info's conn, walked from all the roots, is one pass."""
+    base, query, g = mix20k
+    ctx.upload_base(base)
+    ctx.srand(1)
+    ctx.init_random(10)
+    ctx.nnd_refine(10, 24, 40, 6, 50)
+    st = ctx.ssg_refine(100, 50, 60.0, 10)
+    path = str(tmp_path / "g.ssg")
+    ctx.save_graph(path, with_ep="eps")
+    raw = np.fromfile(path, dtype=np.uint32)
+    assert raw[0] == 10 and np.array_equal(raw[1:11], st["eps"])
+    ids, dist, deg, _ = ctx.get_graph()
+    ctx.load_graph(path, with_ep="eps")
+    info = ctx.index_info(use_ep="eps")
+    assert info["conn"] == 1
+    assert info["max_out"] == int(deg.max()) and info["min_out"] == int(deg.min())

@@ -293,6 +293,7 @@ int wv_upload_graph(wv_ctx *c, const uint32_t *ids, const uint32_t *deg, uint32_
   c->gw = width;
   c->ep = ep;
   c->ep_row.assign(ids + (size_t)ep * width, ids + (size_t)ep * width + deg[ep]);
+  c->eps.clear();
   if (c->vis_words != (n + 31) / 32) c->vis_slots = 0;
   return WV_OK;
 }

@@ -1,5 +1,7 @@
 // C ABI: build components and the graph passed between them.
+#include <algorithm>
 #include <chrono>
+#include <vector>
 
 #include "wv_ctx.h"
 #include "wv_link.h"
@@ -30,6 +32,7 @@ int wv_set_graph(wv_ctx *c, const uint32_t *ids, const float *dist, const uint32
   c->fg_w = width;
   c->fg_ep = ep;
   c->fg_has_ep = true;
+  c->fg_eps.clear();
   return WV_OK;
 }
 
@@ -78,6 +81,7 @@ int wv_load_built_graph(wv_ctx *c) {
   c->gn = (uint32_t)n;
   c->gw = (uint32_t)w;
   c->ep = ep;
+  c->eps = c->fg_eps;
   if (c->vis_words != (n + 31) / 32) c->vis_slots = 0;
   return WV_OK;
 }
@@ -121,7 +125,7 @@ int wv_vamana_refine(wv_ctx *c, uint32_t L_refine, uint32_t R_refine, float alph
   auto t0 = std::chrono::steady_clock::now();
   const unsigned long long d0 = c->rnd.drawn;
   LinkStats st;
-  int rc = link_gpu(c, LinkParams{L_refine, R_refine, 0, alpha, entry_L, false}, &st);
+  int rc = link_gpu(c, LinkParams{L_refine, R_refine, 0, alpha, entry_L, LinkMode::VAMANA}, &st);
   if (stats) {
     *stats = wv_build_stats{};
     stats->rand_draws = c->rnd.drawn - d0;
@@ -138,7 +142,7 @@ int wv_nsg_refine(wv_ctx *c, uint32_t L_refine, uint32_t R_refine, uint32_t C_re
   auto t0 = std::chrono::steady_clock::now();
   const unsigned long long d0 = c->rnd.drawn;
   LinkStats st;
-  int rc = link_gpu(c, LinkParams{L_refine, R_refine, C_refine, 1.0f, L_refine, true}, &st);
+  int rc = link_gpu(c, LinkParams{L_refine, R_refine, C_refine, 1.0f, L_refine, LinkMode::NSG}, &st);
   uint32_t added = 0;
   if (rc == WV_OK) rc = conn_dfs_gpu(c, L_refine, &added);
   if (stats) {
@@ -146,6 +150,34 @@ int wv_nsg_refine(wv_ctx *c, uint32_t L_refine, uint32_t R_refine, uint32_t C_re
     stats->rand_draws = c->rnd.drawn - d0;
     stats->levels = st.levels;
     stats->ep = st.ep;
+    stats->conn_added = added;
+    stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return rc;
+}
+
+int wv_ssg_refine(wv_ctx *c, uint32_t L_refine, uint32_t R_refine, float A, uint32_t n_try, uint32_t *eps,
+                  wv_build_stats *stats) {
+  if (!c) return WV_ERR_ARG;
+  WV_CUDA(c, cudaSetDevice(c->device));
+  WV_CHECK(c, n_try >= 1 && n_try <= c->n, WV_ERR_ARG, "n_try=%u out of range (n=%u)", n_try, c->n);
+  auto t0 = std::chrono::steady_clock::now();
+  const unsigned long long d0 = c->rnd.drawn;
+  LinkStats st;
+  LinkParams lp{L_refine, R_refine, 0, 1.0f, 0, LinkMode::SSG};
+  lp.A = A;
+  int rc = link_gpu(c, lp, &st);
+  uint32_t added = 0;
+  std::vector<uint32_t> roots;
+  if (rc == WV_OK) rc = conn_ssg_gpu(c, n_try, R_refine, roots, &added);
+  if (rc == WV_OK) {
+    c->fg_eps = roots;
+    if (eps) std::copy(roots.begin(), roots.end(), eps);
+  }
+  if (stats) {
+    *stats = wv_build_stats{};
+    stats->rand_draws = c->rnd.drawn - d0;
+    stats->levels = st.levels;
     stats->conn_added = added;
     stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }

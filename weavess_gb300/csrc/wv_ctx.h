@@ -63,6 +63,7 @@ struct wv_ctx {
   wv::DevBuf gids, gdeg;
   uint32_t gn = 0, gw = 0, ep = 0;
   std::vector<uint32_t> ep_row;  // host copy of the entry point's row
+  std::vector<uint32_t> eps;     // SSG roots (eps_) of the search graph
 
   // search scratch
   wv::DevBuf visited, touched;
@@ -77,6 +78,7 @@ struct wv_ctx {
   wv::DevBuf fg_ids, fg_dist, fg_deg;
   uint32_t fg_n = 0, fg_w = 0, fg_ep = 0;
   bool fg_has_ep = false;
+  std::vector<uint32_t> fg_eps;  // SSG roots of the built graph (eps_)
 
   // learned entry / beam model (wv_learn.cu), or null
   void *learn = nullptr;

@@ -21,50 +21,13 @@
 #include <utility>
 #include <vector>
 
+#include "wv_bfs.cuh"
 #include "wv_common.cuh"
 #include "wv_ctx.h"
 
 using namespace wv;
 
 namespace {
-
-__global__ void k_bfs_level(const uint32_t *ids, const uint32_t *deg, uint32_t w, uint32_t n, const uint32_t *front,
-                            uint32_t nfront, uint32_t *bits, uint32_t *next, uint32_t *nnext, int *status) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t f = wid; f < nfront; f += nw) {
-    const uint32_t u = front[f];
-    uint32_t dg = deg[u];
-    if (dg > w) {
-      if (lane == 0) set_err(status, DEV_BAD_ID);
-      dg = w;
-    }
-    for (uint32_t j = lane; j < dg; j += 32) {
-      const uint32_t v = ids[(size_t)u * w + j];
-      if (v >= n) {
-        set_err(status, DEV_BAD_ID);
-        continue;
-      }
-      const uint32_t bit = 1u << (v & 31);
-      if (!(atomicOr(bits + (v >> 5), bit) & bit)) next[atomicAdd(nnext, 1u)] = v;
-    }
-  }
-}
-
-// first node id whose bit is clear (n if none): one block
-__global__ void k_first_unreached(const uint32_t *bits, uint32_t n, uint32_t *out) {
-  __shared__ uint32_t best;
-  if (threadIdx.x == 0) best = n;
-  __syncthreads();
-  const uint32_t words = (n + 31) / 32;
-  for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) {
-    uint32_t free = ~bits[i];
-    if (i == words - 1 && (n & 31)) free &= (1u << (n & 31)) - 1u;
-    if (free) atomicMin(&best, i * 32 + (uint32_t)(__ffs(free) - 1));
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) *out = best;
-}
 
 // per node: share of its first 10 exact neighbours (itself skipped) in its row
 __global__ void k_quality(const uint32_t *ids, const uint32_t *deg, uint32_t w, const uint32_t *ex,
@@ -110,7 +73,12 @@ int wv_save_graph(wv_ctx *c, const char *path, int with_ep) {
   FILE *f = fopen(path, "wb");
   WV_CHECK(c, f, WV_ERR_ARG, "cannot open %s for writing", path);
   bool ok = true;
-  if (with_ep) ok = fwrite(&c->fg_ep, 4, 1, f) == 1;
+  if (with_ep == WV_GRAPH_EPS) {  // INDEX_SSG: root count, then the roots
+    const uint32_t ne = (uint32_t)c->fg_eps.size();
+    ok = fwrite(&ne, 4, 1, f) == 1 && fwrite(c->fg_eps.data(), 4, ne, f) == ne;
+  } else if (with_ep) {
+    ok = fwrite(&c->fg_ep, 4, 1, f) == 1;
+  }
   for (size_t i = 0; i < n && ok; i++) {
     const uint32_t gk = deg[i] <= w ? deg[i] : (uint32_t)w;
     ok = fwrite(&gk, 4, 1, f) == 1 && fwrite(ids.data() + i * w, 4, gk, f) == gk;
@@ -126,7 +94,20 @@ int wv_load_graph(wv_ctx *c, const char *path, int with_ep) {
   FILE *f = fopen(path, "rb");
   WV_CHECK(c, f, WV_ERR_ARG, "cannot open %s", path);
   uint32_t ep = 0;
-  if (with_ep && fread(&ep, 4, 1, f) != 1) {
+  std::vector<uint32_t> eps;
+  if (with_ep == WV_GRAPH_EPS) {
+    uint32_t ne = 0;
+    bool ok = fread(&ne, 4, 1, f) == 1 && ne <= c->n;
+    if (ok) {
+      eps.resize(ne);
+      ok = fread(eps.data(), 4, ne, f) == ne;
+    }
+    for (uint32_t x : eps) ok = ok && x < c->n;
+    if (!ok) {
+      fclose(f);
+      return fail(c, WV_ERR_ARG, "%s: bad root list", path);
+    }
+  } else if (with_ep && fread(&ep, 4, 1, f) != 1) {
     fclose(f);
     return fail(c, WV_ERR_ARG, "%s: no entry point", path);
   }
@@ -151,7 +132,9 @@ int wv_load_graph(wv_ctx *c, const char *path, int with_ep) {
     deg[i] = (uint32_t)rows[i].size();
     for (size_t j = 0; j < rows[i].size(); j++) ids[i * w + j] = rows[i][j];
   }
-  return wv_upload_graph(c, ids.data(), deg.data(), c->n, w, with_ep ? ep : 0);
+  int rc = wv_upload_graph(c, ids.data(), deg.data(), c->n, w, with_ep == 1 ? ep : 0);
+  if (rc == WV_OK) c->eps = eps;
+  return rc;
 }
 
 int wv_index_info(wv_ctx *c, int use_ep, const uint32_t *exact_ids, const uint32_t *exact_deg, uint32_t exact_width,
@@ -180,18 +163,32 @@ int wv_index_info(wv_ctx *c, int use_ep, const uint32_t *exact_ids, const uint32
   uint32_t *cnt = c->buf<uint32_t>("gi_cnt", 4, &e);
   WV_CUDA(c, e);
   WV_CUDA(c, cudaMemsetAsync(bits, 0, (size_t)(n + 31) / 32 * 4, c->stream));
-  uint32_t root = use_ep ? c->ep : 0u, conn = 0;
-  WV_CHECK(c, root < n, WV_ERR_ARG, "entry point %u >= n", root);
+  // the first pass walks from every root (the SSG roots, or the entry point,
+  // or node 0), later passes from the smallest unreached id (conn_info,
+  // builder.cpp:569-595)
+  std::vector<uint32_t> roots;
+  if (use_ep == WV_GRAPH_EPS) roots = c->eps;
+  else roots.push_back(use_ep ? c->ep : 0u);
+  WV_CHECK(c, !roots.empty(), WV_ERR_STATE, "the search graph has no root list");
+  for (uint32_t x : roots) WV_CHECK(c, x < n, WV_ERR_ARG, "root %u >= n", x);
+  uint32_t conn = 0;
   for (;;) {
     conn++;
-    const uint32_t word = root >> 5, bit = 1u << (root & 31);
-    uint32_t wv_ = 0;
-    WV_CUDA(c, cudaMemcpyAsync(&wv_, bits + word, 4, cudaMemcpyDeviceToHost, c->stream));
+    // mark the roots (once each) and make them the frontier
+    std::vector<uint32_t> hbits((n + 31) / 32), front;
+    WV_CUDA(c, cudaMemcpyAsync(hbits.data(), bits, hbits.size() * 4, cudaMemcpyDeviceToHost, c->stream));
     WV_CUDA(c, cudaStreamSynchronize(c->stream));
-    wv_ |= bit;
-    WV_CUDA(c, cudaMemcpyAsync(bits + word, &wv_, 4, cudaMemcpyHostToDevice, c->stream));
-    WV_CUDA(c, cudaMemcpyAsync(fa, &root, 4, cudaMemcpyHostToDevice, c->stream));
-    uint32_t nf = 1;
+    for (uint32_t x : roots) {
+      const uint32_t bit = 1u << (x & 31);
+      if (!(hbits[x >> 5] & bit)) {
+        hbits[x >> 5] |= bit;
+        front.push_back(x);
+      }
+    }
+    WV_CUDA(c, cudaMemcpyAsync(bits, hbits.data(), hbits.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    WV_CUDA(c, cudaMemcpyAsync(fa, front.data(), front.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    uint32_t nf = (uint32_t)front.size();
     while (nf) {
       WV_CUDA(c, cudaMemsetAsync(cnt, 0, 4, c->stream));
       const uint32_t blocks = std::min<uint32_t>((nf + 7) / 8, (uint32_t)c->sms * 32);
@@ -204,9 +201,11 @@ int wv_index_info(wv_ctx *c, int use_ep, const uint32_t *exact_ids, const uint32
     }
     k_first_unreached<<<1, 1024, 0, c->stream>>>(bits, n, cnt);
     WV_CUDA(c, cudaGetLastError());
+    uint32_t root = n;
     WV_CUDA(c, cudaMemcpyAsync(&root, cnt, 4, cudaMemcpyDeviceToHost, c->stream));
     WV_CUDA(c, cudaStreamSynchronize(c->stream));
     if (root >= n) break;
+    roots.assign(1, root);
   }
   r.conn = conn;
   r.quality = -1.0;

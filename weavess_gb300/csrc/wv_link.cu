@@ -29,9 +29,11 @@
 //    the vectors' pairwise distances of its row in shared memory, so an
 //    insertion costs one new distance column.
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "warp_sort.cuh"
+#include "wv_bfs.cuh"
 #include "wv_common.cuh"
 #include "wv_link.h"
 #include "wv_scan.h"
@@ -74,6 +76,7 @@ struct PruneArgs {
   uint32_t R;
   float alpha;
   uint32_t maxc;        // NSG: C_refine
+  float threshold;      // SSG: cos of the angle bound
   const uint32_t *g_ids;  // NSG: the candidate graph (final_graph_)
   const uint32_t *g_deg;
   uint32_t gw;
@@ -85,8 +88,22 @@ struct PruneArgs {
   int *status;
 };
 
-template <bool NSG>
+// the angle test of ComponentPruneSSG / RefineSSG::InterInsert
+// (component_prune.cpp:96-104, component_refine.cpp:685-693) with the
+// reference's operand types: float sums, a float quotient by 2, and the
+// quotient by ::sqrt(double) of the float product taken in double, then
+// stored to float
+__device__ __forceinline__ bool ssg_occludes(float pd, float rd, float djk, float threshold) {
+  const float num = __fmul_rn(__fsub_rn(__fadd_rn(pd, rd), djk), 0.5f);  // x / 2 is exact as x * 0.5
+  const double den = __dsqrt_rn((double)__fmul_rn(pd, rd));
+  const float cos_ij = __double2float_rn(__ddiv_rn((double)num, den));
+  return cos_ij > threshold;
+}
+
+// MODE: 0 Vamana, 1 NSG, 2 SSG
+template <int MODE>
 __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
+  constexpr bool NSG = MODE != 0;  // the NSG-style walk (SSG shares it with the angle test)
   __shared__ uint32_t pk_id[PR_WARPS][LINK_MAX_R];
   __shared__ float pk_d[PR_WARPS][LINK_MAX_R];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -148,7 +165,7 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
       }
       np = 1;
       ex = start + 1;
-      end = min(m, a.maxc);
+      end = MODE == 2 ? m : min(m, a.maxc);  // SSG examines the whole pool
       __syncwarp();
     }
     bool done = np >= a.R;
@@ -162,7 +179,8 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
           if (NSG && pid[j] == cand.i) s1 = true;
           else {
             float dd = l2g(a.base, a.d, pid[j], cand.i);
-            s1 = NSG ? (dd < cand.d) : (__fmul_rn(a.alpha, dd) < cand.d);
+            s1 = MODE == 2 ? ssg_occludes(cand.d, pd[j], dd, a.threshold)
+                           : (NSG ? (dd < cand.d) : (__fmul_rn(a.alpha, dd) < cand.d));
           }
         }
       }
@@ -170,12 +188,14 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
       uint32_t occl = 0;
       for (int b = 0; b < (int)cnt; b++) {
         const uint32_t bid = __shfl_sync(FULL, cand.i, b);
+        const float bd = __shfl_sync(FULL, cand.d, b);
         if (b < lane && lane < (int)cnt) {
           bool hit;
           if (NSG && bid == cand.i) hit = true;
           else {
             float dd = l2g(a.base, a.d, bid, cand.i);
-            hit = NSG ? (dd < cand.d) : (__fmul_rn(a.alpha, dd) < cand.d);
+            hit = MODE == 2 ? ssg_occludes(cand.d, bd, dd, a.threshold)
+                            : (NSG ? (dd < cand.d) : (__fmul_rn(a.alpha, dd) < cand.d));
           }
           if (hit) occl |= 1u << b;
         }
@@ -239,6 +259,8 @@ struct IIArgs {
   uint32_t d, n, R;
   float alpha;
   int vamana;
+  int ssg;                 // SSG re-prune: angle test, sentinel after a short result
+  float threshold;
   const uint32_t *p_ids;   // pruned rows (width R)
   const float *p_dist;
   const uint32_t *p_deg;
@@ -434,7 +456,8 @@ __device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t &rs, 
       bool occ = false;
       for (uint32_t j = lane; j < nres; j += 32) {
         const Ent3 r = w.tmp[w.res[j]];
-        occ |= (r.i == p.i) || (w.D[r.slot * S + p.slot] < p.d);
+        const float djk = w.D[r.slot * S + p.slot];
+        occ |= (r.i == p.i) || (a.ssg ? ssg_occludes(p.d, r.d, djk, a.threshold) : (djk < p.d));
       }
       if (!__any_sync(FULL, occ)) {
         if (lane == 0) w.res[nres] = st;
@@ -444,12 +467,12 @@ __device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t &rs, 
     }
   }
   // des_pool[t] = result[t] for t < result.size() (refine.cpp:527-530,
-  // 943-946).  Vamana results always hold R entries; an NSG result may be
-  // shorter and then, with no sentinel written, the old entries at positions
-  // result.size()..R-1 stay in the row.
+  // 943-946, 706-712).  Vamana results always hold R entries; an NSG result
+  // may be shorter and then, with no sentinel written, the old entries at
+  // positions result.size()..R-1 stay in the row; SSG writes the sentinel.
   for (uint32_t j = lane; j < nres; j += 32) w.row[j] = w.tmp[w.res[j]];
   __syncwarp();
-  if (a.vamana) rs = nres;
+  if (a.vamana || a.ssg) rs = nres;  // SSG writes a sentinel after a short result
   __syncwarp();
 }
 
@@ -576,6 +599,146 @@ __global__ void k_pair_l2(const float *base, uint32_t d, uint32_t a, uint32_t b,
   if (threadIdx.x == 0 && blockIdx.x == 0) *out = l2g(base, d, a, b);
 }
 
+// ---------------------------------------------------------------- Propagation2
+// ComponentCandidatePropagation2::CandidateInner (component_candidate.cpp:90-109):
+// the pool takes the unseen neighbours of the node's neighbours, walking the
+// node's row and each neighbour's row in order, and stops at L entries.  One
+// warp per node handles a neighbour row 32 entries at a time: a lane's entry
+// is new when the seen-set lacks it and no lower lane holds the same id; the
+// first (L - size) new entries, in lane order, are appended and marked.  The
+// seen-set is an open-addressing hash in shared memory (at most L + 1 of its
+// 2^k >= 2(L + 1) words are ever used, so a probe always ends).
+constexpr int P2_WARPS_MAX = 8;
+constexpr uint32_t P2_EMPTY = 0xffffffffu;
+
+struct Prop2Args {
+  const float *base;
+  uint32_t d, n;
+  const uint32_t *g_ids, *g_deg;
+  uint32_t gw;
+  uint32_t n0, cnt;   // nodes [n0, n0 + cnt)
+  uint32_t L;
+  uint32_t hwords;    // seen-set words per warp (power of two)
+  DI *vis;            // cnt x vcap pools
+  uint32_t vcap;
+  uint32_t *vcnt;
+  int *status;
+};
+
+__device__ __forceinline__ uint32_t p2_slot(uint32_t v, uint32_t mask) { return (v * 0x9E3779B1u) & mask; }
+
+__device__ __forceinline__ bool p2_find(const uint32_t *H, uint32_t mask, uint32_t v) {
+  uint32_t h = p2_slot(v, mask);
+  for (uint32_t t = 0; t <= mask; t++, h = (h + 1) & mask) {
+    const uint32_t x = H[h];
+    if (x == v) return true;
+    if (x == P2_EMPTY) return false;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void p2_insert(uint32_t *H, uint32_t mask, uint32_t v) {
+  uint32_t h = p2_slot(v, mask);
+  for (uint32_t t = 0; t <= mask; t++, h = (h + 1) & mask) {
+    const uint32_t old = atomicCAS(H + h, P2_EMPTY, v);
+    if (old == P2_EMPTY || old == v) return;
+  }
+}
+
+__global__ void k_prop2(Prop2Args a) {
+  extern __shared__ uint32_t p2_smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  uint32_t *H = p2_smem + (size_t)warp * a.hwords;
+  const uint32_t mask = a.hwords - 1;
+  const unsigned lt = (1u << lane) - 1u;
+  for (uint32_t qi = blockIdx.x * wpb + warp; qi < a.cnt; qi += gridDim.x * wpb) {
+    const uint32_t q = a.n0 + qi;
+    DI *pool = a.vis + (size_t)qi * a.vcap;
+    for (uint32_t k = lane; k < a.hwords; k += 32) H[k] = P2_EMPTY;
+    __syncwarp();
+    if (lane == 0) p2_insert(H, mask, q);
+    __syncwarp();
+    uint32_t size = 0;
+    const uint32_t qdeg = min(a.g_deg[q], a.gw);
+    for (uint32_t i = 0; i < qdeg && size < a.L; i++) {
+      const uint32_t nid = a.g_ids[(size_t)q * a.gw + i];
+      if (nid >= a.n) {
+        if (lane == 0) set_err(a.status, DEV_BAD_ID);
+        continue;
+      }
+      const uint32_t ndeg = min(a.g_deg[nid], a.gw);
+      for (uint32_t b = 0; b < ndeg && size < a.L; b += 32) {
+        const uint32_t j = b + lane;
+        uint32_t v = j < ndeg ? a.g_ids[(size_t)nid * a.gw + j] : P2_EMPTY;
+        if (j < ndeg && v >= a.n) {
+          set_err(a.status, DEV_BAD_ID);
+          v = P2_EMPTY;
+        }
+        bool fresh = v != P2_EMPTY && !p2_find(H, mask, v);
+        const unsigned same = __match_any_sync(FULL, v);
+        fresh = fresh && (same & lt) == 0;  // the lowest lane holding v speaks for it
+        const unsigned newm = __ballot_sync(FULL, fresh);
+        const uint32_t take = min((uint32_t)__popc(newm), a.L - size);
+        const uint32_t rank = __popc(newm & lt);
+        __syncwarp();  // every lookup of this batch precedes its insertions
+        if (fresh && rank < take) {
+          pool[size + rank] = DI{0.f, v};
+          p2_insert(H, mask, v);
+        }
+        size += take;
+        __syncwarp();
+      }
+    }
+    // distances in the reference's order, one lane per entry
+    for (uint32_t j = lane; j < size; j += 32) pool[j].d = l2g(a.base, a.d, q, pool[j].i);
+    if (lane == 0) a.vcnt[qi] = size;
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------- SSG conn
+// smallest reached node whose row has a free slot (deg < R); *out starts at ~0
+__global__ void k_first_open(const uint32_t *bits, const uint32_t *deg, uint32_t n, uint32_t R, uint32_t *out) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    if (((bits[j >> 5] >> (j & 31)) & 1u) && deg[j] < R) {
+      atomicMin(out, j);
+      return;  // later j of this thread are larger
+    }
+  }
+}
+
+// one repair of ConnSSGDFS (component_conn.cpp:205-221): node u = the smallest
+// unreached id; the first reached node j with a free slot gets the edge
+// j -> u (distance in the reference's order); u is marked and becomes the
+// frontier.  u >= n ends the root's pass (frontier size 0).
+__global__ void k_ssg_repair(const float *base, uint32_t d, uint32_t n, uint32_t w, uint32_t R, uint32_t *ids,
+                             float *dist, uint32_t *deg, const uint32_t *u_in, uint32_t *j_in, uint32_t *bits,
+                             uint32_t *front, uint32_t *nfront, uint32_t *added) {
+  if (threadIdx.x != 0) return;
+  const uint32_t u = *u_in, j = *j_in;
+  *j_in = 0xffffffffu;
+  if (u >= n) {
+    *nfront = 0;
+    return;
+  }
+  if (j < n && deg[j] < R) {
+    const uint32_t pos = deg[j];
+    ids[(size_t)j * w + pos] = u;
+    dist[(size_t)j * w + pos] = l2g(base, d, j, u);
+    deg[j] = pos + 1;
+    *added += 1;
+  }
+  bits[u >> 5] |= 1u << (u & 31);
+  front[0] = u;
+  *nfront = 1;
+}
+
+__global__ void k_mark_root(uint32_t *bits, uint32_t r, uint32_t *front) {
+  bits[r >> 5] |= 1u << (r & 31);
+  front[0] = r;
+}
+
 }  // namespace
 
 // ================================================================ host side
@@ -633,12 +796,56 @@ int run_build_search(wv_ctx *c, const float *d_queries, uint32_t nq, const uint3
   return WV_OK;
 }
 
+// seen-set words per warp for pool size L, and the warps per block that fit
+uint32_t prop2_hwords(uint32_t L) {
+  uint32_t h = 64;
+  while (h < 2 * (L + 1)) h <<= 1;
+  return h;
+}
+
+int run_prop2(wv_ctx *c, uint32_t n0, uint32_t cnt, uint32_t L, DI *vis, uint32_t *vcnt, uint32_t vcap) {
+  Prop2Args a{};
+  a.base = c->base.as<float>();
+  a.d = c->d;
+  a.n = c->n;
+  a.g_ids = c->fg_ids.as<uint32_t>();
+  a.g_deg = c->fg_deg.as<uint32_t>();
+  a.gw = c->fg_w;
+  a.n0 = n0;
+  a.cnt = cnt;
+  a.L = L;
+  a.hwords = prop2_hwords(L);
+  a.vis = vis;
+  a.vcap = vcap;
+  a.vcnt = vcnt;
+  a.status = c->d_status();
+  const size_t per_warp = (size_t)a.hwords * 4;
+  const int wpb = (int)std::max<size_t>(1, std::min<size_t>(P2_WARPS_MAX, (96u << 10) / per_warp));
+  const size_t smem = per_warp * wpb;
+  WV_CUDA(c, cudaFuncSetAttribute(k_prop2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int blocks = (int)std::min<size_t>(((size_t)cnt + wpb - 1) / wpb, (size_t)c->sms * 16);
+  k_prop2<<<std::max(blocks, 1), wpb * 32, smem, c->stream>>>(a);
+  WV_CUDA(c, cudaGetLastError());
+  return WV_OK;
+}
+
+// float threshold = std::cos(A / 180 * kPi) (component_prune.cpp:92-93,
+// component_refine.cpp:640-641): float quotient, double product and cosine
+float ssg_threshold(float A) {
+  const double kPi = std::acos(-1.0);
+  return (float)std::cos((double)(A / 180) * kPi);
+}
+
 }  // namespace
 
 int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
+  const bool ssg = p.mode == LinkMode::SSG, vamana = p.mode == LinkMode::VAMANA;
   WV_CHECK(c, c->n > 0 && c->fg_n == c->n, WV_ERR_STATE, "the link needs the base and a candidate graph");
   WV_CHECK(c, p.R >= 1 && p.R <= LINK_MAX_R, WV_ERR_LIMIT, "R_refine=%u: this build supports 1..%u", p.R, LINK_MAX_R);
-  WV_CHECK(c, p.L >= 1 && p.L < c->n && p.L <= SEARCH_MAX_L, WV_ERR_ARG, "L_refine=%u out of range", p.L);
+  if (ssg)
+    WV_CHECK(c, p.L >= 1 && p.L <= (1u << 13), WV_ERR_ARG, "L_refine=%u out of range", p.L);
+  else
+    WV_CHECK(c, p.L >= 1 && p.L < c->n && p.L <= SEARCH_MAX_L, WV_ERR_ARG, "L_refine=%u out of range", p.L);
   WV_CHECK(c, c->fg_w <= SEARCH_MAX_WIDTH, WV_ERR_LIMIT, "candidate graph width %u above %u", c->fg_w,
            SEARCH_MAX_WIDTH);
   WV_CHECK(c, c->d % 4 == 0, WV_ERR_LIMIT, "dimension %u is not a multiple of 4", c->d);
@@ -665,10 +872,13 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
   uint32_t *seed1 = c->buf<uint32_t>("seed1", p.L, &e);
   uint32_t *one = c->buf<uint32_t>("one", 4, &e);
   WV_CUDA(c, e);
-  // ---- entry point (ComponentRefineEntryCentroid::EntryInner)
+  // ---- entry point (ComponentRefineEntryCentroid::EntryInner); SSG has none
+  // (its RefineInner leaves the entry step out) and draws no rand() here
+  uint32_t ep = 0;
+  if (!ssg) {
   k_centroid<<<(c->d + 127) / 128, 128, 0, c->stream>>>(c->base.as<float>(), n, c->d, center);
   WV_CUDA(c, cudaGetLastError());
-  uint32_t ep = (uint32_t)c->rnd.next() % n;
+  ep = (uint32_t)c->rnd.next() % n;
   if (p.entry_L == 0) {
     ep = 0;  // get_neighbors with L = 0 leaves retset[0] value-initialised
   } else {
@@ -685,6 +895,7 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
     WV_CUDA(c, cudaMemcpyAsync(&ep, one, 4, cudaMemcpyDeviceToHost, c->stream));
     WV_CUDA(c, cudaStreamSynchronize(c->stream));
   }
+  }
   S.ep = ep;
   // ---- candidates + prune, in chunks of nodes
   uint32_t *p_ids = c->buf<uint32_t>("lk_pids", (size_t)n * R, &e);
@@ -692,20 +903,22 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
   uint32_t *p_deg = c->buf<uint32_t>("lk_pdeg", n, &e);
   WV_CUDA(c, e);
   std::vector<uint32_t> ep_row;
-  {
+  if (!ssg) {
     int rc = host_row(ep, ep_row);
     if (rc) return rc;
   }
-  const bool shared_seeds = p.L <= ep_row.size();  // no rand() fill needed
-  uint32_t vcap = std::max<uint32_t>(2048, 8 * p.L) + gw;
+  const bool shared_seeds = ssg || p.L <= ep_row.size();  // no rand() fill needed
+  // SSG pools hold at most L candidates plus the node's row
+  uint32_t vcap = ssg ? p.L + gw : std::max<uint32_t>(2048, 8 * p.L) + gw;
   const uint32_t CH = std::min<uint32_t>(n, 1u << 17);
   std::vector<uint32_t> hseeds;
   uint32_t *dseeds = c->buf<uint32_t>("lk_seeds", (size_t)(shared_seeds ? 1 : CH) * p.L, &e);
   WV_CUDA(c, e);
-  if (shared_seeds)
+  if (shared_seeds && !ssg)
     WV_CUDA(c, cudaMemcpyAsync(dseeds, ep_row.data(), p.L * 4, cudaMemcpyHostToDevice, c->stream));
   const int prune_blocks = c->sms * 8;
   const size_t nwarps = (size_t)prune_blocks * PR_WARPS;
+  const float threshold = ssg ? ssg_threshold(p.A) : 0.f;
   for (uint32_t n0 = 0; n0 < n; n0 += CH) {
     const uint32_t cnt = std::min(CH, n - n0);
     if (!shared_seeds) {
@@ -722,14 +935,16 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
       int *gscr = c->buf<int>("lk_gscr", nwarps * (2 * (size_t)vcap + 256), &e);
       HeapItem *hscr = c->buf<HeapItem>("lk_hscr", nwarps * (size_t)vcap, &e);
       WV_CUDA(c, e);
-      int rc = run_build_search(c, c->base.as<float>() + (size_t)n0 * c->d, cnt, dseeds, shared_seeds ? 0 : p.L, p.L,
-                                c->fg_ids.as<uint32_t>(), c->fg_deg.as<uint32_t>(), gw, vis, vcnt, vcap, nullptr, 1,
-                                vcap - (p.nsg ? gw : 0));
+      int rc = ssg ? run_prop2(c, n0, cnt, p.L, vis, vcnt, vcap)
+                   : run_build_search(c, c->base.as<float>() + (size_t)n0 * c->d, cnt, dseeds,
+                                      shared_seeds ? 0 : p.L, p.L, c->fg_ids.as<uint32_t>(),
+                                      c->fg_deg.as<uint32_t>(), gw, vis, vcnt, vcap, nullptr, 1,
+                                      vcap - (vamana ? 0 : gw));
       if (rc) return rc;
       int st0 = 0;
       WV_CUDA(c, cudaMemcpyAsync(&st0, c->d_status(), 4, cudaMemcpyDeviceToHost, c->stream));
       WV_CUDA(c, cudaStreamSynchronize(c->stream));
-      if (st0 == DEV_OVERFLOW) {  // a visit list outgrew vcap: redo the chunk with room
+      if (st0 == DEV_OVERFLOW && !ssg) {  // a visit list outgrew vcap: redo the chunk with room
         WV_CUDA(c, cudaMemsetAsync(c->d_status(), 0, 4, c->stream));
         vcap = vcap * 2;
         continue;
@@ -748,6 +963,7 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
       pa.R = R;
       pa.alpha = p.alpha;
       pa.maxc = p.C;
+      pa.threshold = threshold;
       pa.g_ids = c->fg_ids.as<uint32_t>();
       pa.g_deg = c->fg_deg.as<uint32_t>();
       pa.gw = gw;
@@ -757,8 +973,9 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
       pa.out_dist = p_dist;
       pa.out_deg = p_deg;
       pa.status = c->d_status();
-      if (p.nsg) k_prune<true><<<prune_blocks, PR_WARPS * 32, 0, c->stream>>>(pa);
-      else k_prune<false><<<prune_blocks, PR_WARPS * 32, 0, c->stream>>>(pa);
+      if (ssg) k_prune<2><<<prune_blocks, PR_WARPS * 32, 0, c->stream>>>(pa);
+      else if (!vamana) k_prune<1><<<prune_blocks, PR_WARPS * 32, 0, c->stream>>>(pa);
+      else k_prune<0><<<prune_blocks, PR_WARPS * 32, 0, c->stream>>>(pa);
       WV_CUDA(c, cudaGetLastError());
       rc = check_device_status(c, "prune");
       if (rc) return rc;
@@ -822,7 +1039,9 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
   ia.n = n;
   ia.R = R;
   ia.alpha = p.alpha;
-  ia.vamana = !p.nsg;
+  ia.vamana = vamana;
+  ia.ssg = ssg;
+  ia.threshold = threshold;
   ia.p_ids = p_ids;
   ia.p_dist = p_dist;
   ia.p_deg = p_deg;
@@ -870,7 +1089,8 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
   if (rc) return rc;
   c->fg_w = R;
   c->fg_ep = ep;
-  c->fg_has_ep = true;
+  c->fg_has_ep = !ssg;
+  c->fg_eps.clear();
   cudaEventRecord(e1, c->stream);
   cudaEventSynchronize(e1);
   cudaEventElapsedTime(&S.ms, e0, e1);
@@ -1023,6 +1243,65 @@ int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
     }
   }
   return WV_OK;
+}
+
+int conn_ssg_gpu(wv_ctx *c, uint32_t n_try, uint32_t R, std::vector<uint32_t> &eps, uint32_t *added) {
+  // ComponentConnSSGDFS::ConnInner (component_conn.cpp:169-225).  The roots
+  // are the first n_try ids of std::random_shuffle(0..n-1) on rand()
+  // (libstdc++: for i = 1..n-1 swap ids[i] with ids[rand() % (i + 1)]).
+  // From each root a breadth-first walk; while nodes stay unreached, the
+  // smallest unreached id u is linked from the first reached node with a free
+  // slot (if any), marked, and walked from.  Reach does not depend on the
+  // walk's order, so the walk runs level-synchronously on the GPU.
+  const uint32_t n = c->n, w = c->fg_w;
+  WV_CHECK(c, n_try >= 1 && n_try <= n, WV_ERR_ARG, "n_try=%u out of range (n=%u)", n_try, n);
+  WV_CHECK(c, R <= w, WV_ERR_ARG, "range %u above the row width %u", R, w);
+  std::vector<uint32_t> perm(n);
+  for (uint32_t i = 0; i < n; i++) perm[i] = i;
+  for (uint32_t i = 1; i < n; i++) {
+    const uint32_t j = (uint32_t)c->rnd.next() % (i + 1);
+    if (i != j) std::swap(perm[i], perm[j]);
+  }
+  eps.assign(perm.begin(), perm.begin() + n_try);
+  cudaError_t e = cudaSuccess;
+  const uint32_t words = (n + 31) / 32;
+  uint32_t *bits = c->buf<uint32_t>("sc_bits", words, &e);
+  uint32_t *fa = c->buf<uint32_t>("sc_fa", n, &e);
+  uint32_t *fb = c->buf<uint32_t>("sc_fb", n, &e);
+  uint32_t *cnt = c->buf<uint32_t>("sc_cnt", 8, &e);  // [0] frontier size, [1] u, [2] j, [3] added
+  WV_CUDA(c, e);
+  WV_CUDA(c, cudaMemsetAsync(cnt, 0, 32, c->stream));
+  WV_CUDA(c, cudaMemsetAsync(cnt + 2, 0xff, 4, c->stream));
+  uint32_t *ids = c->fg_ids.as<uint32_t>(), *deg = c->fg_deg.as<uint32_t>();
+  float *dist = c->fg_dist.as<float>();
+  const int scan_blocks = c->sms * 4;
+  for (uint32_t t = 0; t < n_try; t++) {
+    WV_CUDA(c, cudaMemsetAsync(bits, 0, (size_t)words * 4, c->stream));
+    k_mark_root<<<1, 1, 0, c->stream>>>(bits, eps[t], fa);
+    uint32_t nf = 1;
+    for (;;) {
+      while (nf) {
+        WV_CUDA(c, cudaMemsetAsync(cnt, 0, 4, c->stream));
+        const uint32_t blocks = std::min<uint32_t>((nf + 7) / 8, (uint32_t)c->sms * 32);
+        k_bfs_level<<<blocks, 256, 0, c->stream>>>(ids, deg, w, n, fa, nf, bits, fb, cnt, c->d_status());
+        WV_CUDA(c, cudaGetLastError());
+        WV_CUDA(c, cudaMemcpyAsync(&nf, cnt, 4, cudaMemcpyDeviceToHost, c->stream));
+        WV_CUDA(c, cudaStreamSynchronize(c->stream));
+        std::swap(fa, fb);
+      }
+      k_first_unreached<<<1, 1024, 0, c->stream>>>(bits, n, cnt + 1);
+      k_first_open<<<scan_blocks, 256, 0, c->stream>>>(bits, deg, n, R, cnt + 2);
+      k_ssg_repair<<<1, 32, 0, c->stream>>>(c->base.as<float>(), c->d, n, w, R, ids, dist, deg, cnt + 1,
+                                            cnt + 2, bits, fa, cnt, cnt + 3);
+      WV_CUDA(c, cudaGetLastError());
+      WV_CUDA(c, cudaMemcpyAsync(&nf, cnt, 4, cudaMemcpyDeviceToHost, c->stream));
+      WV_CUDA(c, cudaStreamSynchronize(c->stream));
+      if (!nf) break;
+    }
+  }
+  WV_CUDA(c, cudaMemcpyAsync(added, cnt + 3, 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  return check_device_status(c, "ssg conn");
 }
 
 }  // namespace wv

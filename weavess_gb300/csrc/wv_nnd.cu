@@ -667,6 +667,7 @@ int init_random_gpu(wv_ctx *c, uint32_t S) {
   c->fg_n = c->n;
   c->fg_w = S;
   c->fg_has_ep = false;
+  c->fg_eps.clear();
   return check_device_status(c, "init_random");
 }
 
@@ -897,6 +898,7 @@ int nndescent_gpu(wv_ctx *c, const NndParams &p, NndStats *st) {
   cudaEventDestroy(ev1);
   c->fg_w = p.K;
   c->fg_has_ep = false;
+  c->fg_eps.clear();
   return check_device_status(c, "nndescent");
 }
 

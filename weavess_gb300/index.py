@@ -111,6 +111,15 @@ class Context:
         self._check(self.L.wv_nsg_refine(self.h, L_refine, R_refine, C_refine, C.byref(st)))
         return st.as_dict()
 
+    def ssg_refine(self, L_refine: int, R_refine: int, A: float, n_try: int):
+        """REFINE_SSG; returns the build stats with the n_try roots under "eps"."""
+        st = _lib.BuildStats()
+        eps = np.zeros(n_try, np.uint32)
+        self._check(self.L.wv_ssg_refine(self.h, L_refine, R_refine, A, n_try, eps.ctypes.data, C.byref(st)))
+        out = st.as_dict()
+        out["eps"] = eps
+        return out
+
     # -- search (IndexBuilder::search, L_SEARCH_ASSIGN)
     def search(self, queries, L: int, K: int = 10, entry="rand", return_dist=False):
         q = _f32(queries)
@@ -218,21 +227,26 @@ class Context:
         return out
 
     # -- graph files and statistics (IndexBuilder::save_graph / load_graph / print_index_info)
-    def save_graph(self, path: str, with_ep: bool = False):
-        self._check(self.L.wv_save_graph(self.h, path.encode(), 1 if with_ep else 0))
+    # graph-file headers: False / "plain" (none), True / "ep" (ep_), "eps" (SSG roots)
+    @staticmethod
+    def _hdr(with_ep):
+        return {False: 0, True: 1, "plain": 0, "ep": 1, "eps": 2}[with_ep]
 
-    def load_graph(self, path: str, with_ep: bool = False):
-        self._check(self.L.wv_load_graph(self.h, path.encode(), 1 if with_ep else 0))
+    def save_graph(self, path: str, with_ep=False):
+        self._check(self.L.wv_save_graph(self.h, path.encode(), self._hdr(with_ep)))
 
-    def index_info(self, use_ep: bool = False, exact_ids=None, exact_deg=None):
+    def load_graph(self, path: str, with_ep=False):
+        self._check(self.L.wv_load_graph(self.h, path.encode(), self._hdr(with_ep)))
+
+    def index_info(self, use_ep=False, exact_ids=None, exact_deg=None):
         r = _lib.IndexInfo()
+        h = self._hdr(use_ep)
         if exact_ids is not None:
             ex = _u32(exact_ids)
             exd = _u32(exact_deg if exact_deg is not None else np.full(ex.shape[0], ex.shape[1], np.uint32))
-            self._check(self.L.wv_index_info(self.h, 1 if use_ep else 0, ex.ctypes.data, exd.ctypes.data, ex.shape[1],
-                                             C.byref(r)))
+            self._check(self.L.wv_index_info(self.h, h, ex.ctypes.data, exd.ctypes.data, ex.shape[1], C.byref(r)))
         else:
-            self._check(self.L.wv_index_info(self.h, 1 if use_ep else 0, None, None, 0, C.byref(r)))
+            self._check(self.L.wv_index_info(self.h, h, None, None, 0, C.byref(r)))
         return {"max_out": r.max_out, "min_out": r.min_out, "avg_out": r.avg_out, "conn": r.conn,
                 "quality": r.quality}
 
