@@ -36,7 +36,13 @@ typedef enum {
 typedef enum {
   WV_ENTRY_RAND = 0,     /* ComponentSearchEntryRand (component_search_entry.cpp:9-30) */
   WV_ENTRY_CENTROID = 1, /* ComponentSearchEntryCentroid (component_search_entry.cpp:33-67) */
-  WV_ENTRY_SEEDS = 2     /* caller-supplied seed ids (nq x L) */
+  WV_ENTRY_SEEDS = 2,    /* caller-supplied seed ids (nq x L) */
+  /* ComponentSearchEntrySubCentroid (component_search_entry.cpp:70-99), the
+   * SSG search entry: the Rand draw with its first ids replaced by the
+   * search graph's SSG roots, seed distances taken -- as the reference
+   * takes them -- to each row shifted by one float (a zero follows the last
+   * row) */
+  WV_ENTRY_SUB_CENTROID = 3
 } wv_entry;
 
 typedef struct wv_ctx wv_ctx;
@@ -69,6 +75,12 @@ int wv_upload_base(wv_ctx *ctx, const float *base, uint32_t n, uint32_t d);
  * (load_graph_) as fixed-width rows, ids[n*width], deg[n], entry point ep_. */
 int wv_upload_graph(wv_ctx *ctx, const uint32_t *ids, const uint32_t *deg, uint32_t n, uint32_t width,
                     uint32_t ep);
+/* The SSG roots eps_ of the search graph (load_graph of INDEX_SSG,
+ * builder.cpp:1091-1095); uploading a graph clears them. */
+int wv_set_eps(wv_ctx *ctx, const uint32_t *eps, uint32_t n_eps);
+/* Reads the roots of the built graph (built != 0) or of the search graph:
+ * *n_eps = their count, the first min(cap, count) copied to eps (nullable). */
+int wv_get_eps(wv_ctx *ctx, int built, uint32_t *eps, uint32_t cap, uint32_t *n_eps);
 
 /* ---- build ------------------------------------------------------------- */
 typedef struct {

@@ -56,9 +56,9 @@ def lib():
         L.orc_ssg.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint, C.c_uint, C.c_float,
                               C.c_uint, C.c_void_p, u32p, f32p, u32p, C.c_uint, u32p, u32p]
         L.orc_search.argtypes = [f32p, C.c_uint, C.c_uint, f32p, C.c_uint, u32p, u32p, C.c_uint, C.c_uint,
-                                 C.c_int, C.c_uint, C.c_uint, C.c_void_p, C.c_int, u32p, u64p]
+                                 C.c_int, C.c_uint, C.c_uint, C.c_void_p, C.c_int, u32p, u64p, u32p, C.c_uint]
         L.orc_search_seeds.argtypes = [C.c_uint, C.c_uint, u32p, u32p, C.c_uint, C.c_uint, C.c_int, C.c_uint,
-                                       C.c_void_p, u32p]
+                                       C.c_void_p, u32p, u32p, C.c_uint]
         _lib = L
     return _lib
 
@@ -200,22 +200,35 @@ def ssg(base, g: Graph, L_refine, R_refine, A, n_try, rnd: Rand, out_w=None) -> 
     return out
 
 
+ENTRIES = {"rand": 0, "centroid": 1, "sub_centroid": 2}
+
+
+def _eps(g: Graph, entry):
+    eps = getattr(g, "eps", None) if entry == "sub_centroid" else None
+    eps = np.zeros(1, np.uint32) if eps is None else _c(eps, np.uint32)
+    return eps, (len(eps) if entry == "sub_centroid" else 0)
+
+
 def search(base, query, g: Graph, L, rnd: Rand, entry="rand", K=10, threads=1):
+    """IndexBuilder::search (L_SEARCH_ASSIGN): entry "rand", "centroid" (the
+    graph's ep) or "sub_centroid" (the graph's SSG roots, g.eps)."""
     base, query = _c(base, np.float32), _c(query, np.float32)
     n, d = base.shape
     nq = query.shape[0]
     res = np.zeros((nq, K), np.uint32)
     cnt = np.zeros(2, np.uint64)
+    eps, ne = _eps(g, entry)
     rc = lib().orc_search(base, n, d, query, nq, _c(g.ids, np.uint32), _c(g.deg, np.uint32), g.width,
-                          int(g.ep or 0), 0 if entry == "rand" else 1, L, K, rnd.h, threads, res, cnt)
+                          int(g.ep or 0), ENTRIES[entry], L, K, rnd.h, threads, res, cnt, eps, ne)
     assert rc == 0
     return res, int(cnt[0]), int(cnt[1])
 
 
 def search_seeds(n, nq, g: Graph, L, rnd: Rand, entry="rand"):
     seeds = np.zeros((nq, L), np.uint32)
+    eps, ne = _eps(g, entry)
     lib().orc_search_seeds(n, nq, _c(g.ids, np.uint32), _c(g.deg, np.uint32), g.width, int(g.ep or 0),
-                           0 if entry == "rand" else 1, L, rnd.h, seeds)
+                           ENTRIES[entry], L, rnd.h, seeds, eps, ne)
     return seeds
 
 

@@ -16,7 +16,9 @@
 //
 // usage: ref_driver base.fvecs query.fvecs gt.ivecs outprefix key=val ... -- step ...
 //   steps: init_random | init_rand | nndescent | vamana | nsg | ssg | load:<kgraph|vamana|nsg|ssg>
-//          | search_rand:<L> | search_centroid:<L> | rand_probe
+//          | search_rand:<L> | search_centroid:<L> | search_sub:<L> | rand_probe
+//   (search_sub: SEARCH_ENTRY_SUB_CENTROID, the entry the reference's SSG
+//   test searches with, test/main.cpp:117)
 #include <bits/stdc++.h>
 #include <omp.h>
 #include <boost/dynamic_bitset.hpp>
@@ -76,6 +78,16 @@ int main(int argc, char **argv) {
   idx->R_refine = 0;
   idx->C_refine = 0;
   idx->alpha = alpha;
+  // ComponentSearchEntrySubCentroid reads the base row shifted by one float
+  // (component_search_entry.cpp:84-86), so for the last row it reads one
+  // float past the array.  The driver gives that float a defined value, 0 --
+  // what a fresh allocation above the mmap threshold holds there.
+  {
+    const size_t nd = (size_t)idx->getBaseLen() * idx->getBaseDim();
+    float *padded = new float[nd + 4]();
+    std::memcpy(padded, idx->getBaseData(), nd * sizeof(float));
+    idx->setBaseData(padded);
+  }
   for (; a < argc; a++) {
     std::string step = argv[a];
     std::string arg;
@@ -121,12 +133,14 @@ int main(int argc, char **argv) {
       builder->save_graph(t, &gf[0]);
       idx->getLoadGraph().clear();
       builder->load_graph(t, &gf[0]);
-    } else if (step == "search_rand" || step == "search_centroid") {
+    } else if (step == "search_rand" || step == "search_centroid" || step == "search_sub") {
       unsigned L = (unsigned)std::stoul(arg);
       idx->getParam().set<unsigned>("K_search", 10);
       idx->getParam().set<unsigned>("L_search", L);
-      ComponentSearchEntry *e = step == "search_rand" ? (ComponentSearchEntry *)new ComponentSearchEntryRand(idx)
-                                                      : (ComponentSearchEntry *)new ComponentSearchEntryCentroid(idx);
+      ComponentSearchEntry *e =
+          step == "search_rand"       ? (ComponentSearchEntry *)new ComponentSearchEntryRand(idx)
+          : step == "search_centroid" ? (ComponentSearchEntry *)new ComponentSearchEntryCentroid(idx)
+                                      : (ComponentSearchEntry *)new ComponentSearchEntrySubCentroid(idx);
       auto *r = new ComponentSearchRouteGreedy(idx);
       idx->resetDistCount();
       idx->resetHopCount();

@@ -1033,38 +1033,63 @@ int orc_ssg(const float *base, unsigned n, unsigned d, const unsigned *in_ids, c
   return graph_to_arrays(out, ids, dist, deg, out_w);
 }
 
-// IndexBuilder::search with L_SEARCH_ASSIGN (builder.cpp:430-454):
-// entry 0 = SearchEntryRand (component_search_entry.cpp:9-30),
-// entry 1 = SearchEntryCentroid (component_search_entry.cpp:33-67),
-// route = ComponentSearchRouteGreedy (component_route.cpp:9-53).
+// Seed draws of the three entries (the host side of the GPU search makes the
+// same draws):
+// entry 0 = SearchEntryRand (component_search_entry.cpp:9-30): one rand()
+//   seeds an mt19937, GenRandom draws L distinct ids;
+// entry 1 = SearchEntryCentroid (component_search_entry.cpp:33-67): the entry
+//   point's row, then rand() % n fills (no repeats);
+// entry 2 = SearchEntrySubCentroid (component_search_entry.cpp:70-99): the
+//   Rand draw with its first n_eps ids replaced by the SSG roots (the pool
+//   may then hold an id twice).
+static void draw_entry(unsigned n, const unsigned *g_ids, const unsigned *g_deg, unsigned g_w, unsigned ep, int entry,
+                unsigned L, const unsigned *eps, unsigned n_eps, GlibcRand &r, unsigned *s) {
+  if (entry == 0 || entry == 2) {
+    std::mt19937 rng(r.next());
+    gen_random(rng, s, L, n);
+    if (entry == 2)
+      for (unsigned i = 0; i < n_eps && i < L; i++) s[i] = eps[i];
+  } else {
+    std::vector<char> flags(n, 0);
+    unsigned t = 0;
+    for (; t < L && t < g_deg[ep]; t++) {
+      s[t] = g_ids[(size_t)ep * g_w + t];
+      flags[s[t]] = 1;
+    }
+    while (t < L) {
+      unsigned id = (unsigned)r.next() % n;
+      if (flags[id]) continue;
+      flags[id] = 1;
+      s[t++] = id;
+    }
+  }
+}
+
+// SearchEntrySubCentroid's seed distance (component_search_entry.cpp:84-89):
+// the row pointer is advanced by one float (its first value taken as a
+// norm) and d floats compared from there -- for the last row that is one
+// float past the base, read as 0 here
+static float sub_centroid_dist(const float *base, unsigned n, unsigned d, unsigned id, const float *qv) {
+  std::vector<float> x(d);
+  const float *row = base + (size_t)id * d + 1;
+  for (unsigned j = 0; j + 1 < d; j++) x[j] = row[j];
+  x[d - 1] = id + 1 < n ? row[d - 1] : 0.0f;
+  return l2(x.data(), qv, d);
+}
+
+// IndexBuilder::search with L_SEARCH_ASSIGN (builder.cpp:430-454): seeds by
+// draw_entry, route = ComponentSearchRouteGreedy (component_route.cpp:9-53).
 // res: nq x K ids; counters: [dist_count, hop_count].  With threads > 1 the
 // seed draws are made first in query order (so results stay deterministic)
 // and the queries then run in an OpenMP loop like builder.cpp:285-295.
 int orc_search(const float *base, unsigned n, unsigned d, const float *query, unsigned nq, const unsigned *g_ids,
                const unsigned *g_deg, unsigned g_w, unsigned ep, int entry, unsigned L, unsigned K, void *rnd,
-               int threads, unsigned *res, unsigned long long *counters) {
+               int threads, unsigned *res, unsigned long long *counters, const unsigned *eps, unsigned n_eps) {
   if (L < K) return -1;
+  if (entry == 2 && n_eps > L) return -1;  // the reference asserts eps_.size() <= L
   GlibcRand &r = *(GlibcRand *)rnd;
   std::vector<std::vector<unsigned>> seeds(nq, std::vector<unsigned>(L));
-  for (unsigned q = 0; q < nq; q++) {
-    if (entry == 0) {
-      std::mt19937 rng(r.next());
-      gen_random(rng, seeds[q].data(), L, n);
-    } else {
-      std::vector<char> flags(n, 0);
-      unsigned t = 0;
-      for (; t < L && t < g_deg[ep]; t++) {
-        seeds[q][t] = g_ids[(size_t)ep * g_w + t];
-        flags[seeds[q][t]] = 1;
-      }
-      while (t < L) {
-        unsigned id = (unsigned)r.next() % n;
-        if (flags[id]) continue;
-        flags[id] = 1;
-        seeds[q][t++] = id;
-      }
-    }
-  }
+  for (unsigned q = 0; q < nq; q++) draw_entry(n, g_ids, g_deg, g_w, ep, entry, L, eps, n_eps, r, seeds[q].data());
   unsigned long long dc = 0, hc = 0;
 #pragma omp parallel num_threads(threads < 1 ? 1 : threads) reduction(+ : dc, hc)
   {
@@ -1075,7 +1100,8 @@ int orc_search(const float *base, unsigned n, unsigned d, const float *query, un
       const float *qv = query + (size_t)q * d;
       for (unsigned i = 0; i < L; i++) {
         unsigned id = seeds[q][i];
-        pool[i] = Neighbor(id, l2(qv, base + (size_t)id * d, d), true);
+        const float dist = entry == 2 ? sub_centroid_dist(base, n, d, id, qv) : l2(qv, base + (size_t)id * d, d);
+        pool[i] = Neighbor(id, dist, true);
         dc++;
       }
       std::sort(pool.begin(), pool.begin() + L);
@@ -1111,28 +1137,10 @@ int orc_search(const float *base, unsigned n, unsigned d, const float *query, un
 
 // Seeds only (the host side of the GPU search does the same draws)
 int orc_search_seeds(unsigned n, unsigned nq, const unsigned *g_ids, const unsigned *g_deg, unsigned g_w, unsigned ep,
-                     int entry, unsigned L, void *rnd, unsigned *seeds) {
+                     int entry, unsigned L, void *rnd, unsigned *seeds, const unsigned *eps, unsigned n_eps) {
   GlibcRand &r = *(GlibcRand *)rnd;
-  for (unsigned q = 0; q < nq; q++) {
-    unsigned *s = seeds + (size_t)q * L;
-    if (entry == 0) {
-      std::mt19937 rng(r.next());
-      gen_random(rng, s, L, n);
-    } else {
-      std::vector<char> flags(n, 0);
-      unsigned t = 0;
-      for (; t < L && t < g_deg[ep]; t++) {
-        s[t] = g_ids[(size_t)ep * g_w + t];
-        flags[s[t]] = 1;
-      }
-      while (t < L) {
-        unsigned id = (unsigned)r.next() % n;
-        if (flags[id]) continue;
-        flags[id] = 1;
-        s[t++] = id;
-      }
-    }
-  }
+  for (unsigned q = 0; q < nq; q++)
+    draw_entry(n, g_ids, g_deg, g_w, ep, entry, L, eps, n_eps, r, seeds + (size_t)q * L);
   return 0;
 }
 

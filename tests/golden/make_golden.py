@@ -46,7 +46,7 @@ CASES = {
                                   "vamana", "load:vamana", "search_centroid:30", "search_rand:17"],
                                  ["init_random", "nndescent", "nsg", "load:nsg", "search_centroid:30",
                                   "search_rand:40"],
-                                 ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:30"]]),
+                                 ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:30", "search_sub:30"]]),
     # S > 16 and L_refine > K: introsort on ties, rand() seed fill in the
     # candidate search, heavy reverse-list overflow (R=12)
     "int_n1500_s20": dict(data=lambda: ds.int_mixture(1500, 128, 4, seed=3, n_query=40),
@@ -55,7 +55,7 @@ CASES = {
                           pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:33",
                                       "vamana", "load:vamana", "search_centroid:64", "vamana", "load:vamana",
                                       "search_rand:25"],
-                                     ["init_random", "nndescent", "ssg"]]),
+                                     ["init_random", "nndescent", "ssg", "load:ssg", "search_sub:40"]]),
     # massive distance ties (values in {0,1,2}, d=16)
     "ties_n1000": dict(data=lambda: tie_heavy(1000, 16, 3, seed=5, nq=40),
                        params=dict(S=12, K=16, L=30, ITER=5, R=20, L_refine=30, R_refine=12, C_refine=60,
@@ -63,21 +63,21 @@ CASES = {
                        pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:20", "search_rand:40",
                                    "vamana", "load:vamana", "search_centroid:24"],
                                   ["init_random", "nndescent", "nsg", "load:nsg", "search_centroid:20"],
-                                  ["init_random", "nndescent", "ssg"]]),
+                                  ["init_random", "nndescent", "ssg", "load:ssg", "search_sub:20"]]),
     # real-valued unit vectors (FP32 summation order matters), d=32
     "unit_n1200": dict(data=lambda: ds.unit_mixture(1200, 32, 20, seed=2, n_query=40),
                        params=dict(S=10, K=20, L=40, ITER=6, R=50, L_refine=40, R_refine=16, C_refine=120,
                                    alpha=1.2, A=60, n_try=10),
                        pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:30",
                                    "vamana", "load:vamana", "search_centroid:30"],
-                                  ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:24"]]),
+                                  ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:24", "search_sub:24"]]),
     # tiny graph: GenRandom wrap-around, self hits, L = N-1 style edges
     "tiny_n60": dict(data=lambda: ds.int_mixture(60, 8, 3, seed=9, n_query=10),
                      params=dict(S=10, K=8, L=16, ITER=4, R=6, L_refine=12, R_refine=6, C_refine=30, alpha=1.2,
                                  A=60, n_try=3),
                      pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:10", "search_rand:20",
                                  "vamana", "load:vamana", "search_centroid:12"],
-                                ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:10"]]),
+                                ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:10", "search_sub:10"]]),
 }
 
 

@@ -85,7 +85,7 @@ def replay_oracle(f, pi, on_search=None, on_graph=None):
             loaded = g
             continue
         else:
-            entry = "rand" if kind == "search_rand" else "centroid"
+            entry = {"search_rand": "rand", "search_centroid": "centroid", "search_sub": "sub_centroid"}[kind]
             L = int(arg)
             got = on_search(entry, L, loaded, rnd) if on_search else O.search(base, query, loaded, L, rnd,
                                                                               entry=entry)

@@ -55,7 +55,7 @@ def _replay(ctx, f, pi):
             ctx.load_built_graph()
             continue
         else:
-            entry = "rand" if kind == "search_rand" else "centroid"
+            entry = {"search_rand": "rand", "search_centroid": "centroid", "search_sub": "sub_centroid"}[kind]
             res, dc, hc = ctx.search(query, int(arg), 10, entry=entry)
             k = f"{key}{kind}_{arg}"
             assert np.array_equal(res, f[k + ".res"]), s
@@ -134,6 +134,18 @@ def test_ssg_matches_oracle_20k(ctx, mix20k, L_refine, R_refine, A, n_try):
     assert rows_equal(ids, dist, deg, gs.ids, gs.dist, gs.deg) == 0, st
     # the rand stream continues where the reference's would
     assert ctx.rand() == ro.next()
+    # the SSG search (sub-centroid entry over the roots), per call and batched
+    ctx.load_built_graph()
+    assert np.array_equal(ctx.get_eps(), gs.eps)
+    L = max(50, n_try)
+    res, dc, hc = ctx.search(query, L, 10, entry="sub_centroid")
+    eres, edc, ehc = O.search(base, query, gs, L, ro, entry="sub_centroid")
+    assert np.array_equal(res, eres) and (dc, hc) == (edc, ehc)
+    Ls = np.full(query.shape[0], L, np.uint32)
+    Ks = np.full(query.shape[0], 10, np.uint32)
+    bres, bdc, bhc = ctx.search_batch(query, Ls, Ks, entry="sub_centroid")
+    eres, edc, ehc = O.search(base, query, gs, L, ro, entry="sub_centroid")
+    assert np.array_equal(bres[:, :10], eres) and (bdc, bhc) == (edc, ehc)
 
 
 def test_ssg_graph_file_and_conn(ctx, mix20k, tmp_path):

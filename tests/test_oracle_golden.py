@@ -59,7 +59,7 @@ def test_oracle_replays_reference(name):
                 loaded = g
                 continue
             elif kind.startswith("search"):
-                entry = "rand" if kind == "search_rand" else "centroid"
+                entry = {"search_rand": "rand", "search_centroid": "centroid", "search_sub": "sub_centroid"}[kind]
                 res, dc, hc = O.search(base, query, loaded, int(arg), rnd, entry=entry)
                 k = f"{key}{kind}_{arg}"
                 assert np.array_equal(res, f[k + ".res"]), (name, s)

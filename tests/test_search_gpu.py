@@ -24,6 +24,15 @@ def test_search_matches_reference_golden(ctx, name):
     checked = 0
 
     def on_search(entry, L, g, rnd):
+        if entry == "sub_centroid":
+            # the GPU draws from the oracle's rand stream (its seed distances
+            # are not those of plain seeds)
+            ctx.upload_graph(g.ids, g.deg, 0, eps=g.eps)
+            ctx.set_rand_source(rnd.next)
+            try:
+                return ctx.search(query, L, 10, entry="sub_centroid")
+            finally:
+                ctx.set_rand_source(None)
         seeds = O.search_seeds(g.n, query.shape[0], g, L, rnd, entry=entry)
         ctx.upload_graph(g.ids, g.deg, g.ep or 0)
         return ctx.search(query, L, 10, entry=seeds)

@@ -101,6 +101,8 @@ def load(build_if_needed: bool = True):
     L.wv_set_stream.argtypes = [vp, vp]
     L.wv_upload_base.argtypes = [vp, f32p, C.c_uint32, C.c_uint32]
     L.wv_upload_graph.argtypes = [vp, u32p, u32p, C.c_uint32, C.c_uint32, C.c_uint32]
+    L.wv_set_eps.argtypes = [vp, vp, C.c_uint32]
+    L.wv_get_eps.argtypes = [vp, C.c_int, vp, C.c_uint32, C.POINTER(C.c_uint32)]
     L.wv_search.argtypes = [vp, f32p, C.c_uint32, C.c_int, C.c_uint32, C.c_uint32, vp, u32p, vp,
                             C.POINTER(Counters)]
     L.wv_search_batch.argtypes = [vp, f32p, C.c_uint32, C.c_int, u32p, u32p, C.c_uint32, u32p, vp,

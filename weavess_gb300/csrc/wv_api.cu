@@ -127,13 +127,14 @@ int wv::search_enqueue(wv_ctx *c, const SearchArgs &a, SearchShape shape, int bl
 // runs the kernel on device-resident queries / seeds / outputs
 int wv::run_search_device(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t *d_seeds, uint32_t seed_stride,
                const uint32_t *d_L, const uint32_t *d_K, uint32_t L, uint32_t K, uint32_t Lmax, uint32_t *d_out,
-               float *d_dist, uint32_t out_stride, wv_counters *counters) {
+               float *d_dist, uint32_t out_stride, wv_counters *counters, bool shift_seeds) {
   const SearchShape sh{};
   int blocks = 0;
   int rc = search_prepare(c, Lmax, sh, &blocks);
   if (rc) return rc;
-  const SearchArgs a =
+  SearchArgs a =
       search_args(c, d_q, nq, nullptr, d_seeds, seed_stride, d_L, d_K, L, K, Lmax, d_out, d_dist, out_stride);
+  a.seed_shift = shift_seeds ? 1 : 0;
   int nb = std::min<long>(blocks, ((long)nq + sh.wpb - 1) / sh.wpb);
   if (nb < 1) nb = 1;
   rc = search_enqueue(c, a, sh, nb);
@@ -162,12 +163,25 @@ int check_search_args(wv_ctx *c, uint32_t nq, uint32_t L, uint32_t K) {
   return WV_OK;
 }
 
+// SearchEntrySubCentroid overwrites the first eps_.size() of L seeds
+// (component_search_entry.cpp:77-80; the reference asserts they fit)
+int check_roots(wv_ctx *c, uint32_t L) {
+  WV_CHECK(c, !c->eps.empty(), WV_ERR_STATE, "sub-centroid entry needs the search graph's SSG roots");
+  WV_CHECK(c, c->eps.size() <= L, WV_ERR_ARG, "%zu SSG roots do not fit L=%u", c->eps.size(), L);
+  return WV_OK;
+}
+
 int draw(wv_ctx *c, uint32_t nq, int entry, uint32_t L, uint32_t *seeds, uint32_t stride) {
   if (entry == WV_ENTRY_RAND) {
     draw_seeds_rand(c->rnd, nq, L, c->n, seeds, stride);
   } else if (entry == WV_ENTRY_CENTROID) {
     WV_CHECK(c, c->gn == c->n, WV_ERR_STATE, "centroid entry needs the search graph");
     draw_seeds_centroid(c->rnd, nq, L, c->n, c->ep_row.data(), (uint32_t)c->ep_row.size(), seeds, stride);
+  } else if (entry == WV_ENTRY_SUB_CENTROID) {
+    int rc = check_roots(c, L);
+    if (rc) return rc;
+    draw_seeds_rand(c->rnd, nq, L, c->n, seeds, stride);
+    for (uint32_t q = 0; q < nq; q++) std::copy(c->eps.begin(), c->eps.end(), seeds + (size_t)q * stride);
   } else {
     return fail(c, WV_ERR_ARG, "unknown entry %d", entry);
   }
@@ -250,8 +264,11 @@ int wv_upload_base(wv_ctx *c, const float *base, uint32_t n, uint32_t d) {
   WV_CHECK(c, (uint64_t)n * d < (1ull << 32), WV_ERR_LIMIT, "n*d=%llu overflows the reference's 32-bit offsets",
            (unsigned long long)n * d);
   WV_CUDA(c, cudaSetDevice(c->device));
-  WV_CUDA(c, c->base.ensure((size_t)n * d * 4));
+  // a zero float follows the last row: SearchEntrySubCentroid reads the row
+  // shifted by one float (component_search_entry.cpp:84-86)
+  WV_CUDA(c, c->base.ensure((size_t)n * d * 4 + 16));
   WV_CUDA(c, cudaMemcpyAsync(c->base.p, base, (size_t)n * d * 4, cudaMemcpyHostToDevice, c->stream));
+  WV_CUDA(c, cudaMemsetAsync(c->base.as<char>() + (size_t)n * d * 4, 0, 16, c->stream));
   WV_CUDA(c, cudaStreamSynchronize(c->stream));
   c->generation++;
   if (c->n != n) c->gn = 0;  // the old graph no longer matches
@@ -298,6 +315,24 @@ int wv_upload_graph(wv_ctx *c, const uint32_t *ids, const uint32_t *deg, uint32_
   return WV_OK;
 }
 
+int wv_set_eps(wv_ctx *c, const uint32_t *eps, uint32_t n_eps) {
+  if (!c) return WV_ERR_ARG;
+  WV_CHECK(c, c->gn == c->n && c->n > 0, WV_ERR_STATE, "upload the search graph first");
+  WV_CHECK(c, n_eps == 0 || eps, WV_ERR_ARG, "null roots");
+  for (uint32_t i = 0; i < n_eps; i++) WV_CHECK(c, eps[i] < c->n, WV_ERR_ARG, "root %u >= n=%u", eps[i], c->n);
+  c->eps.assign(eps, eps + n_eps);
+  c->generation++;
+  return WV_OK;
+}
+
+int wv_get_eps(wv_ctx *c, int built, uint32_t *eps, uint32_t cap, uint32_t *n_eps) {
+  if (!c || !n_eps) return WV_ERR_ARG;
+  const std::vector<uint32_t> &v = built ? c->fg_eps : c->eps;
+  *n_eps = (uint32_t)v.size();
+  if (eps) std::copy(v.begin(), v.begin() + std::min<size_t>(cap, v.size()), eps);
+  return WV_OK;
+}
+
 int wv_draw_seeds(wv_ctx *c, uint32_t nq, int entry, uint32_t L, uint32_t *seeds) {
   if (!c || !seeds) return WV_ERR_ARG;
   WV_CHECK(c, c->n > 0 && L < c->n, WV_ERR_ARG, "L=%u must be smaller than n=%u", L, c->n);
@@ -331,10 +366,18 @@ int wv_search(wv_ctx *c, const float *queries, uint32_t nq, int entry, uint32_t 
   if (entry == WV_ENTRY_SEEDS) {
     WV_CHECK(c, seeds != nullptr, WV_ERR_ARG, "WV_ENTRY_SEEDS needs seeds");
     for (size_t i = 0; i < (size_t)nq * L; i++) WV_CHECK(c, seeds[i] < c->n, WV_ERR_ARG, "seed id %u >= n", seeds[i]);
-  } else if (entry == WV_ENTRY_RAND) {
+  } else if (entry == WV_ENTRY_RAND || entry == WV_ENTRY_SUB_CENTROID) {
     // one rand() per query on the host, the mt19937 draws on the device
+    if (entry == WV_ENTRY_SUB_CENTROID) {
+      rc = check_roots(c, L);
+      if (rc) return rc;
+    }
     rc = draw_seeds_rand_device(c, nq, nullptr, L, L, c->seed_buf.as<uint32_t>(), L);
     if (rc) return rc;
+    if (entry == WV_ENTRY_SUB_CENTROID) {
+      rc = put_roots_device(c, nq, nullptr, c->seed_buf.as<uint32_t>(), L);
+      if (rc) return rc;
+    }
   } else {
     hs.resize((size_t)nq * L);
     rc = draw(c, nq, entry, L, hs.data(), L);
@@ -344,7 +387,8 @@ int wv_search(wv_ctx *c, const float *queries, uint32_t nq, int entry, uint32_t 
   if (seeds)
     WV_CUDA(c, cudaMemcpyAsync(c->seed_buf.p, seeds, (size_t)nq * L * 4, cudaMemcpyHostToDevice, c->stream));
   rc = run_search_device(c, c->q_buf.as<float>(), nq, c->seed_buf.as<uint32_t>(), L, nullptr, nullptr, L, K, L,
-                  c->out_ids_buf.as<uint32_t>(), out_dist ? c->out_dist_buf.as<float>() : nullptr, K, counters);
+                         c->out_ids_buf.as<uint32_t>(), out_dist ? c->out_dist_buf.as<float>() : nullptr, K, counters,
+                         entry == WV_ENTRY_SUB_CENTROID);
   if (rc) return rc;
   WV_CUDA(c, cudaMemcpyAsync(out_ids, c->out_ids_buf.p, (size_t)nq * K * 4, cudaMemcpyDeviceToHost, c->stream));
   if (out_dist)
@@ -357,7 +401,8 @@ int wv_search_batch(wv_ctx *c, const float *queries, uint32_t nq, int entry, con
                     uint32_t out_stride, uint32_t *out_ids, float *out_dist, wv_counters *counters) {
   if (!c) return WV_ERR_ARG;
   WV_CHECK(c, queries && L && K && out_ids, WV_ERR_ARG, "null buffer");
-  WV_CHECK(c, entry == WV_ENTRY_RAND || entry == WV_ENTRY_CENTROID, WV_ERR_ARG, "batch search draws its seeds");
+  WV_CHECK(c, entry == WV_ENTRY_RAND || entry == WV_ENTRY_CENTROID || entry == WV_ENTRY_SUB_CENTROID, WV_ERR_ARG,
+           "batch search draws its seeds");
   if (counters) *counters = wv_counters{0, 0};
   if (nq == 0) return WV_OK;
   uint32_t Lmax = 0;
@@ -365,6 +410,10 @@ int wv_search_batch(wv_ctx *c, const float *queries, uint32_t nq, int entry, con
     int rc = check_search_args(c, nq, L[q], K[q]);
     if (rc) return rc;
     WV_CHECK(c, K[q] <= out_stride, WV_ERR_ARG, "K[%u]=%u > out_stride", q, K[q]);
+    if (entry == WV_ENTRY_SUB_CENTROID) {
+      rc = check_roots(c, L[q]);
+      if (rc) return rc;
+    }
     Lmax = std::max(Lmax, L[q]);
   }
   WV_CUDA(c, cudaSetDevice(c->device));
@@ -380,9 +429,13 @@ int wv_search_batch(wv_ctx *c, const float *queries, uint32_t nq, int entry, con
   // seeds drawn query by query with each query's own L, as the reference's
   // loop would draw them (Rand: one rand() per query, the rest on the device)
   std::vector<uint32_t> hs;
-  if (entry == WV_ENTRY_RAND) {
+  if (entry == WV_ENTRY_RAND || entry == WV_ENTRY_SUB_CENTROID) {
     int rc = draw_seeds_rand_device(c, nq, c->lq_buf.as<uint32_t>(), 0, Lmax, c->seed_buf.as<uint32_t>(), Lmax);
     if (rc) return rc;
+    if (entry == WV_ENTRY_SUB_CENTROID) {
+      rc = put_roots_device(c, nq, nullptr, c->seed_buf.as<uint32_t>(), Lmax);
+      if (rc) return rc;
+    }
   } else {
     hs.resize((size_t)nq * Lmax);
     for (uint32_t q = 0; q < nq; q++) {
@@ -393,7 +446,8 @@ int wv_search_batch(wv_ctx *c, const float *queries, uint32_t nq, int entry, con
   }
   int rc = run_search_device(c, c->q_buf.as<float>(), nq, c->seed_buf.as<uint32_t>(), Lmax, c->lq_buf.as<uint32_t>(),
                       c->kq_buf.as<uint32_t>(), 0, 0, Lmax, c->out_ids_buf.as<uint32_t>(),
-                      out_dist ? c->out_dist_buf.as<float>() : nullptr, out_stride, counters);
+                      out_dist ? c->out_dist_buf.as<float>() : nullptr, out_stride, counters,
+                      entry == WV_ENTRY_SUB_CENTROID);
   if (rc) return rc;
   WV_CUDA(c, cudaMemcpyAsync(out_ids, c->out_ids_buf.p, (size_t)nq * out_stride * 4, cudaMemcpyDeviceToHost,
                              c->stream));

@@ -168,9 +168,10 @@ struct SearchScratch {
 };
 
 // the search kernel on device-resident queries / seeds / outputs (per-query
-// L and K optional); counters (nullable) are read back
+// L and K optional); counters (nullable) are read back.  shift_seeds: seed
+// distances as SearchEntrySubCentroid takes them
 int run_search_device(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t *d_seeds, uint32_t seed_stride,
                       const uint32_t *d_L, const uint32_t *d_K, uint32_t L, uint32_t K, uint32_t Lmax, uint32_t *d_out,
-                      float *d_dist, uint32_t out_stride, wv_counters *counters);
+                      float *d_dist, uint32_t out_stride, wv_counters *counters, bool shift_seeds = false);
 
 }  // namespace wv

@@ -504,6 +504,22 @@ __device__ __forceinline__ float cand_dist(const SearchArgs &a, bool ints, uint3
               : batch_dist<false>(a.base, a.d, my, cnt, qv, lane);
 }
 
+// SearchEntrySubCentroid's seed distance (component_search_entry.cpp:84-89):
+// the row pointer is advanced by one float and d floats are compared from
+// there, in the reference's order (one lane per seed; the last row reads the
+// zero float that follows the base)
+__device__ __forceinline__ float shifted_seed_dist(const float *__restrict__ base, uint32_t d, uint32_t id,
+                                                   const float *qv) {
+  const float *x = base + (size_t)id * d + 1;
+  const float4 *q4 = reinterpret_cast<const float4 *>(qv);
+  float acc = 0.f;
+  for (uint32_t g = 0; g < (d >> 2); g++) {
+    const float4 xv = make_float4(__ldg(x + 4 * g), __ldg(x + 4 * g + 1), __ldg(x + 4 * g + 2), __ldg(x + 4 * g + 3));
+    acc = __fadd_rn(acc, group4(xv, q4[g]));
+  }
+  return acc;
+}
+
 // BUILD = false: SearchEntry* + ROUTER_GREEDY (seeds not marked visited,
 //   DistCount / HopCount kept, top-K written).
 // BUILD = true: CandidateNSG::CandidateInner for base points: seeds are
@@ -566,7 +582,8 @@ __global__ void __maxnreg__(128) k_search(SearchArgs a) {
         set_err(a.status, DEV_BAD_ID);
         id = 0;
       }
-      const float dist = cand_dist(a, ints, id, cnt, s.qv, lane, qn);
+      const float dist = (!BUILD && a.seed_shift) ? (lane < cnt ? shifted_seed_dist(a.base, a.d, id, s.qv) : 0.f)
+                                                 : cand_dist(a, ints, id, cnt, s.qv, lane, qn);
       if (lane < cnt) {
         drawn[b + lane] = DI{dist, id};
         if (BUILD && nvis + lane < a.vlimit) vis_out[nvis + lane] = DI{dist, id};
@@ -645,6 +662,11 @@ __global__ void __maxnreg__(128) k_search(SearchArgs a) {
       // than the pool's last entry, and not a seed (a seed still closer than
       // the last entry is still in the pool: InsertIntoPool rejects it)
       int ncand = 0;
+      // sub-centroid seeds sit in the pool under their shifted distances, so
+      // a returning seed is not simply a duplicate: such expansions replay
+      // InsertIntoPool one candidate at a time (below)
+      const bool shift = !BUILD && a.seed_shift;
+      bool replay = false;
       for (uint32_t b = 0; b < nfresh; b += 32) {
         const int cnt = (int)min(32u, nfresh - b);
         const uint32_t raw = lane < cnt ? s.si[b + lane] : 0u;
@@ -654,8 +676,9 @@ __global__ void __maxnreg__(128) k_search(SearchArgs a) {
           if (lane < cnt && nvis + lane < a.vlimit) vis_out[nvis + lane] = DI{dist, my};
           nvis += cnt;
         }
-        bool acc = lane < cnt && dist < thr && !(raw & SEEDBIT);
-        if (acc && vis.seed_over) {
+        bool acc = lane < cnt && dist < thr && (shift || !(raw & SEEDBIT));
+        if (shift) replay |= __any_sync(FULL, acc && ((raw & SEEDBIT) || vis.seed_over));
+        if (acc && vis.seed_over && !shift) {
           // a seed the hash could not record: look for the id in the pool
           // (same id, same distance: inside the run of equal distances)
           const int lo = lower_bound_of(pd, L, dist), hi = upper_bound_of(pd, L, dist);
@@ -673,7 +696,51 @@ __global__ void __maxnreg__(128) k_search(SearchArgs a) {
       dcount += nfresh;
       __syncwarp();
       int nk = L;
-      if (ncand > 0) {
+      if (ncand > 0 && replay) {
+        // InsertIntoPool (include/weavess/index.h), candidate by candidate in
+        // adjacency order: skipped unless closer than the current last entry;
+        // put in front of a farther first entry unchecked; otherwise placed
+        // after its equal-distance run unless its id is in that run, just
+        // below it, or just above it
+        for (int c = 0; c < ncand; c++) {
+          const float dist = s.cd[c];
+          const uint32_t id = s.ci[c];
+          if (!(dist < pd[L - 1])) continue;
+          int pos = 0;
+          if (!(pd[0] > dist)) {
+            const int ub = upper_bound_of(pd, L, dist), lb = lower_bound_of(pd, L, dist);
+            bool hit = false;
+            for (int t = max(lb - 1, 0) + lane; t <= ub && t < L; t += 32) hit |= (pi[t] & ID_MASK) == id;
+            if (__any_sync(FULL, hit)) continue;
+            pos = ub;
+          }
+          // entries pos..L-2 move up one slot (chunks from the end: each chunk
+          // reads its sources before writing, and no chunk writes a slot a
+          // later chunk still reads)
+          for (int jt = L - 1; jt > pos; jt -= 32) {
+            const int j = jt - lane;
+            const bool act = j > pos;
+            float v = 0.f;
+            uint32_t x = 0;
+            if (act) {
+              v = pd[j - 1];
+              x = pi[j - 1];
+            }
+            __syncwarp();
+            if (act) {
+              pd[j] = v;
+              pi[j] = x;
+            }
+            __syncwarp();
+          }
+          if (lane == 0) {
+            pd[pos] = dist;
+            pi[pos] = id | FLAG;
+          }
+          __syncwarp();
+          nk = min(nk, pos);
+        }
+      } else if (ncand > 0) {
         // stable order of the candidates by distance (adjacency order on ties)
         for (int c = lane; c < ncand; c += 32) {
           const float dc = s.cd[c];

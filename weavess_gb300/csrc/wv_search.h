@@ -43,6 +43,9 @@ struct SearchArgs {
   // their distances by a warp reduction (exact in any order)
   int int_exact;
   const float *xnorm;  // squared norms of the base rows (set when int_exact)
+  // SearchEntrySubCentroid: seed distances to the row shifted by one float
+  // (the base carries a zero float after its last row)
+  int seed_shift;
   // candidate distances from a low-precision copy of the base (0: the FP32
   // base; 1: bf16 rows; 2: fp8 e4m3 rows with a per-row FP32 scale), FP32
   // accumulation; the first `rerank` pool entries are then re-scored exactly

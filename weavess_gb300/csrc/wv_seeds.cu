@@ -13,6 +13,7 @@
 // addr[i] - i, and writes the ids.  Identical to the host draw
 // (wv_host.cpp gen_random) bit for bit.
 #include <cstdint>
+#include <algorithm>
 #include <vector>
 
 #include "wv_common.cuh"
@@ -104,7 +105,31 @@ __global__ void __launch_bounds__(SEED_WARPS * 32)
   }
 }
 
+__global__ void k_put_roots(uint32_t nq, const uint32_t *d_nq, const uint32_t *roots, uint32_t nr, uint32_t *out,
+                            uint32_t stride) {
+  const uint32_t n = d_nq ? min(nq, *d_nq) : nq;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)n * nr; t += (size_t)gridDim.x * blockDim.x)
+    out[(t / nr) * stride + t % nr] = roots[t % nr];
+}
+
 }  // namespace
+
+int put_roots_device(wv_ctx *c, uint32_t nq, const uint32_t *d_nq, uint32_t *d_out, uint32_t stride) {
+  const uint32_t nr = (uint32_t)c->eps.size();
+  WV_CHECK(c, nr > 0, WV_ERR_STATE, "the search graph has no SSG roots");
+  WV_CHECK(c, nr <= stride, WV_ERR_ARG, "%u roots do not fit a seed row of %u", nr, stride);
+  if (nq == 0) return WV_OK;
+  cudaError_t e = cudaSuccess;
+  uint32_t *d_roots = c->buf<uint32_t>("sd_roots", nr, &e);
+  WV_CUDA(c, e);
+  WV_CUDA(c, cudaMemcpyAsync(d_roots, c->eps.data(), (size_t)nr * 4, cudaMemcpyHostToDevice, c->stream));
+  const size_t total = (size_t)nq * nr;
+  const int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)c->sms * 8);
+  k_put_roots<<<blocks, 256, 0, c->stream>>>(nq, d_nq, d_roots, nr, d_out, stride);
+  WV_CUDA(c, cudaGetLastError());
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));  // the roots' host copy may change after this call
+  return WV_OK;
+}
 
 size_t seeds_rand_smem(uint32_t Lmax) { return (size_t)SEED_WARPS * (624 + pow2_ge(Lmax) + 1) * 4; }
 

@@ -24,4 +24,8 @@ cudaError_t seeds_rand_launch(const uint32_t *d_sv, uint32_t nq, const uint32_t 
 int draw_seeds_rand_device(wv_ctx *c, uint32_t nq, const uint32_t *d_L, uint32_t L, uint32_t Lmax, uint32_t *d_out,
                            uint32_t stride);
 
+// SearchEntrySubCentroid: the first n_eps seeds of every query (the first
+// nq, or *d_nq) become the search graph's SSG roots (ctx->eps, uploaded here)
+int put_roots_device(wv_ctx *c, uint32_t nq, const uint32_t *d_nq, uint32_t *d_out, uint32_t stride);
+
 }  // namespace wv

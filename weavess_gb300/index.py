@@ -11,7 +11,8 @@ import numpy as np
 
 from . import _lib
 
-ENTRY = {"rand": 0, "centroid": 1, "seeds": 2}
+ENTRY = {"rand": 0, "centroid": 1, "seeds": 2, "sub_centroid": 3}
+RAND_FN = C.CFUNCTYPE(C.c_int)
 
 
 def _u32(x):
@@ -56,6 +57,12 @@ class Context:
     def srand(self, seed: int):
         self._check(self.L.wv_srand(self.h, seed))
 
+    def set_rand_source(self, fn=None):
+        """Draw rand() values from the callable `fn` (None: the context's own
+        glibc-compatible stream), e.g. to share a process-wide stream."""
+        self._rand_cb = RAND_FN(fn) if fn is not None else None
+        self._check(self.L.wv_set_rand_source(self.h, C.cast(self._rand_cb, C.c_void_p) if fn else None))
+
     def rand(self) -> int:
         v = C.c_int()
         self._check(self.L.wv_rand(self.h, C.byref(v)))
@@ -67,9 +74,21 @@ class Context:
         self._check(self.L.wv_upload_base(self.h, base, base.shape[0], base.shape[1]))
         self.n, self.d = base.shape
 
-    def upload_graph(self, ids: np.ndarray, deg: np.ndarray, ep: int = 0):
+    def upload_graph(self, ids: np.ndarray, deg: np.ndarray, ep: int = 0, eps=None):
+        """The search graph; `eps` are its SSG roots (the sub-centroid entry)."""
         ids = _u32(ids)
         self._check(self.L.wv_upload_graph(self.h, ids, _u32(deg), ids.shape[0], ids.shape[1], int(ep or 0)))
+        if eps is not None:
+            e = _u32(eps)
+            self._check(self.L.wv_set_eps(self.h, e.ctypes.data, len(e)))
+
+    def get_eps(self, built: bool = False) -> np.ndarray:
+        """SSG roots of the built graph (built=True) or of the search graph."""
+        n = C.c_uint32()
+        self._check(self.L.wv_get_eps(self.h, int(built), None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.uint32)
+        self._check(self.L.wv_get_eps(self.h, int(built), out.ctypes.data, n.value, C.byref(n)))
+        return out
 
     # -- build graph (final_graph_)
     def set_graph(self, ids, deg, dist=None, ep=0):
