@@ -119,6 +119,18 @@ int wv_init_random(wv_ctx *ctx, uint32_t S, wv_build_stats *stats);
 int wv_nnd_refine(wv_ctx *ctx, uint32_t S, uint32_t K, uint32_t L, uint32_t ITER, uint32_t R,
                   wv_build_stats *stats);
 
+/* ComponentRefineEFANNA::RefineInner (component_refine.cpp:959-1178) on the
+ * current graph (the KD-tree graph in the reference's EFANNA pipeline; any
+ * graph whose rows hold at most L entries): REFINE_NN_DESCENT's join /
+ * update / PruneNaive, with EFANNA's init -- one rand() seeds an mt19937
+ * from which every node draws 2S random ids as its first nn_new (GenRandom,
+ * node order), and the pools take each row sorted by distance without the
+ * node itself or repeated ids -- so the first join does work.  Result: the
+ * current graph (width K).  Bit-exact with the reference run on one thread;
+ * stats->rand_draws counts the values taken from the rand stream. */
+int wv_efanna_refine(wv_ctx *ctx, uint32_t S, uint32_t K, uint32_t L, uint32_t ITER, uint32_t R,
+                     wv_build_stats *stats);
+
 /* ComponentRefineVAMANA::RefineInner (component_refine.cpp:794-950) on the
  * current graph: entry point (ComponentRefineEntryCentroid), a greedy
  * candidate search of L_refine per node (ComponentCandidateNSG), the alpha
@@ -246,6 +258,7 @@ int wv_draw_seeds_device(wv_ctx *ctx, uint32_t nq, uint32_t L, uint32_t *d_seeds
 #define WV_GRAPH_PLAIN 0 /* no header (KGraph, ...) */
 #define WV_GRAPH_EP 1    /* one entry point ep_ (INDEX_NSG, INDEX_VAMANA) */
 #define WV_GRAPH_EPS 2   /* root count, then the roots eps_ (INDEX_SSG) */
+#define WV_GRAPH_HNSW 3  /* the INDEX_HNSW file (load only, into the HNSW search graph) */
 /* The per-node graph file of IndexBuilder::save_graph / load_graph
  * (src/builder.cpp:918-1095): the header (WV_GRAPH_*), then, per node, its
  * degree and ids (u32 each).  Save writes the built graph (final_graph_);
@@ -268,6 +281,25 @@ typedef struct {
 } wv_index_stats;
 int wv_index_info(wv_ctx *ctx, int use_ep, const uint32_t *exact_ids, const uint32_t *exact_deg,
                   uint32_t exact_width, wv_index_stats *out);
+
+/* ---- HNSW / NSW routing --------------------------------------------------- */
+/* The HNSW search graph, given as the words of the reference's INDEX_HNSW
+ * file (IndexBuilder::save_graph / load_graph, builder.cpp:925-944,
+ * 1096-1124): enterpoint id, max level, then per node its id, its layer
+ * count and per layer the friend count and ids.  Every node of the uploaded
+ * base appears once.  wv_load_graph(ctx, path, WV_GRAPH_HNSW) reads the
+ * file into it. */
+int wv_load_hnsw(wv_ctx *ctx, const uint32_t *words, size_t count);
+/* ComponentSearchRouteHNSW::RouteInner (router 0: greedy descent through
+ * every layer from the enterpoint, then SearchAtLayer on layer 0 from the
+ * path element before the last -- the enterpoint when the path holds only
+ * it, where the reference reads before its path vector) or
+ * ComponentSearchRouteNSW::RouteInner (router 1: SearchAtLayer on layer 0
+ * from node 0), src/component_route.cpp:56-260, for every query, with L as
+ * L_search (L >= K) and K as K_search.  Results equal the reference's,
+ * DistCount / HopCount included (its priority queues are reproduced). */
+int wv_search_hnsw(wv_ctx *ctx, const float *queries, uint32_t nq, int router, uint32_t L, uint32_t K,
+                   uint32_t *out_ids, float *out_dist, wv_counters *counters);
 
 /* ---- batched search plans (CUDA graphs, tuned launch shape) -------------- */
 /* No counterpart in the reference (IndexBuilder::search loops over queries,

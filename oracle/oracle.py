@@ -47,6 +47,9 @@ def lib():
         L.orc_init_random.argtypes = [f32p, C.c_uint, C.c_uint, C.c_uint, C.c_void_p, u32p, f32p, u32p]
         L.orc_nndescent.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint, C.c_uint,
                                     C.c_uint, C.c_uint, C.c_uint, C.c_void_p, C.c_int, u32p, f32p, u32p, u64p]
+        L.orc_efanna.argtypes = L.orc_nndescent.argtypes[:12] + [C.c_void_p, u32p, f32p, u32p, u64p]
+        L.orc_search_hnsw.argtypes = [f32p, C.c_uint, C.c_uint, f32p, C.c_uint, u32p, C.c_size_t, C.c_int, C.c_uint,
+                                      C.c_uint, u32p, u64p]
         L.orc_nndescent_pools.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint,
                                           C.c_uint, C.c_uint, C.c_uint, C.c_void_p, u32p, f32p, u8p, u32p, u32p]
         L.orc_vamana.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint, C.c_uint,
@@ -139,6 +142,22 @@ def nndescent(base, init: Graph, S, K, L, ITER, R, rnd: Rand, threads=1):
     return g
 
 
+def efanna(base, init: Graph, S, K, L, ITER, R, rnd: Rand):
+    """REFINE_EFANNA on `init` (its rows are the KD-tree graph in the
+    reference's pipeline; any graph with rows of at most L entries here)."""
+    base = _c(base, np.float32)
+    n, d = base.shape
+    ids = np.zeros((n, K), np.uint32)
+    dist = np.zeros((n, K), np.float32)
+    deg = np.zeros(n, np.uint32)
+    stats = np.zeros(2, np.uint64)
+    assert lib().orc_efanna(base, n, d, _c(init.ids, np.uint32), _c(init.dist, np.float32), _c(init.deg, np.uint32),
+                            init.width, S, K, L, ITER, R, rnd.h, ids, dist, deg, stats) == 0
+    g = Graph(ids, dist, deg)
+    g.overflow_events = int(stats[0])
+    return g
+
+
 def nndescent_pools(base, init: Graph, S, L, iters, R, rnd: Rand):
     base = _c(base, np.float32)
     n, d = base.shape
@@ -221,6 +240,20 @@ def search(base, query, g: Graph, L, rnd: Rand, entry="rand", K=10, threads=1):
     rc = lib().orc_search(base, n, d, query, nq, _c(g.ids, np.uint32), _c(g.deg, np.uint32), g.width,
                           int(g.ep or 0), ENTRIES[entry], L, K, rnd.h, threads, res, cnt, eps, ne)
     assert rc == 0
+    return res, int(cnt[0]), int(cnt[1])
+
+
+def search_hnsw(base, query, words, L, K=10, router="hnsw"):
+    """ROUTER_HNSW / ROUTER_NSW over a graph in the INDEX_HNSW file layout
+    (a uint32 array); returns (ids nq x K, dist_count, hop_count)."""
+    base, query = _c(base, np.float32), _c(query, np.float32)
+    n, d = base.shape
+    nq = query.shape[0]
+    w = _c(words, np.uint32)
+    res = np.zeros((nq, K), np.uint32)
+    cnt = np.zeros(2, np.uint64)
+    rc = lib().orc_search_hnsw(base, n, d, query, nq, w, w.size, 0 if router == "hnsw" else 1, L, K, res, cnt)
+    assert rc == 0, rc
     return res, int(cnt[0]), int(cnt[1])
 
 

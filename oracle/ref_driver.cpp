@@ -15,8 +15,9 @@
 // deterministic.
 //
 // usage: ref_driver base.fvecs query.fvecs gt.ivecs outprefix key=val ... -- step ...
-//   steps: init_random | init_rand | nndescent | vamana | nsg | ssg | load:<kgraph|vamana|nsg|ssg>
-//          | search_rand:<L> | search_centroid:<L> | search_sub:<L> | rand_probe
+//   steps: init_random | init_rand | nndescent | efanna | vamana | nsg | ssg | load:<kgraph|vamana|nsg|ssg|efanna>
+//          | hnsw | search_rand:<L> | search_centroid:<L> | search_sub:<L> | search_hnsw:<L>
+//          | search_nsw:<L> | rand_probe
 //   (search_sub: SEARCH_ENTRY_SUB_CENTROID, the entry the reference's SSG
 //   test searches with, test/main.cpp:117)
 #include <bits/stdc++.h>
@@ -106,6 +107,46 @@ int main(int argc, char **argv) {
     } else if (step == "nndescent") {
       builder->refine(REFINE_NN_DESCENT, false);
       write_final_graph(prefix + ".nnd.bin", idx, false);
+    } else if (step == "hnsw") {
+      // INIT_HNSW (component_init.cpp:1340-1540; its level rng is seeded per
+      // thread, so one thread makes it deterministic); the graph file the
+      // reference writes for it (save_graph, builder.cpp:925-944) is dumped
+      // byte for byte
+      builder->init(INIT_HNSW, false);
+      std::string gf = prefix + ".hnswgraph.bin";
+      builder->save_graph(INDEX_HNSW, &gf[0]);
+    } else if (step == "search_hnsw" || step == "search_nsw") {
+      // ROUTER_HNSW / ROUTER_NSW (component_route.cpp:56-260) over the graph
+      // as load_graph(INDEX_HNSW) reads it back
+      std::string gf = prefix + ".hnswgraph.bin";
+      builder->load_graph(INDEX_HNSW, &gf[0]);
+      unsigned L = (unsigned)std::stoul(arg);
+      idx->getParam().set<unsigned>("K_search", 10);
+      idx->getParam().set<unsigned>("L_search", L);
+      ComponentSearchRoute *r = step == "search_hnsw" ? (ComponentSearchRoute *)new ComponentSearchRouteHNSW(idx)
+                                                      : (ComponentSearchRoute *)new ComponentSearchRouteNSW(idx);
+      idx->resetDistCount();
+      idx->resetHopCount();
+      unsigned nq = idx->getQueryLen();
+      std::vector<std::vector<unsigned>> res(nq);
+      for (unsigned i = 0; i < nq; i++) {
+        std::vector<Index::Neighbor> pool;
+        r->RouteInner(i, pool, res[i]);
+      }
+      std::string out = prefix + "." + step + "_" + arg + ".bin";
+      FILE *f = fopen(out.c_str(), "wb");
+      fwrite(&nq, 4, 1, f);
+      unsigned k = 10;
+      fwrite(&k, 4, 1, f);
+      for (unsigned i = 0; i < nq; i++) fwrite(res[i].data(), 4, 10, f);
+      unsigned dc = idx->getDistCount(), hc = idx->getHopCount();
+      fwrite(&dc, 4, 1, f);
+      fwrite(&hc, 4, 1, f);
+      fclose(f);
+    } else if (step == "efanna") {
+      // REFINE_EFANNA (component_refine.cpp:959-1178) on the current graph
+      builder->refine(REFINE_EFANNA, false);
+      write_final_graph(prefix + ".efanna.bin", idx, false);
     } else if (step == "vamana") {
       // alpha is set once, at load; the reference itself sets it to 2 at the
       // end of every Vamana link (component_refine.cpp:871)
@@ -128,6 +169,7 @@ int main(int argc, char **argv) {
       TYPE t = arg == "kgraph" ? INDEX_KGRAPH
                : arg == "vamana" ? INDEX_VAMANA
                : arg == "ssg"    ? INDEX_SSG
+               : arg == "efanna" ? INDEX_KGRAPH
                                  : INDEX_NSG;
       std::string gf = prefix + "." + arg + ".graph";
       builder->save_graph(t, &gf[0]);

@@ -20,6 +20,7 @@
 #include <mutex>
 #include <random>
 #include <stack>
+#include <queue>
 #include <vector>
 #include <omp.h>
 
@@ -234,6 +235,32 @@ struct NNDescent {
       graph[i].nn_new.assign(2 * S, 0u);
       graph[i].pool.reserve(L);
       for (auto &nb : fg[i]) graph[i].pool.emplace_back(nb.id, nb.distance, true);
+      std::make_heap(graph[i].pool.begin(), graph[i].pool.end());
+    }
+  }
+
+  // ComponentRefineEFANNA::init (component_refine.cpp:1036-1058): one rand()
+  // seeds an mt19937 from which nhood(L, S, rng, N) (index.h:105-111) draws
+  // 2S random ids into each node's nn_new in node order (GenRandom); the
+  // pool takes the node's row sorted by distance (std::sort), skipping the
+  // node itself and an id equal to its predecessor in that order.  The
+  // first join therefore has work to do.
+  void init_efanna(FinalGraph fg) {
+    std::mt19937 rng(rnd.next());
+    for (unsigned i = 0; i < D.n; i++) {
+      graph[i].M = S;
+      graph[i].nn_new.assign(2 * S, 0u);
+      gen_random(rng, graph[i].nn_new.data(), 2 * S, D.n);
+      graph[i].pool.reserve(L);
+    }
+    for (unsigned i = 0; i < D.n; i++) {
+      auto &ids = fg[i];
+      std::sort(ids.begin(), ids.end());
+      for (unsigned j = 0; j < ids.size(); j++) {
+        const unsigned id = ids[j].id;
+        if (id == i || (j > 0 && id == ids[j - 1].id)) continue;
+        graph[i].pool.emplace_back(id, ids[j].distance, true);
+      }
       std::make_heap(graph[i].pool.begin(), graph[i].pool.end());
     }
   }
@@ -919,9 +946,181 @@ FinalGraph link_ssg(const Data &D, const FinalGraph &g, unsigned Lr, unsigned Rr
   return cut_to_final(cut, D.n, Rr);
 }
 
+// ---------------------------------------------------------------- HNSW / NSW routing
+// The graph as IndexBuilder::load_graph(INDEX_HNSW) reads it (builder.cpp:
+// 1096-1124): enterpoint id, max level, then per node its id, its layer count
+// and, per layer, the friend count and ids.
+struct HnswGraph {
+  unsigned ep = 0, max_level = 0;
+  std::vector<std::vector<std::vector<unsigned>>> fr;  // node -> layer -> friends
+};
+
+bool parse_hnsw(const unsigned *w, size_t count, unsigned n, HnswGraph &g) {
+  size_t p = 0;
+  auto next = [&](unsigned &x) {
+    if (p >= count) return false;
+    x = w[p++];
+    return true;
+  };
+  if (!next(g.ep) || !next(g.max_level)) return false;
+  g.fr.assign(n, std::vector<std::vector<unsigned>>(1));
+  for (unsigned i = 0; i < n; i++) {
+    unsigned id, layers;
+    if (!next(id) || !next(layers) || id >= n) return false;
+    g.fr[id].assign(std::max(layers, 1u), {});
+    for (unsigned l = 0; l < layers; l++) {
+      unsigned gk;
+      if (!next(gk)) return false;
+      g.fr[id][l].resize(gk);
+      for (unsigned k = 0; k < gk; k++)
+        if (!next(g.fr[id][l][k]) || g.fr[id][l][k] >= n) return false;
+    }
+  }
+  return g.ep < n;
+}
+
+struct FurtherFirst {  // Index::FurtherFirst (index.h:435-447)
+  float d;
+  unsigned id;
+  bool operator<(const FurtherFirst &o) const { return d < o.d; }
+};
+struct CloserFirst {  // Index::CloserFirst (index.h:449-459)
+  float d;
+  unsigned id;
+  bool operator<(const CloserFirst &o) const { return d > o.d; }
+};
+
+struct RouteCtx {
+  const Data &D;
+  const HnswGraph &g;
+  const float *q;
+  unsigned L;
+  std::vector<unsigned> visited;  // VisitedList (index.h:461-491): a mark per reset
+  unsigned mark = 0;
+  unsigned long long dc = 0, hc = 0;
+  void reset() { ++mark; }
+};
+
+// SearchAtLayer (component_route.cpp:85-131 and 214-260, the same body)
+void search_at_layer(RouteCtx &c, unsigned entry, unsigned level, std::priority_queue<FurtherFirst> &result) {
+  std::priority_queue<CloserFirst> candidates;
+  float d = l2(c.q, c.D.row(entry), c.D.d);
+  c.dc++;
+  result.push(FurtherFirst{d, entry});
+  candidates.push(CloserFirst{d, entry});
+  c.reset();
+  c.visited[entry] = c.mark;
+  while (!candidates.empty()) {
+    const CloserFirst cand = candidates.top();
+    const float lower_bound = result.top().d;
+    if (cand.d > lower_bound) break;
+    const std::vector<unsigned> &nb = c.g.fr[cand.id][level];
+    candidates.pop();
+    c.hc++;
+    for (unsigned id : nb) {
+      if (c.visited[id] == c.mark) continue;
+      c.visited[id] = c.mark;
+      d = l2(c.q, c.D.row(id), c.D.d);
+      c.dc++;
+      if (result.size() < c.L || result.top().d > d) {
+        result.push(FurtherFirst{d, id});
+        candidates.push(CloserFirst{d, id});
+        if (result.size() > c.L) result.pop();
+      }
+    }
+  }
+}
+
+// the K nearest of `result`, through the CloserFirst queue the reference
+// moves them into (unfilled slots stay 0, as res.resize(K) leaves them)
+void take_k(std::priority_queue<FurtherFirst> &result, unsigned K, unsigned *res) {
+  std::priority_queue<CloserFirst> tmp;
+  while (!result.empty()) {
+    tmp.push(CloserFirst{result.top().d, result.top().id});
+    result.pop();
+  }
+  for (unsigned pos = 0; pos < K; pos++) {
+    res[pos] = 0;
+    if (!tmp.empty()) {
+      res[pos] = tmp.top().id;
+      tmp.pop();
+    }
+  }
+}
+
+// ComponentSearchRouteHNSW::RouteInner (component_route.cpp:134-212): greedy
+// descent from the enterpoint through every layer down to 0 (a fresh visited
+// mark per layer; every improvement appended to the path), then the layer-0
+// search from the path element before the last one.  When the path holds
+// only the enterpoint the reference reads before its vector's start; here
+// the search then starts from the enterpoint.
+void route_hnsw(RouteCtx &c, unsigned K, unsigned *res) {
+  unsigned cur = c.g.ep;
+  float cur_dist = l2(c.q, c.D.row(cur), c.D.d);
+  c.dc++;
+  std::vector<std::pair<unsigned, float>> path{{cur, cur_dist}};
+  for (int i = (int)c.g.max_level; i >= 0; --i) {
+    c.reset();
+    c.visited[cur] = c.mark;
+    bool changed = true;
+    while (changed) {
+      changed = false;
+      const std::vector<unsigned> &nb = c.g.fr[cur][i];
+      c.hc++;
+      for (unsigned id : nb) {
+        if (c.visited[id] == c.mark) continue;
+        c.visited[id] = c.mark;
+        const float d = l2(c.q, c.D.row(id), c.D.d);
+        c.dc++;
+        if (d < cur_dist) {
+          cur_dist = d;
+          cur = id;
+          changed = true;
+          path.emplace_back(cur, cur_dist);
+        }
+      }
+    }
+  }
+  std::priority_queue<FurtherFirst> result;
+  while (result.size() < K && !path.empty()) {
+    path.pop_back();
+    const unsigned entry = path.empty() ? c.g.ep : path.back().first;
+    search_at_layer(c, entry, 0, result);
+  }
+  take_k(result, K, res);
+}
+
+// ComponentSearchRouteNSW::RouteInner (component_route.cpp:56-83): the
+// layer-0 search from node 0
+void route_nsw(RouteCtx &c, unsigned K, unsigned *res) {
+  std::priority_queue<FurtherFirst> result;
+  search_at_layer(c, 0, 0, result);
+  take_k(result, K, res);
+}
+
 }  // namespace
 
 extern "C" {
+
+// ROUTER_HNSW (router 0) / ROUTER_NSW (router 1) over a graph in the
+// INDEX_HNSW file layout (words), every query: res nq x K, counters
+// [dist_count, hop_count]
+int orc_search_hnsw(const float *base, unsigned n, unsigned d, const float *query, unsigned nq, const unsigned *words,
+                    size_t nwords, int router, unsigned L, unsigned K, unsigned *res, unsigned long long *counters) {
+  HnswGraph g;
+  if (!parse_hnsw(words, nwords, n, g)) return -1;
+  if (g.max_level >= g.fr[g.ep].size() && router == 0) return -2;
+  Data D{base, n, d};
+  RouteCtx c{D, g, nullptr, L, std::vector<unsigned>(n, 0u)};
+  for (unsigned q = 0; q < nq; q++) {
+    c.q = query + (size_t)q * d;
+    if (router == 0) route_hnsw(c, K, res + (size_t)q * K);
+    else route_nsw(c, K, res + (size_t)q * K);
+  }
+  counters[0] = c.dc;
+  counters[1] = c.hc;
+  return 0;
+}
 
 void *orc_rand_create(unsigned seed) { return new GlibcRand(seed); }
 void orc_rand_destroy(void *r) { delete (GlibcRand *)r; }
@@ -952,6 +1151,28 @@ int orc_nndescent(const float *base, unsigned n, unsigned d, const unsigned *in_
   FinalGraph init = graph_from_arrays(in_ids, in_dist, in_deg, n, in_w);
   NNDescent nd(D, S, K, L, ITER, R, *(GlibcRand *)rnd, threads < 1 ? 1 : threads);
   nd.init(init);
+  for (unsigned it = 0; it < ITER; it++) {
+    nd.join();
+    nd.update();
+  }
+  FinalGraph fg = nd.finish();
+  if (stats) stats[0] = nd.overflow_events;
+  return graph_to_arrays(fg, ids, dist, deg, K);
+}
+
+// REFINE_EFANNA (component_refine.cpp:959-1178) from a given init graph: the
+// NN-Descent of REFINE_NN_DESCENT with EFANNA's init; out rows of width K.
+// Init rows longer than L are refused (the reference's pool would outgrow
+// its reserved capacity).
+int orc_efanna(const float *base, unsigned n, unsigned d, const unsigned *in_ids, const float *in_dist,
+               const unsigned *in_deg, unsigned in_w, unsigned S, unsigned K, unsigned L, unsigned ITER, unsigned R,
+               void *rnd, unsigned *ids, float *dist, unsigned *deg, unsigned long long *stats) {
+  Data D{base, n, d};
+  for (unsigned i = 0; i < n; i++)
+    if (in_deg[i] > L) return -1;
+  FinalGraph init = graph_from_arrays(in_ids, in_dist, in_deg, n, in_w);
+  NNDescent nd(D, S, K, L, ITER, R, *(GlibcRand *)rnd, 1);
+  nd.init_efanna(init);
   for (unsigned it = 0; it < ITER; it++) {
     nd.join();
     nd.update();

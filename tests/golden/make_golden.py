@@ -6,8 +6,8 @@ seeded inputs.  Run from the repository root:
 
 Each fixture is an .npz holding the inputs (base / query vectors) and every
 output the reference driver dumped: the INIT_RANDOM graph, the NN-Descent
-graph, the Vamana / NSG graphs (with entry point), the SSG graph (with its
-random roots) and greedy-search result
+graph, the EFANNA-refined graph, the Vamana / NSG graphs (with entry point), the SSG graph (with its
+random roots), the HNSW graph (the reference's INDEX_HNSW file, as words) and search result
 ids plus DistCount / HopCount for the listed beam widths.  The oracle is
 checked against these by tests/test_oracle_golden.py, and the GPU path
 against the oracle by the gpu tests.
@@ -41,12 +41,15 @@ CASES = {
     # overflow active (R=100 < in-degree of hubs)
     "int_n2000": dict(data=lambda: ds.int_mixture(2000, 128, 8, seed=1, n_query=50),
                       params=dict(S=10, K=20, L=40, ITER=8, R=100, L_refine=40, R_refine=16, C_refine=200,
-                                  alpha=1.2, A=60, n_try=5),
+                                  alpha=1.2, A=60, n_try=5, max_m=8, max_m0=16, ef_construction=40, mult=0,
+                                  n_threads=1),
                       pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:20", "search_rand:50",
                                   "vamana", "load:vamana", "search_centroid:30", "search_rand:17"],
                                  ["init_random", "nndescent", "nsg", "load:nsg", "search_centroid:30",
                                   "search_rand:40"],
-                                 ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:30", "search_sub:30"]]),
+                                 ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:30", "search_sub:30"],
+                                 ["init_random", "efanna", "load:efanna", "search_rand:30"],
+                                 ["hnsw", "search_hnsw:20", "search_hnsw:50", "search_nsw:30"]]),
     # S > 16 and L_refine > K: introsort on ties, rand() seed fill in the
     # candidate search, heavy reverse-list overflow (R=12)
     "int_n1500_s20": dict(data=lambda: ds.int_mixture(1500, 128, 4, seed=3, n_query=40),
@@ -59,25 +62,33 @@ CASES = {
     # massive distance ties (values in {0,1,2}, d=16)
     "ties_n1000": dict(data=lambda: tie_heavy(1000, 16, 3, seed=5, nq=40),
                        params=dict(S=12, K=16, L=30, ITER=5, R=20, L_refine=30, R_refine=12, C_refine=60,
-                                   alpha=1.2, A=60, n_try=4),
+                                   alpha=1.2, A=60, n_try=4, max_m=6, max_m0=12, ef_construction=30, mult=0,
+                                   n_threads=1),
                        pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:20", "search_rand:40",
                                    "vamana", "load:vamana", "search_centroid:24"],
                                   ["init_random", "nndescent", "nsg", "load:nsg", "search_centroid:20"],
-                                  ["init_random", "nndescent", "ssg", "load:ssg", "search_sub:20"]]),
+                                  ["init_random", "nndescent", "ssg", "load:ssg", "search_sub:20"],
+                                  ["init_random", "efanna"],
+                                  ["hnsw", "search_hnsw:16", "search_nsw:24"]]),
     # real-valued unit vectors (FP32 summation order matters), d=32
     "unit_n1200": dict(data=lambda: ds.unit_mixture(1200, 32, 20, seed=2, n_query=40),
                        params=dict(S=10, K=20, L=40, ITER=6, R=50, L_refine=40, R_refine=16, C_refine=120,
-                                   alpha=1.2, A=60, n_try=10),
+                                   alpha=1.2, A=60, n_try=10, max_m=8, max_m0=16, ef_construction=40, mult=0,
+                                   n_threads=1),
                        pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:30",
                                    "vamana", "load:vamana", "search_centroid:30"],
-                                  ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:24", "search_sub:24"]]),
+                                  ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:24", "search_sub:24"],
+                                  ["init_random", "efanna", "load:efanna", "search_rand:20"],
+                                  ["hnsw", "search_hnsw:24", "search_nsw:24"]]),
     # tiny graph: GenRandom wrap-around, self hits, L = N-1 style edges
     "tiny_n60": dict(data=lambda: ds.int_mixture(60, 8, 3, seed=9, n_query=10),
                      params=dict(S=10, K=8, L=16, ITER=4, R=6, L_refine=12, R_refine=6, C_refine=30, alpha=1.2,
-                                 A=60, n_try=3),
+                                 A=60, n_try=3, max_m=4, max_m0=8, ef_construction=16, mult=0, n_threads=1),
                      pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:10", "search_rand:20",
                                  "vamana", "load:vamana", "search_centroid:12"],
-                                ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:10", "search_sub:10"]]),
+                                ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:10", "search_sub:10"],
+                                ["init_random", "efanna"],
+                                ["hnsw", "search_hnsw:10", "search_hnsw:30", "search_nsw:12"]]),
 }
 
 
@@ -117,7 +128,9 @@ def run_case(name, spec):
                 if not f.startswith(f"p{pi}.") or not f.endswith(".bin"):
                     continue
                 key = f[: -len(".bin")]
-                if key.endswith(".ssgeps"):
+                if key.endswith(".hnswgraph"):
+                    out[f"p{pi}.hnsw.words"] = np.fromfile(os.path.join(tmp, f), np.uint32)
+                elif key.endswith(".ssgeps"):
                     out[key[: -len("eps")] + ".eps"] = np.fromfile(os.path.join(tmp, f), np.uint32)[1:]
                 elif "search" in key:
                     res, dc, hc = O.read_search_dump(os.path.join(tmp, f))

@@ -78,11 +78,23 @@ def replay_oracle(f, pi, on_search=None, on_graph=None):
             g = O.nsg(base, g, p["L_refine"], p["R_refine"], p["C_refine"], rnd)
             entry_L = p["L_refine"]
             exp = key + "nsg"
+        elif kind == "efanna":
+            g = O.efanna(base, g, p["S"], p["K"], p["L"], p["ITER"], p["R"], rnd)
+            exp = key + "efanna"
         elif kind == "ssg":
             g = O.ssg(base, g, p["L_refine"], p["R_refine"], float(p["A"]), p["n_try"], rnd)
             exp = key + "ssg"
         elif kind == "load":
             loaded = g
+            continue
+        elif kind == "hnsw":
+            hwords = f[key + "hnsw.words"]
+            continue
+        elif kind in ("search_hnsw", "search_nsw"):
+            router, L = kind[len("search_"):], int(arg)
+            got = (on_search(router, L, hwords, rnd) if on_search
+                   else O.search_hnsw(base, query, hwords, L, router=router))
+            yield s, f"{key}{kind}_{arg}", got
             continue
         else:
             entry = {"search_rand": "rand", "search_centroid": "centroid", "search_sub": "sub_centroid"}[kind]

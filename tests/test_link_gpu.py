@@ -47,6 +47,9 @@ def _replay(ctx, f, pi):
             ctx.nsg_refine(p["L_refine"], p["R_refine"], p["C_refine"])
             entry_L = p["L_refine"]
             exp = key + "nsg"
+        elif kind == "efanna":
+            ctx.efanna_refine(p["S"], p["K"], p["L"], p["ITER"], p["R"])
+            exp = key + "efanna"
         elif kind == "ssg":
             st = ctx.ssg_refine(p["L_refine"], p["R_refine"], float(p["A"]), p["n_try"])
             exp = key + "ssg"
@@ -74,7 +77,9 @@ def _replay(ctx, f, pi):
 @pytest.mark.parametrize("name", cases())
 def test_full_pipelines_match_reference_golden(ctx, name):
     f = load(name)
-    for pi in range(len(f["pipelines"])):
+    for pi, steps in enumerate(f["pipelines"]):
+        if steps[0] == "hnsw":
+            continue  # HNSW routing over the reference's graph: tests/test_hnsw_gpu.py
         assert _replay(ctx, f, pi)
 
 

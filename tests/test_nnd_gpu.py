@@ -74,3 +74,20 @@ def test_nndescent_unit_vectors_exact_fp32(ctx):
     ctx.nnd_refine(12, 16, 32, 5, 24)
     ids, dist, deg, _ = ctx.get_graph()
     assert rows_equal(ids, dist, deg, g.ids, g.dist, g.deg) == 0
+
+
+@pytest.mark.parametrize("S,L,R", [(10, 40, 50), (16, 48, 12), (4, 24, 100)])
+def test_efanna_matches_oracle_20k(ctx, mix20k, S, L, R):
+    """REFINE_EFANNA (random first nn_new, sorted de-duplicated pools, live
+    first join) on an INIT_RANDOM graph: every row and the rand stream."""
+    base, _ = mix20k
+    ctx.upload_base(base)
+    ctx.srand(1)
+    ctx.init_random(S)
+    st = ctx.efanna_refine(S, 24, L, 6, R)
+    ro = O.Rand(1)
+    ge = O.efanna(base, O.init_random(base, S, ro), S, 24, L, 6, R, ro)
+    ids, dist, deg, _ = ctx.get_graph()
+    assert rows_equal(ids, dist, deg, ge.ids, ge.dist, ge.deg) == 0, st
+    assert st["rand_draws"] == 1 + ge.overflow_events
+    assert ctx.rand() == ro.next()

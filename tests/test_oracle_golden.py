@@ -51,12 +51,24 @@ def test_oracle_replays_reference(name):
                 g = O.nsg(base, g, p["L_refine"], p["R_refine"], p["C_refine"], rnd)
                 entry_L = p["L_refine"]
                 exp = graph_of(f, key + "nsg")
+            elif kind == "efanna":
+                g = O.efanna(base, g, p["S"], p["K"], p["L"], p["ITER"], p["R"], rnd)
+                exp = graph_of(f, key + "efanna")
             elif kind == "ssg":
                 g = O.ssg(base, g, p["L_refine"], p["R_refine"], float(p["A"]), p["n_try"], rnd)
                 exp = graph_of(f, key + "ssg")
                 assert np.array_equal(g.eps, f[key + "ssg.eps"]), (name, s)
             elif kind == "load":
                 loaded = g
+                continue
+            elif kind == "hnsw":
+                hwords = f[key + "hnsw.words"]
+                continue
+            elif kind in ("search_hnsw", "search_nsw"):
+                res, dc, hc = O.search_hnsw(base, query, hwords, int(arg), router=kind[len("search_"):])
+                k = f"{key}{kind}_{arg}"
+                assert np.array_equal(res, f[k + ".res"]), (name, s)
+                assert [dc, hc] == f[k + ".counts"].tolist(), (name, s)
                 continue
             elif kind.startswith("search"):
                 entry = {"search_rand": "rand", "search_centroid": "centroid", "search_sub": "sub_centroid"}[kind]

@@ -24,6 +24,9 @@ def test_search_matches_reference_golden(ctx, name):
     checked = 0
 
     def on_search(entry, L, g, rnd):
+        if entry in ("hnsw", "nsw"):  # g: the reference's INDEX_HNSW file, as words
+            ctx.load_hnsw(g)
+            return ctx.search_hnsw(query, L, 10, router=entry)
         if entry == "sub_centroid":
             # the GPU draws from the oracle's rand stream (its seed distances
             # are not those of plain seeds)

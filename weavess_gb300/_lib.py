@@ -102,6 +102,9 @@ def load(build_if_needed: bool = True):
     L.wv_upload_base.argtypes = [vp, f32p, C.c_uint32, C.c_uint32]
     L.wv_upload_graph.argtypes = [vp, u32p, u32p, C.c_uint32, C.c_uint32, C.c_uint32]
     L.wv_set_eps.argtypes = [vp, vp, C.c_uint32]
+    L.wv_load_hnsw.argtypes = [vp, u32p, C.c_size_t]
+    L.wv_search_hnsw.argtypes = [vp, f32p, C.c_uint32, C.c_int, C.c_uint32, C.c_uint32, u32p, vp,
+                                 C.POINTER(Counters)]
     L.wv_get_eps.argtypes = [vp, C.c_int, vp, C.c_uint32, C.POINTER(C.c_uint32)]
     L.wv_search.argtypes = [vp, f32p, C.c_uint32, C.c_int, C.c_uint32, C.c_uint32, vp, u32p, vp,
                             C.POINTER(Counters)]
@@ -118,6 +121,8 @@ def load(build_if_needed: bool = True):
     L.wv_nnd_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                 C.POINTER(BuildStats)]
     L.wv_vamana_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, C.POINTER(BuildStats)]
+    L.wv_efanna_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                   C.POINTER(BuildStats)]
     L.wv_nsg_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(BuildStats)]
     L.wv_ssg_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, vp, C.POINTER(BuildStats)]
     L.wv_set_search_precision.argtypes = [vp, C.c_int, C.c_uint32]

@@ -118,6 +118,29 @@ int wv_nnd_refine(wv_ctx *c, uint32_t S, uint32_t K, uint32_t L, uint32_t ITER, 
   return rc;
 }
 
+int wv_efanna_refine(wv_ctx *c, uint32_t S, uint32_t K, uint32_t L, uint32_t ITER, uint32_t R,
+                     wv_build_stats *stats) {
+  if (!c) return WV_ERR_ARG;
+  WV_CUDA(c, cudaSetDevice(c->device));
+  auto t0 = std::chrono::steady_clock::now();
+  const unsigned long long d0 = c->rnd.drawn;
+  NndStats st;
+  NndParams np{S, K, L, ITER, R};
+  np.efanna = true;
+  int rc = nndescent_gpu(c, np, &st);
+  if (stats) {
+    *stats = wv_build_stats{};
+    stats->rand_draws = c->rnd.drawn - d0;
+    stats->offers = st.offers;
+    stats->pairs = st.pairs;
+    stats->chunks = st.chunks;
+    stats->ms_join = st.ms_join;
+    stats->ms_update = st.ms_update;
+    stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return rc;
+}
+
 int wv_vamana_refine(wv_ctx *c, uint32_t L_refine, uint32_t R_refine, float alpha, uint32_t entry_L,
                      wv_build_stats *stats) {
   if (!c) return WV_ERR_ARG;

@@ -80,6 +80,12 @@ struct wv_ctx {
   bool fg_has_ep = false;
   std::vector<uint32_t> fg_eps;  // SSG roots of the built graph (eps_)
 
+  // HNSW / NSW search graph (wv_hnsw.cu): layer-0 rows and the upper layers
+  // in named work buffers; n = 0 while none is loaded
+  struct {
+    uint32_t n = 0, w0 = 0, wu = 0, ep = 0, max_level = 0, ep_layers = 0;
+  } hnsw;
+
   // learned entry / beam model (wv_learn.cu), or null
   void *learn = nullptr;
 

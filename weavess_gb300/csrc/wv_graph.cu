@@ -93,6 +93,14 @@ int wv_load_graph(wv_ctx *c, const char *path, int with_ep) {
   WV_CHECK(c, c->n > 0, WV_ERR_STATE, "upload the base first (the graph's node count must match it)");
   FILE *f = fopen(path, "rb");
   WV_CHECK(c, f, WV_ERR_ARG, "cannot open %s", path);
+  if (with_ep == WV_GRAPH_HNSW) {  // the whole file, as words
+    std::vector<uint32_t> w;
+    uint32_t buf[4096];
+    size_t got;
+    while ((got = fread(buf, 4, 4096, f)) > 0) w.insert(w.end(), buf, buf + got);
+    fclose(f);
+    return wv_load_hnsw(c, w.data(), w.size());
+  }
   uint32_t ep = 0;
   std::vector<uint32_t> eps;
   if (with_ep == WV_GRAPH_EPS) {

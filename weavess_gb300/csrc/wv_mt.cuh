@@ -69,4 +69,55 @@ __device__ __forceinline__ void mt_twist_warp(uint32_t *mt, int lane) {
   __syncwarp();
 }
 
+__host__ __device__ inline uint32_t pow2_ge(uint32_t x) {
+  uint32_t p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+// The tail of GenRandom (include/weavess/util.h:13-27) for one warp: key[0..L)
+// holds the residues rng() % (N - L) in draw order (key has room for
+// pow2_ge(L) words); they are sorted ascending, each one that does not exceed
+// its predecessor becomes predecessor + 1 -- a_i = max(v_i, a_{i-1} + 1) =
+// i + max_{j <= i}(v_j - j), a prefix maximum -- and (a_i + off) % N is
+// written to out[i].  Integer keys: any correct sort gives std::sort's order.
+__device__ inline void warp_gen_random_tail(uint32_t *key, uint32_t L, uint32_t off, uint32_t N, uint32_t *out,
+                                            int lane) {
+  const uint32_t P = pow2_ge(L);
+  for (uint32_t i = L + lane; i < P; i += 32) key[i] = 0xffffffffu;
+  __syncwarp();
+  // ascending bitonic sort of key[0..P)
+  for (uint32_t k = 2; k <= P; k <<= 1)
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = lane; i < P; i += 32) {
+        const uint32_t l = i ^ j;
+        if (l > i) {
+          const uint32_t a = key[i], b = key[l];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            key[i] = b;
+            key[l] = a;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  long long carry = -(1ll << 40);
+  for (uint32_t b = 0; b < L; b += 32) {
+    const uint32_t i = b + lane;
+    long long m = i < L ? (long long)key[i] - (long long)i : -(1ll << 40);
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, m, o);
+      if (lane >= o) m = max(m, y);
+    }
+    m = max(m, carry);
+    carry = __shfl_sync(0xffffffffu, m, 31);
+    if (i < L) {
+      const unsigned long long a = (unsigned long long)(m + (long long)i);
+      out[i] = (uint32_t)((a + off) % N);
+    }
+  }
+  __syncwarp();
+}
+
 }  // namespace wv

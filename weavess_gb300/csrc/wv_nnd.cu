@@ -172,18 +172,54 @@ struct Nnd {
   float *maxd, *hback;
 };
 
-// init(): pools <- init rows (flag true), make_heap; M = S
-__global__ void k_nnd_init(Nnd s, const uint32_t *ids, const float *dist, const uint32_t *deg, uint32_t w) {
+// init(): pools <- init rows (flag true), make_heap; M = S.
+// efanna: ComponentRefineEFANNA::init (component_refine.cpp:1044-1057) sorts
+// the row by distance (std::sort) and skips the node itself and an id equal
+// to its predecessor in that order
+__global__ void k_nnd_init(Nnd s, const uint32_t *ids, const float *dist, const uint32_t *deg, uint32_t w,
+                           int efanna) {
   extern __shared__ __align__(16) uint8_t smem[];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   Ent *P = (Ent *)smem + (size_t)threadIdx.x * (s.L + 1);
   if (i >= s.n) return;
   uint32_t sz = min(deg[i], s.L);
   for (uint32_t j = 0; j < sz; j++) P[j] = Ent{dist[(size_t)i * w + j], ids[(size_t)i * w + j] | FLAG};
+  if (efanna) {
+    stl::sort(P, (int)sz, EntLess());
+    uint32_t k = 0, prev = 0;
+    for (uint32_t t = 0; t < sz; t++) {
+      const uint32_t id = P[t].idf & ID_MASK;
+      const bool skip = id == i || (t > 0 && id == prev);
+      prev = id;
+      if (!skip) P[k++] = P[t];
+    }
+    sz = k;
+  }
   stl::make_heap(P, (int)sz, EntLess());
   for (uint32_t j = 0; j < sz; j++) s.pool[(size_t)i * s.L + j] = P[j];
   s.psz[i] = sz;
   s.M[i] = s.S;
+}
+
+// nhood(L, S, rng, N) (index.h:105-111) for every node: nn_new = GenRandom of
+// 2S ids from the shared mt19937 stream (node i reads outputs
+// [i (2S + 1), (i + 1)(2S + 1))), nn_old empty.  A warp per node.
+constexpr int EF_WARPS = 4;
+__global__ void __launch_bounds__(EF_WARPS * 32) k_efanna_nnew(Nnd s, const uint32_t *mtv) {
+  extern __shared__ uint32_t ef_key[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t L2 = 2 * s.S;
+  uint32_t *key = ef_key + (size_t)warp * pow2_ge(L2);
+  for (uint32_t i = blockIdx.x * EF_WARPS + warp; i < s.n; i += gridDim.x * EF_WARPS) {
+    const uint32_t *r = mtv + (size_t)i * (L2 + 1);
+    for (uint32_t j = lane; j < L2; j += 32) key[j] = r[j] % (s.n - L2);
+    __syncwarp();
+    warp_gen_random_tail(key, L2, r[L2] % s.n, s.n, s.nnew + (size_t)i * s.capn, lane);
+    if (lane == 0) {
+      s.lnew[i] = L2;
+      s.lold[i] = 0;
+    }
+  }
 }
 
 // update() passes 1-3 for node i: sort, sampled prefix M, new/old lists from
@@ -690,7 +726,7 @@ int nndescent_gpu(wv_ctx *c, const NndParams &p, NndStats *st) {
   s.K = p.K;
   s.L = p.L;
   s.R = p.R;
-  s.capn = p.S + p.R;
+  s.capn = std::max(p.S + p.R, 2 * p.S);  // EFANNA's first nn_new holds 2S ids
   s.capo = std::min(p.L + p.R, 2 * p.R);
   s.base = c->base.as<float>();
   s.pool = c->buf<Ent>("pool", (size_t)n * p.L, &e);
@@ -750,8 +786,28 @@ int nndescent_gpu(wv_ctx *c, const NndParams &p, NndStats *st) {
   WV_CUDA(c, cudaFuncSetAttribute(k_nnd_init, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)node_smem));
   WV_CUDA(c, cudaFuncSetAttribute(k_upd_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)node_smem));
   WV_CUDA(c, cudaFuncSetAttribute(k_nnd_final, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)node_smem));
+  if (p.efanna) {
+    // one rand() seeds the mt19937 the nhoods draw their first nn_new from
+    WV_CHECK(c, 2ull * p.S < n, WV_ERR_ARG, "EFANNA needs 2S < n (S=%u, n=%u)", p.S, n);
+    std::vector<uint32_t> hdeg(n);
+    WV_CUDA(c, cudaMemcpyAsync(hdeg.data(), c->fg_deg.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (uint32_t i = 0; i < n; i++)
+      WV_CHECK(c, hdeg[i] <= p.L, WV_ERR_LIMIT, "init row %u has %u entries > L=%u (the pool would outgrow L)", i,
+               hdeg[i], p.L);
+    const uint32_t seed = (uint32_t)c->rnd.next();
+    const size_t count = (size_t)n * (2 * p.S + 1);
+    uint32_t *mtv = c->buf<uint32_t>("ef_mt", count, &e);
+    WV_CUDA(c, e);
+    int rc = mt19937_gpu(c, seed, mtv, count);
+    if (rc) return rc;
+    const size_t ef_smem = (size_t)EF_WARPS * pow2_ge(2 * p.S) * 4;
+    WV_CUDA(c, cudaFuncSetAttribute(k_efanna_nnew, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ef_smem));
+    k_efanna_nnew<<<c->sms * 8, EF_WARPS * 32, ef_smem, c->stream>>>(s, mtv);
+    WV_CUDA(c, cudaGetLastError());
+  }
   k_nnd_init<<<nb, NODE_THREADS, node_smem, c->stream>>>(s, c->fg_ids.as<uint32_t>(), c->fg_dist.as<float>(),
-                                                          c->fg_deg.as<uint32_t>(), c->fg_w);
+                                                          c->fg_deg.as<uint32_t>(), c->fg_w, p.efanna ? 1 : 0);
   WV_CUDA(c, cudaGetLastError());
 
   const uint32_t stride = ((c->d + 3) & ~3u) + 4;
@@ -769,7 +825,8 @@ int nndescent_gpu(wv_ctx *c, const NndParams &p, NndStats *st) {
   std::vector<uint32_t> h_lnew(n), h_lold(n);
   for (uint32_t it = 0; it < p.ITER; it++) {
     // ------------------------------------------------------------ join
-    if (it > 0) {
+    // (NN_DESCENT's first join pairs 2S zero ids -- nothing; EFANNA's is live)
+    if (it > 0 || p.efanna) {
       cudaEventRecord(ev0, c->stream);
       WV_CUDA(c, cudaMemcpyAsync(h_lnew.data(), s.lnew, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
       WV_CUDA(c, cudaMemcpyAsync(h_lold.data(), s.lold, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));

@@ -8,6 +8,9 @@ namespace wv {
 
 struct NndParams {
   uint32_t S, K, L, ITER, R;
+  // ComponentRefineEFANNA's init (random nn_new, sorted de-duplicated pools)
+  // instead of ComponentRefineNNDescent's
+  bool efanna = false;
 };
 
 struct NndStats {
@@ -20,7 +23,8 @@ struct NndStats {
 
 // ComponentInitRandom::InitInner: rows of width S into ctx->fg_*
 int init_random_gpu(wv_ctx *c, uint32_t S);
-// ComponentRefineNNDescent::RefineInner: ctx->fg_* (init graph) -> ctx->fg_* (width K)
+// ComponentRefineNNDescent::RefineInner / ComponentRefineEFANNA::RefineInner:
+// ctx->fg_* (init graph) -> ctx->fg_* (width K)
 int nndescent_gpu(wv_ctx *c, const NndParams &p, NndStats *st);
 // mt19937 outputs [0, count) for `seed` (tests)
 int mt19937_gpu(wv_ctx *c, uint32_t seed, uint32_t *d_out, size_t count);

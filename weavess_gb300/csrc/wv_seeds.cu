@@ -26,12 +26,6 @@ namespace {
 
 constexpr int SEED_WARPS = 4;
 
-__host__ __device__ inline uint32_t pow2_ge(uint32_t x) {
-  uint32_t p = 1;
-  while (p < x) p <<= 1;
-  return p;
-}
-
 __global__ void __launch_bounds__(SEED_WARPS * 32)
     k_seeds_rand(const uint32_t *sv, uint32_t nq, const uint32_t *nq_dev, const uint32_t *Lq, uint32_t L0,
                  uint32_t Lmax, uint32_t N, uint32_t *out, uint32_t stride, int *status) {
@@ -47,7 +41,6 @@ __global__ void __launch_bounds__(SEED_WARPS * 32)
     if (lane == 0) set_err(status, DEV_OVERFLOW);
     return;
   }
-  const uint32_t P = pow2_ge(L);
   if (lane == 0) {
     uint32_t x = sv[q];
     mt[0] = x;
@@ -69,40 +62,7 @@ __global__ void __launch_bounds__(SEED_WARPS * 32)
   }
   const uint32_t off = key[L];
   __syncwarp();
-  for (uint32_t i = L + lane; i < P; i += 32) key[i] = 0xffffffffu;
-  __syncwarp();
-  // ascending bitonic sort of key[0..P)
-  for (uint32_t k = 2; k <= P; k <<= 1)
-    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-      for (uint32_t i = lane; i < P; i += 32) {
-        const uint32_t l = i ^ j;
-        if (l > i) {
-          const uint32_t a = key[i], b = key[l];
-          const bool up = (i & k) == 0;
-          if ((a > b) == up) {
-            key[i] = b;
-            key[l] = a;
-          }
-        }
-      }
-      __syncwarp();
-    }
-  // a_i = max(v_i, a_{i-1} + 1) = i + max_{j <= i} (v_j - j); then + off mod N
-  long long carry = -(1ll << 40);
-  for (uint32_t b = 0; b < L; b += 32) {
-    const uint32_t i = b + lane;
-    long long m = i < L ? (long long)key[i] - (long long)i : -(1ll << 40);
-    for (int o = 1; o < 32; o <<= 1) {
-      const long long y = __shfl_up_sync(FULL, m, o);
-      if (lane >= o) m = max(m, y);
-    }
-    m = max(m, carry);
-    carry = __shfl_sync(FULL, m, 31);
-    if (i < L) {
-      const unsigned long long a = (unsigned long long)(m + (long long)i);
-      out[(size_t)q * stride + i] = (uint32_t)((a + off) % N);
-    }
-  }
+  warp_gen_random_tail(key, L, off, N, out + (size_t)q * stride, lane);
 }
 
 __global__ void k_put_roots(uint32_t nq, const uint32_t *d_nq, const uint32_t *roots, uint32_t nr, uint32_t *out,

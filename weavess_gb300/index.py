@@ -82,6 +82,26 @@ class Context:
             e = _u32(eps)
             self._check(self.L.wv_set_eps(self.h, e.ctypes.data, len(e)))
 
+    # -- HNSW / NSW routing over the reference's INDEX_HNSW graph
+    def load_hnsw(self, words: np.ndarray):
+        """The HNSW search graph from the words of an INDEX_HNSW file."""
+        w = _u32(np.asarray(words).reshape(-1))
+        self._check(self.L.wv_load_hnsw(self.h, w, w.size))
+
+    def search_hnsw(self, queries, L: int, K: int = 10, router: str = "hnsw", return_dist=False):
+        """ROUTER_HNSW / ROUTER_NSW; returns (ids nq x K, dist_count, hop_count)
+        (and the distances when return_dist)."""
+        q = _f32(queries)
+        nq = q.shape[0]
+        out = np.zeros((nq, K), np.uint32)
+        dist = np.zeros((nq, K), np.float32) if return_dist else None
+        cnt = _lib.Counters()
+        self._check(self.L.wv_search_hnsw(self.h, q, nq, {"hnsw": 0, "nsw": 1}[router], L, K, out,
+                                          None if dist is None else dist.ctypes.data, C.byref(cnt)))
+        if return_dist:
+            return out, dist, int(cnt.dist_count), int(cnt.hop_count)
+        return out, int(cnt.dist_count), int(cnt.hop_count)
+
     def get_eps(self, built: bool = False) -> np.ndarray:
         """SSG roots of the built graph (built=True) or of the search graph."""
         n = C.c_uint32()
@@ -118,6 +138,11 @@ class Context:
     def nnd_refine(self, S: int, K: int, L: int, ITER: int, R: int):
         st = _lib.BuildStats()
         self._check(self.L.wv_nnd_refine(self.h, S, K, L, ITER, R, C.byref(st)))
+        return st.as_dict()
+
+    def efanna_refine(self, S: int, K: int, L: int, ITER: int, R: int):
+        st = _lib.BuildStats()
+        self._check(self.L.wv_efanna_refine(self.h, S, K, L, ITER, R, C.byref(st)))
         return st.as_dict()
 
     def vamana_refine(self, L_refine: int, R_refine: int, alpha: float, entry_L: int = 0):
@@ -249,7 +274,7 @@ class Context:
     # graph-file headers: False / "plain" (none), True / "ep" (ep_), "eps" (SSG roots)
     @staticmethod
     def _hdr(with_ep):
-        return {False: 0, True: 1, "plain": 0, "ep": 1, "eps": 2}[with_ep]
+        return {False: 0, True: 1, "plain": 0, "ep": 1, "eps": 2, "hnsw": 3}[with_ep]
 
     def save_graph(self, path: str, with_ep=False):
         self._check(self.L.wv_save_graph(self.h, path.encode(), self._hdr(with_ep)))
