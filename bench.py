@@ -43,7 +43,7 @@ CFG = dict(n=1_000_000, d=128, centers=256, nq=10_000, seed=7, S=20, K=64, L=80,
 METRIC = "QPS at recall@10>=0.95 (learned+BF16 vs plain FP32, 1 GB300); build sec"
 # DRAM bytes (read + write) of one learned-plan search launch on the 1M x 128
 # workload, from an ncu capture of this command (profiles/)
-TRAFFIC_LEARNED_1M = 3089417984 + 4369664
+TRAFFIC_LEARNED_1M = 3251252992 + 4440064
 
 
 def log(*a):
