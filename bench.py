@@ -700,6 +700,159 @@ def run_learned10m(args):
     print(json.dumps(line), flush=True)
 
 
+def layered_graph_words(torch, dev, base, knn_ids, knn_deg, m, m0, seed):
+    """A graph in the INDEX_HNSW file layout for the routing measurement (the
+    HNSW build itself is not part of this library): layer 0 = the first m0
+    entries of the KNN rows; levels drawn geometrically with HNSW's rule
+    (P(level >= l) = m^-l); layer l >= 1 = the m nearest nodes among those of
+    level >= l (exact, on the GPU); the enterpoint is the first top-level
+    node."""
+    n = base.shape[0]
+    rng = np.random.default_rng(seed)
+    level = np.minimum(rng.geometric(1 - 1 / m, size=n) - 1, 8)
+    top = int(level.max())
+    ep = int(np.flatnonzero(level == top)[0])
+    upper = {}
+    xb = torch.from_numpy(base).to(dev)
+    for lv in range(1, top + 1):
+        ids = np.flatnonzero(level >= lv)
+        k = min(m, len(ids) - 1)
+        if k <= 0:
+            upper[lv] = (ids, np.zeros((len(ids), 0), np.int64))
+            continue
+        x = xb[torch.from_numpy(ids).to(dev)]
+        sq = (x * x).sum(1)
+        nn = []
+        for c0 in range(0, len(ids), 4096):
+            blk = x[c0:c0 + 4096]
+            d2 = sq[c0:c0 + 4096, None] + sq[None, :] - 2 * blk @ x.T
+            d2[torch.arange(d2.shape[0], device=dev), torch.arange(c0, c0 + d2.shape[0], device=dev)] = float("inf")
+            nn.append(torch.topk(d2, k, dim=1, largest=False).indices.cpu().numpy())
+        upper[lv] = (ids, ids[np.concatenate(nn)])
+    pos = {lv: {int(v): r for r, v in enumerate(upper[lv][0])} for lv in upper}
+    deg0 = np.minimum(knn_deg, m0).astype(np.uint32)
+    chunks = [np.array([ep, top], np.uint32)]
+    for v in range(n):
+        rec = [v, level[v] + 1, deg0[v]]
+        chunks.append(np.array(rec, np.uint32))
+        chunks.append(knn_ids[v, :deg0[v]].astype(np.uint32))
+        for lv in range(1, level[v] + 1):
+            fr = upper[lv][1][pos[lv][v]]
+            chunks.append(np.array([len(fr)], np.uint32))
+            chunks.append(fr.astype(np.uint32))
+    return np.concatenate(chunks), level
+
+
+def run_graphs1m(args):
+    """The rows built beyond the KGraph/NSG path, on the 1M x 128 data: the
+    SSG refine (REFINE_SSG) and its SubCentroid search, the EFANNA refine
+    (REFINE_EFANNA) from INIT_RANDOM, and HNSW routing (ROUTER_HNSW) over a
+    layered graph whose layer 0 is the NN-Descent graph.  Search QPS are
+    measured through the host entry points (queries copied in, ids out), at
+    the smallest L of the grid with recall@10 >= 0.95."""
+    import torch
+    from weavess_gb300 import Context
+    from weavess_gb300.groundtruth import knn_fp64
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    cfg = dict(CFG)
+    if args.n:
+        cfg["n"] = args.n
+    if args.nq:
+        cfg["nq"] = args.nq
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    base, query = make_data(cfg)
+    gt = knn_fp64(base, query, 100)
+    ctx = Context(0)
+    K = cfg["k"]
+    nq = query.shape[0]
+
+    def timed_search(fn):
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(max(1, args.steps // 2)):
+            out = fn()
+        return nq * max(1, args.steps // 2) / (time.perf_counter() - t), out
+
+    def sweep(fn):
+        for L in cfg["L_grid"]:
+            res = fn(L)[0]
+            r = recall(res, gt, K)
+            log(f"  L={L} recall={r:.4f}")
+            if r >= cfg["target_recall"]:
+                return L, r
+        return cfg["L_grid"][-1], r
+
+    out = {}
+    # ---- KNN graph (shared by SSG and the HNSW layer 0)
+    ctx.upload_base(base)
+    ctx.srand(1)
+    t = time.time()
+    ctx.init_random(cfg["S"])
+    ctx.nnd_refine(cfg["S"], cfg["K"], cfg["L"], cfg["ITER"], cfg["R"])
+    torch.cuda.synchronize()
+    knn_s = time.time() - t
+    kids, _, kdeg, _ = ctx.get_graph()
+    # ---- SSG
+    t = time.time()
+    st = ctx.ssg_refine(100, 50, 60.0, 10)
+    torch.cuda.synchronize()
+    ssg_s = time.time() - t
+    ctx.load_built_graph()
+    sids, sdist, sdeg, _ = ctx.get_graph()
+    Ls, rs = sweep(lambda L: ctx.search(query, L, K, entry="sub_centroid"))
+    qps, _ = timed_search(lambda: ctx.search(query, Ls, K, entry="sub_centroid"))
+    g = O.Graph(sids, sdist, sdeg, 0)
+    g.eps = st["eps"]
+    smp = 1000
+    tc = time.perf_counter()
+    O.search(base, query[:smp], g, Ls, O.Rand(1), entry="sub_centroid", threads=os.cpu_count() or 1)
+    cpu_ssg = smp / (time.perf_counter() - tc)
+    out["ssg"] = {"refine_s": round(ssg_s, 2), "params": "L_refine=100 R_refine=50 A=60 n_try=10",
+                  "avg_degree": float(sdeg.mean()), "conn_added": st["conn_added"], "L_search": Ls,
+                  "recall@10": round(rs, 4), "qps_e2e": round(qps, 1),
+                  "cpu_oracle_qps": round(cpu_ssg, 1), "cpu_threads": os.cpu_count()}
+    log(f"ssg {out['ssg']}")
+    # ---- HNSW routing over a layered graph (layer 0: the KNN rows)
+    t = time.time()
+    words, level = layered_graph_words(torch, dev, base, kids, kdeg, 16, 32, seed=5)
+    lay_s = time.time() - t
+    ctx.load_hnsw(words)
+    Lh, rh = sweep(lambda L: ctx.search_hnsw(query, L, K))
+    qps_h, (res_h, dc_h, hc_h) = timed_search(lambda: ctx.search_hnsw(query, Lh, K))
+    tc = time.perf_counter()
+    O.search_hnsw(base, query[:smp], words, Lh)
+    cpu_h = smp / (time.perf_counter() - tc)
+    out["hnsw"] = {"graph": f"layer 0 = first 32 NN-Descent neighbours; {int((level > 0).sum())} upper-layer "
+                            f"nodes, top level {int(level.max())}, m=16 (made in {lay_s:.1f}s)",
+                   "L_search": Lh, "recall@10": round(rh, 4), "qps_e2e": round(qps_h, 1),
+                   "dist_count": dc_h, "hop_count": hc_h, "cpu_oracle_qps_1thread": round(cpu_h, 1)}
+    log(f"hnsw {out['hnsw']}")
+    # ---- EFANNA refine from INIT_RANDOM
+    ctx.srand(1)
+    ctx.init_random(cfg["S"])
+    t = time.time()
+    est = ctx.efanna_refine(cfg["S"], cfg["K"], cfg["L"], cfg["ITER"], cfg["R"])
+    torch.cuda.synchronize()
+    ef_s = time.time() - t
+    eids, _, edeg, _ = ctx.get_graph()
+    sample = np.random.default_rng(1).choice(base.shape[0], 1000, replace=False)
+    ex = knn_fp64(base, base[sample], 11)[:, 1:11]
+    grec = float(np.mean([len(set(eids[v, :10].tolist()) & set(ex[i].tolist())) / 10 for i, v in enumerate(sample)]))
+    out["efanna"] = {"refine_s": round(ef_s, 2), "params": f"S={cfg['S']} K={cfg['K']} L={cfg['L']} "
+                     f"ITER={cfg['ITER']} R={cfg['R']} from INIT_RANDOM", "graph_recall@10_1000_nodes": round(grec, 4),
+                     "pairs": est["pairs"], "rand_draws": est["rand_draws"], "nndescent_s_same_params": round(knn_s, 2)}
+    log(f"efanna {out['efanna']}")
+    line = {"metric": "HNSW routing QPS at recall@10>=0.95, with the SSG and EFANNA rows (1M x 128)",
+            "value": out["hnsw"]["qps_e2e"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded integer Gaussian mixture)",
+            "config": {"workload": f"{cfg['n']}x128 int-mixture(256), {nq} queries, top-10", "rows": out}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -710,7 +863,8 @@ def main():
     ap.add_argument("--nq", type=int, default=0, help="override the number of queries")
     ap.add_argument("--n", type=int, default=0, help="override the number of base vectors")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned + bf16 leg")
-    ap.add_argument("--workload", default="int128", choices=["int128", "precision96", "batch960", "learned10m"],
+    ap.add_argument("--workload", default="int128",
+                    choices=["int128", "precision96", "batch960", "learned10m", "graphs1m"],
                     help="int128: the 1M x 128 measurement (default); the others print informational lines")
     ap.add_argument("--profile-region", choices=["search", "build"], default="search",
                     help="region bracketed by cudaProfilerStart/Stop (ncu --profile-from-start off)")
@@ -727,7 +881,7 @@ def main():
         if rank != 0:
             return
     {"int128": run_ours, "precision96": run_precision96, "batch960": run_batch960,
-     "learned10m": run_learned10m}[args.workload](args)
+     "learned10m": run_learned10m, "graphs1m": run_graphs1m}[args.workload](args)
 
 
 if __name__ == "__main__":

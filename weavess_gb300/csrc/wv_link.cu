@@ -1,12 +1,17 @@
-// K3/K4/K5: the Vamana and NSG link (REFINE_VAMANA / REFINE_NSG) on GB300.
+// K3/K4/K5: the Vamana, NSG and SSG link (REFINE_VAMANA / REFINE_NSG /
+// REFINE_SSG) on GB300.
 //
 // Replaces ComponentRefineVAMANA::RefineInner / Link / InterInsert
 // (src/component_refine.cpp:794-950), ComponentRefineNSG::RefineInner / Link /
-// InterInsert (component_refine.cpp:393-541), ComponentCandidateNSG
-// (component_candidate.cpp:10-85), ComponentPruneVAMANA / ComponentPruneNSG
-// (component_prune.cpp:20-69, 245-300) and ComponentRefineEntryCentroid
-// (component_entry.cpp:9-92).  ComponentConnNSGDFS runs on the host (a serial
-// depth-first walk), with its greedy searches on the GPU.
+// InterInsert (component_refine.cpp:393-541), ComponentRefineSSG::
+// RefineInner / Link / InterInsert (component_refine.cpp:550-720),
+// ComponentCandidateNSG and ComponentCandidatePropagation2
+// (component_candidate.cpp:10-109), ComponentPruneVAMANA / ComponentPruneNSG /
+// ComponentPruneSSG (component_prune.cpp:20-122, 245-300) and
+// ComponentRefineEntryCentroid (component_entry.cpp:9-92).
+// ComponentConnNSGDFS runs on the host (a serial depth-first walk), with its
+// greedy searches on the GPU; ComponentConnSSGDFS (component_conn.cpp:
+// 169-225) walks on the GPU (frontier kernels) with the repairs on the device.
 //
 // Plain form, bit-exact with the single-threaded reference:
 //  * candidates: the beam kernel in build mode (seeds flagged, every visit
