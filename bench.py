@@ -50,6 +50,52 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+# ---- ranks: under torchrun every rank holds a replica of the index on its
+# own GPU and searches its own batch (search shards by query, weak scaling);
+# the only collectives are the timing barrier and the max / sum of the
+# per-rank figures
+def world():
+    return int(os.environ.get("WORLD_SIZE", "1"))
+
+
+def rank():
+    return int(os.environ.get("RANK", "0"))
+
+
+def local_device():
+    return int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def _dist():
+    import torch.distributed as dist
+    return dist if dist.is_available() and dist.is_initialized() else None
+
+
+def rank_barrier():
+    d = _dist()
+    if d is not None:
+        d.barrier()
+
+
+def rank_reduce(x, op):
+    """x reduced over ranks ("max" or "sum"); x itself without a process group."""
+    d = _dist()
+    if d is None:
+        return float(x)
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device()) if d.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    d.all_reduce(t, op=d.ReduceOp.MAX if op == "max" else d.ReduceOp.SUM)
+    return float(t.item())
+
+
+def job_rate(units, ms_per_step):
+    """Whole-job throughput: all ranks' units of one step over the slowest
+    rank's step time.  Returns (units per second, max ms per step)."""
+    ms_max = rank_reduce(ms_per_step, "max")
+    return rank_reduce(units, "sum") / (ms_max / 1e3), ms_max
+
+
 class Clocks:
     """nvidia-smi samples while the timed region runs."""
 
@@ -119,6 +165,7 @@ def timed_steps(step, steps, stream, flush, clk, after=None):
     import torch
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     torch.cuda.synchronize()
+    rank_barrier()
     t0 = time.perf_counter()
     if PROFILE_REGION == "search":
         torch.cuda.profiler.start()
@@ -130,6 +177,7 @@ def timed_steps(step, steps, stream, flush, clk, after=None):
         if after is not None:
             after(i)
     torch.cuda.synchronize()
+    rank_barrier()
     if PROFILE_REGION == "search":
         torch.cuda.profiler.stop()
     clk.mark(t0, time.perf_counter())
@@ -292,10 +340,10 @@ def run_ours(args):
         cfg["nq"] = args.nq
     if args.n:
         cfg["n"] = args.n
-    dev = torch.device("cuda:0")
+    dev = torch.device("cuda", local_device())
     torch.cuda.set_device(dev)
     base, query = make_data(cfg)
-    ctx = Context(0)
+    ctx = Context(local_device())
     # one stream for everything timed: the L2 flush, the events and the
     # context's kernels (the legacy default stream would not order the
     # context's non-blocking stream)
@@ -380,10 +428,12 @@ def run_ours(args):
     learned = None
     if not args.no_learned:
         learned = run_learned(ctx, cfg, base, query, gt, args, dev, stream, flush)
-    # ---- CPU baseline: the oracle on the host cores, bounded sample
+    # ---- CPU baseline: the oracle on the host cores, bounded sample (rank 0)
     threads = os.cpu_count() or 1
     sample = 2000 if not args.small else 1000
-    cpu_qps, cpu_dt, _ = cpu_search_qps(base, query, g_ids, g_deg, Lsel, threads, sample)
+    cpu_qps, cpu_dt = 0.0, 0.0
+    if rank() == 0:
+        cpu_qps, cpu_dt, _ = cpu_search_qps(base, query, g_ids, g_deg, Lsel, threads, sample)
     plain = {"qps": round(value, 1), "ms_per_step": round(ms, 4), "L_search": Lsel, "recall@10": round(r_dev, 4),
              "recall_sweep": sweep, "e2e_qps": round(e2e_qps, 1), "dist_count": dc, "hop_count": hc,
              "qps_default_shape": round(nq / (ms_default / 1e3), 1), "tuned_shape": tune_p["chosen"],
@@ -414,8 +464,13 @@ def run_ours(args):
                 "timing": "CUDA events captured around the search kernel in each timed replay"}
         h2d = nq * d * 4 + nq * 4  # queries and one rand() value per query (seeds drawn on the device)
         launches = args.steps
+    # whole job: every rank searched its own nq queries per step
+    head_qps, head_ms = job_rate(nq, head_ms)
+    head_e2e = rank_reduce(head_e2e, "sum")
+    if rank() != 0:
+        return
     line = {
-        "metric": METRIC, "value": round(head_qps, 1), "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+        "metric": METRIC, "value": round(head_qps, 1), "unit": "queries/s", "n_gpus": world(), "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(head_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16 candidates, f32 rerank" if learned else "f32",
         "data": "synthetic (seeded integer Gaussian mixture)",
@@ -871,17 +926,21 @@ def main():
     args = ap.parse_args()
     global PROFILE_REGION
     PROFILE_REGION = args.profile_region
-    rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
-        if rank == 0:
+        if rank() == 0:
             run_reference(args)
         return
-    if args.gpus > 1:
-        # search shards by query; this build measures one GPU (replicas only)
-        if rank != 0:
-            return
+    if args.workload != "int128" and rank() != 0:
+        return  # the informational workloads run on rank 0 alone
+    if args.workload == "int128" and world() > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_device())
+        dist.init_process_group(backend="nccl")
     {"int128": run_ours, "precision96": run_precision96, "batch960": run_batch960,
      "learned10m": run_learned10m, "graphs1m": run_graphs1m}[args.workload](args)
+    if _dist() is not None:
+        _dist().destroy_process_group()
 
 
 if __name__ == "__main__":
