@@ -759,9 +759,10 @@ def layered_graph_words(torch, dev, base, knn_ids, knn_deg, m, m0, seed):
     """A graph in the INDEX_HNSW file layout for the routing measurement (the
     HNSW build itself is not part of this library): layer 0 = the first m0
     entries of the KNN rows; levels drawn geometrically with HNSW's rule
-    (P(level >= l) = m^-l); layer l >= 1 = the m nearest nodes among those of
-    level >= l (exact, on the GPU); the enterpoint is the first top-level
-    node."""
+    (P(level >= l) = m^-l); layer l >= 1 = the m/2 nearest nodes among those
+    of level >= l (exact, on the GPU) and m/2 random ones of that layer (long
+    links, so that the descent crosses clusters); the enterpoint is the first
+    top-level node."""
     n = base.shape[0]
     rng = np.random.default_rng(seed)
     level = np.minimum(rng.geometric(1 - 1 / m, size=n) - 1, 8)
@@ -771,7 +772,7 @@ def layered_graph_words(torch, dev, base, knn_ids, knn_deg, m, m0, seed):
     xb = torch.from_numpy(base).to(dev)
     for lv in range(1, top + 1):
         ids = np.flatnonzero(level >= lv)
-        k = min(m, len(ids) - 1)
+        k = min(m // 2, len(ids) - 1)
         if k <= 0:
             upper[lv] = (ids, np.zeros((len(ids), 0), np.int64))
             continue
@@ -783,7 +784,9 @@ def layered_graph_words(torch, dev, base, knn_ids, knn_deg, m, m0, seed):
             d2 = sq[c0:c0 + 4096, None] + sq[None, :] - 2 * blk @ x.T
             d2[torch.arange(d2.shape[0], device=dev), torch.arange(c0, c0 + d2.shape[0], device=dev)] = float("inf")
             nn.append(torch.topk(d2, k, dim=1, largest=False).indices.cpu().numpy())
-        upper[lv] = (ids, ids[np.concatenate(nn)])
+        near = ids[np.concatenate(nn)]
+        far = ids[rng.integers(0, len(ids), size=(len(ids), min(m - k, len(ids) - 1)))]
+        upper[lv] = (ids, np.concatenate([near, far], 1))
     pos = {lv: {int(v): r for r, v in enumerate(upper[lv][0])} for lv in upper}
     deg0 = np.minimum(knn_deg, m0).astype(np.uint32)
     chunks = [np.array([ep, top], np.uint32)]
@@ -793,6 +796,7 @@ def layered_graph_words(torch, dev, base, knn_ids, knn_deg, m, m0, seed):
         chunks.append(knn_ids[v, :deg0[v]].astype(np.uint32))
         for lv in range(1, level[v] + 1):
             fr = upper[lv][1][pos[lv][v]]
+            fr = fr[fr != v]
             chunks.append(np.array([len(fr)], np.uint32))
             chunks.append(fr.astype(np.uint32))
     return np.concatenate(chunks), level
@@ -896,7 +900,7 @@ def run_graphs1m(args):
     O.search_hnsw(base, query[:smp], words, Lh)
     cpu_h = smp / (time.perf_counter() - tc)
     out["hnsw"] = {"graph": f"layer 0 = the NSG rows (R={cfg['R_refine']}); {int((level > 0).sum())} upper-layer "
-                            f"nodes (exact 16-NN per layer), top level {int(level.max())} (made in {lay_s:.1f}s)",
+                            f"nodes (8 nearest + 8 random per upper layer), top level {int(level.max())} (made in {lay_s:.1f}s)",
                    "L_search": Lh, "recall@10": round(rh, 4), "qps_e2e": round(qps_h, 1),
                    "dist_count": dc_h, "hop_count": hc_h, "cpu_oracle_qps_1thread": round(cpu_h, 1)}
     log(f"hnsw {out['hnsw']}")
