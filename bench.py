@@ -755,48 +755,32 @@ def run_learned10m(args):
     print(json.dumps(line), flush=True)
 
 
-def layered_graph_words(torch, dev, base, knn_ids, knn_deg, m, m0, seed):
+def layered_graph_words(base, l0_ids, l0_deg, m, m0, seed, upper_rows):
     """A graph in the INDEX_HNSW file layout for the routing measurement (the
     HNSW build itself is not part of this library): layer 0 = the first m0
-    entries of the KNN rows; levels drawn geometrically with HNSW's rule
-    (P(level >= l) = m^-l); layer l >= 1 = the m/2 nearest nodes among those
-    of level >= l (exact, on the GPU) and m/2 random ones of that layer (long
-    links, so that the descent crosses clusters); the enterpoint is the first
-    top-level node."""
+    entries of the given rows; levels drawn geometrically with HNSW's rule
+    (P(level >= l) = m^-l); layer l >= 1 = upper_rows(ids) over the nodes of
+    level >= l (rows of global ids, at most m each); the enterpoint is the
+    first top-level node."""
     n = base.shape[0]
     rng = np.random.default_rng(seed)
     level = np.minimum(rng.geometric(1 - 1 / m, size=n) - 1, 8)
     top = int(level.max())
     ep = int(np.flatnonzero(level == top)[0])
     upper = {}
-    xb = torch.from_numpy(base).to(dev)
     for lv in range(1, top + 1):
         ids = np.flatnonzero(level >= lv)
-        k = min(m // 2, len(ids) - 1)
-        if k <= 0:
-            upper[lv] = (ids, np.zeros((len(ids), 0), np.int64))
-            continue
-        x = xb[torch.from_numpy(ids).to(dev)]
-        sq = (x * x).sum(1)
-        nn = []
-        for c0 in range(0, len(ids), 4096):
-            blk = x[c0:c0 + 4096]
-            d2 = sq[c0:c0 + 4096, None] + sq[None, :] - 2 * blk @ x.T
-            d2[torch.arange(d2.shape[0], device=dev), torch.arange(c0, c0 + d2.shape[0], device=dev)] = float("inf")
-            nn.append(torch.topk(d2, k, dim=1, largest=False).indices.cpu().numpy())
-        near = ids[np.concatenate(nn)]
-        far = ids[rng.integers(0, len(ids), size=(len(ids), min(m - k, len(ids) - 1)))]
-        upper[lv] = (ids, np.concatenate([near, far], 1))
+        rows, deg = upper_rows(ids)
+        upper[lv] = (ids, rows, deg)
     pos = {lv: {int(v): r for r, v in enumerate(upper[lv][0])} for lv in upper}
-    deg0 = np.minimum(knn_deg, m0).astype(np.uint32)
+    deg0 = np.minimum(l0_deg, m0).astype(np.uint32)
     chunks = [np.array([ep, top], np.uint32)]
     for v in range(n):
-        rec = [v, level[v] + 1, deg0[v]]
-        chunks.append(np.array(rec, np.uint32))
-        chunks.append(knn_ids[v, :deg0[v]].astype(np.uint32))
+        chunks.append(np.array([v, level[v] + 1, deg0[v]], np.uint32))
+        chunks.append(l0_ids[v, :deg0[v]].astype(np.uint32))
         for lv in range(1, level[v] + 1):
-            fr = upper[lv][1][pos[lv][v]]
-            fr = fr[fr != v]
+            r = pos[lv][v]
+            fr = upper[lv][1][r, :upper[lv][2][r]][:m]
             chunks.append(np.array([len(fr)], np.uint32))
             chunks.append(fr.astype(np.uint32))
     return np.concatenate(chunks), level
@@ -890,8 +874,25 @@ def run_graphs1m(args):
     ctx.set_graph(kids, kdeg, dist=kdist)
     ctx.nsg_refine(cfg["L_refine"], cfg["R_refine"], cfg["C_refine"])
     nids, _, ndeg, _ = ctx.get_graph()
+    sub = Context(local_device())
+
+    def nsg_rows(ids):
+        # upper layers: an NSG (R=16) over the layer's nodes; tiny layers are
+        # fully connected
+        if len(ids) <= 17:
+            rows = np.array([[u for u in ids if u != v] + [0] * (17 - len(ids)) for v in ids], np.int64)
+            return rows, np.full(len(ids), len(ids) - 1)
+        sub.upload_base(np.ascontiguousarray(base[ids]))
+        sub.srand(1)
+        S = min(20, len(ids) - 2)
+        sub.init_random(S)
+        sub.nnd_refine(S, min(32, len(ids) - 1), min(40, len(ids) - 1), 8, 100)
+        sub.nsg_refine(min(40, len(ids) - 1), 16, 200)
+        r, _, d, _ = sub.get_graph()
+        return ids[r.astype(np.int64)], d
+
     t = time.time()
-    words, level = layered_graph_words(torch, dev, base, nids, ndeg, 16, 32, seed=5)
+    words, level = layered_graph_words(base, nids, ndeg, 16, 32, 5, nsg_rows)
     lay_s = time.time() - t
     ctx.load_hnsw(words)
     Lh, rh = sweep(lambda L: ctx.search_hnsw(query, L, K))
@@ -900,7 +901,7 @@ def run_graphs1m(args):
     O.search_hnsw(base, query[:smp], words, Lh)
     cpu_h = smp / (time.perf_counter() - tc)
     out["hnsw"] = {"graph": f"layer 0 = the NSG rows (R={cfg['R_refine']}); {int((level > 0).sum())} upper-layer "
-                            f"nodes (8 nearest + 8 random per upper layer), top level {int(level.max())} (made in {lay_s:.1f}s)",
+                            f"nodes (an NSG with R=16 per upper layer), top level {int(level.max())} (made in {lay_s:.1f}s)",
                    "L_search": Lh, "recall@10": round(rh, 4), "qps_e2e": round(qps_h, 1),
                    "dist_count": dc_h, "hop_count": hc_h, "cpu_oracle_qps_1thread": round(cpu_h, 1)}
     log(f"hnsw {out['hnsw']}")

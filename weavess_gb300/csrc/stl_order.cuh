@@ -36,8 +36,10 @@ WV_HD int lg2(int n) {  // floor(log2(n)), n > 0
 }
 
 // ---- heap ----
-template <class T, class Less>
-WV_HD void push_heap_hole(T *first, int hole, int top, T value, Less less) {
+// The heap routines take any handle `first` with first[i] yielding an
+// assignable element (a plain pointer, or an array split across memories).
+template <class P, class T, class Less>
+WV_HD void push_heap_hole(P first, int hole, int top, T value, Less less) {
   int parent = (hole - 1) / 2;
   while (hole > top && less(first[parent], value)) {
     first[hole] = first[parent];
@@ -47,8 +49,8 @@ WV_HD void push_heap_hole(T *first, int hole, int top, T value, Less less) {
   first[hole] = value;
 }
 
-template <class T, class Less>
-WV_HD void adjust_heap(T *first, int hole, int len, T value, Less less) {
+template <class P, class T, class Less>
+WV_HD void adjust_heap(P first, int hole, int len, T value, Less less) {
   const int top = hole;
   int child = hole;
   while (child < (len - 1) / 2) {
@@ -65,12 +67,12 @@ WV_HD void adjust_heap(T *first, int hole, int len, T value, Less less) {
   push_heap_hole(first, hole, top, value, less);
 }
 
-template <class T, class Less>
-WV_HD void make_heap(T *first, int len, Less less) {
+template <class P, class Less>
+WV_HD void make_heap(P first, int len, Less less) {
   if (len < 2) return;
   int parent = (len - 2) / 2;
   while (true) {
-    T value = first[parent];
+    auto value = first[parent];
     adjust_heap(first, parent, len, value, less);
     if (parent == 0) return;
     parent--;
@@ -78,9 +80,9 @@ WV_HD void make_heap(T *first, int len, Less less) {
 }
 
 // std::push_heap(first, first + len): the new element is first[len - 1]
-template <class T, class Less>
-WV_HD void push_heap(T *first, int len, Less less) {
-  T value = first[len - 1];
+template <class P, class Less>
+WV_HD void push_heap(P first, int len, Less less) {
+  auto value = first[len - 1];
   push_heap_hole(first, len - 1, 0, value, less);
 }
 
@@ -93,9 +95,13 @@ WV_HD void pop_heap_into(T *first, int len, T *result, Less less) {
 }
 
 // std::pop_heap(first, first + len)
-template <class T, class Less>
-WV_HD void pop_heap(T *first, int len, Less less) {
-  if (len > 1) pop_heap_into(first, len - 1, first + len - 1, less);
+template <class P, class Less>
+WV_HD void pop_heap(P first, int len, Less less) {
+  if (len > 1) {
+    auto value = first[len - 1];
+    first[len - 1] = first[0];
+    adjust_heap(first, 0, len - 1, value, less);
+  }
 }
 
 template <class T, class Less>

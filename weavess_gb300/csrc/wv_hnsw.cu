@@ -36,10 +36,18 @@ namespace {
 constexpr int HN_WARPS = 4;
 constexpr uint32_t HN_PATH = 64;       // ensure_k_path_ entries kept (the last ones)
 constexpr uint32_t HN_NONE = 0xffffffffu;
+constexpr int HN_CSH = 512;            // candidate-queue entries kept in shared memory
 
 struct HEnt {
   float d;
   uint32_t id;
+};
+// the candidate queue's array: its first HN_CSH entries (the heap's top nine
+// levels, which every push and pop walks) in shared memory, the rest in
+// global memory
+struct SplitHeap {
+  HEnt *sh, *gl;
+  __device__ __forceinline__ HEnt &operator[](int i) const { return i < HN_CSH ? sh[i] : gl[i - HN_CSH]; }
 };
 struct FurtherLess {  // std::less<FurtherFirst>: a max-heap by distance (index.h:435-447)
   __device__ bool operator()(const HEnt &a, const HEnt &b) const { return a.d < b.d; }
@@ -63,7 +71,7 @@ struct HnswArgs {
   float *out_dist;
   uint32_t *bits, *touched;  // per warp slot: words each
   uint32_t words;
-  HEnt *cand;                // per warp slot: ccap entries (candidate queue, then the final queue)
+  HEnt *cand;                // per warp slot: ccap entries past the shared part (candidate queue, final queue)
   uint32_t ccap;
   unsigned *next_query;
   unsigned long long *counters;
@@ -77,12 +85,13 @@ struct WarpState {
   uint32_t *ids;  // 32: the current chunk's fresh ids
   float *dist;    // 32
   HEnt *path;     // HN_PATH
+  HEnt *csh;      // HN_CSH: the shared part of the candidate queue
 };
 
 __host__ __device__ inline size_t hn_warp_bytes(uint32_t d, uint32_t L) {
   const size_t q = ((size_t)d * 4 + 15) & ~size_t(15);
   return q + (size_t)STAGE_FLOATS * 4 + (((size_t)(L + 1) * 8 + 15) & ~size_t(15)) + 32 * 4 + 32 * 4 +
-         (size_t)HN_PATH * 8;
+         (size_t)HN_PATH * 8 + (size_t)HN_CSH * 8;
 }
 
 __device__ inline WarpState hn_carve(uint8_t *p, uint32_t d, uint32_t L) {
@@ -98,6 +107,8 @@ __device__ inline WarpState hn_carve(uint8_t *p, uint32_t d, uint32_t L) {
   w.dist = reinterpret_cast<float *>(p);
   p += 32 * 4;
   w.path = reinterpret_cast<HEnt *>(p);
+  p += (size_t)HN_PATH * 8;
+  w.csh = reinterpret_cast<HEnt *>(p);
   return w;
 }
 
@@ -168,7 +179,7 @@ __device__ int hn_chunk(const HnswArgs &a, WarpState &s, Bits &vis, const uint32
 
 // SearchAtLayer (component_route.cpp:85-131 / 214-260) from `entry`,
 // pushing into the result queue (size rs, lane 0's copy is authoritative)
-__device__ bool hn_search_layer(const HnswArgs &a, WarpState &s, Bits &vis, HEnt *cand, uint32_t entry,
+__device__ bool hn_search_layer(const HnswArgs &a, WarpState &s, Bits &vis, SplitHeap cand, uint32_t entry,
                                 uint32_t &rs, unsigned long long &dc, unsigned long long &hc, int lane) {
   // the entry's distance, then both queues hold it
   {
@@ -214,7 +225,7 @@ __device__ bool hn_search_layer(const HnswArgs &a, WarpState &s, Bits &vis, HEnt
             s.res[rs] = HEnt{d, s.ids[t]};
             stl::push_heap(s.res, (int)rs + 1, FurtherLess());
             rs++;
-            if (cs >= a.ccap) {
+            if (cs >= HN_CSH + a.ccap) {
               set_err(a.status, DEV_OVERFLOW);
               cs = 0;
               break;
@@ -243,7 +254,7 @@ __global__ void __launch_bounds__(HN_WARPS * 32) k_hnsw(HnswArgs a) {
   WarpState s = hn_carve(smem + (size_t)warp * hn_warp_bytes(a.d, a.L), a.d, a.L);
   const uint32_t slot = blockIdx.x * HN_WARPS + warp;
   Bits vis{a.bits + (size_t)slot * a.words, a.touched + (size_t)slot * a.words, 0};
-  HEnt *cand = a.cand + (size_t)slot * a.ccap;
+  const SplitHeap cand{s.csh, a.cand + (size_t)slot * a.ccap};
   unsigned long long dc = 0, hc = 0;
   for (;;) {
     uint32_t q = 0;
@@ -317,7 +328,7 @@ __global__ void __launch_bounds__(HN_WARPS * 32) k_hnsw(HnswArgs a) {
     }
     // ---- the K nearest through the CloserFirst queue (component_route.cpp:197-210)
     if (lane == 0) {
-      HEnt *tmp = cand;
+      const SplitHeap tmp = cand;
       uint32_t ts = 0;
       while (rs > 0) {
         tmp[ts] = s.res[0];
