@@ -17,7 +17,7 @@
 // CloserFirst, a min-heap) are kept as libstdc++ heaps with the same
 // comparators, so equal distances resolve exactly as they do there.  A
 // neighbour list is handled 32 entries at a time: the lanes mark the visited
-// bits and take the distances (exact reference order), then one lane applies
+// bits and take the distances (exact reference order, a lane per row), then one lane applies
 // the queue updates in list order.  The visited set is a per-warp bitset over
 // the nodes, cleared through the list of words it touched (VisitedList::Reset
 // gives a fresh set for every layer and every SearchAtLayer).
@@ -80,7 +80,6 @@ struct HnswArgs {
 
 struct WarpState {
   float *qv;     // d floats
-  float *stage;  // STAGE_FLOATS
   HEnt *res;     // L + 1 entries: the result queue
   uint32_t *ids;  // 32: the current chunk's fresh ids
   float *dist;    // 32
@@ -90,7 +89,7 @@ struct WarpState {
 
 __host__ __device__ inline size_t hn_warp_bytes(uint32_t d, uint32_t L) {
   const size_t q = ((size_t)d * 4 + 15) & ~size_t(15);
-  return q + (size_t)STAGE_FLOATS * 4 + (((size_t)(L + 1) * 8 + 15) & ~size_t(15)) + 32 * 4 + 32 * 4 +
+  return q + (((size_t)(L + 1) * 8 + 15) & ~size_t(15)) + 32 * 4 + 32 * 4 +
          (size_t)HN_PATH * 8 + (size_t)HN_CSH * 8;
 }
 
@@ -98,8 +97,6 @@ __device__ inline WarpState hn_carve(uint8_t *p, uint32_t d, uint32_t L) {
   WarpState w;
   w.qv = reinterpret_cast<float *>(p);
   p += ((size_t)d * 4 + 15) & ~size_t(15);
-  w.stage = reinterpret_cast<float *>(p);
-  p += (size_t)STAGE_FLOATS * 4;
   w.res = reinterpret_cast<HEnt *>(p);
   p += ((size_t)(L + 1) * 8 + 15) & ~size_t(15);
   w.ids = reinterpret_cast<uint32_t *>(p);
@@ -110,6 +107,19 @@ __device__ inline WarpState hn_carve(uint8_t *p, uint32_t d, uint32_t L) {
   p += (size_t)HN_PATH * 8;
   w.csh = reinterpret_cast<HEnt *>(p);
   return w;
+}
+
+// exact-order squared L2 (Distance::compare, include/weavess/distance.h) of
+// base row `id` and the query in shared memory, by one lane: a row's 16-byte
+// pieces are read straight from global memory (each lane its own row)
+__device__ __forceinline__ float hn_dist(const float *__restrict__ base, uint32_t d, uint32_t id, const float *qv) {
+  const float4 *x = reinterpret_cast<const float4 *>(base + (size_t)id * d);
+  const float4 *q = reinterpret_cast<const float4 *>(qv);
+  float acc = 0.f;
+  const uint32_t d4 = d >> 2;
+#pragma unroll 8
+  for (uint32_t g = 0; g < d4; g++) acc = __fadd_rn(acc, group4(q[g], __ldg(x + g)));
+  return acc;
 }
 
 // the visited bitset of one warp: words that go from 0 to non-0 are listed
@@ -171,7 +181,7 @@ __device__ int hn_chunk(const HnswArgs &a, WarpState &s, Bits &vis, const uint32
   if (fresh) s.ids[__popc(fm & ((1u << lane) - 1u))] = my;
   __syncwarp();
   const uint32_t cid = lane < cnt ? s.ids[lane] : 0u;
-  const float dd = cnt ? warp_l2_rows(a.base, a.d, cid, cnt, s.qv, s.stage, lane) : 0.f;
+  const float dd = lane < cnt ? hn_dist(a.base, a.d, cid, s.qv) : 0.f;
   if (lane < cnt) s.dist[lane] = dd;
   __syncwarp();
   return cnt;
@@ -183,7 +193,7 @@ __device__ bool hn_search_layer(const HnswArgs &a, WarpState &s, Bits &vis, Spli
                                 uint32_t &rs, unsigned long long &dc, unsigned long long &hc, int lane) {
   // the entry's distance, then both queues hold it
   {
-    const float de = warp_l2_rows(a.base, a.d, entry, 1, s.qv, s.stage, lane);
+    const float de = lane == 0 ? hn_dist(a.base, a.d, entry, s.qv) : 0.f;
     dc++;
     vis.clear(lane);
     vis.test_set(lane == 0, entry, lane);
@@ -267,7 +277,7 @@ __global__ void __launch_bounds__(HN_WARPS * 32) k_hnsw(HnswArgs a) {
     if (a.router == 0) {
       // ---- greedy descent through every layer (component_route.cpp:144-184)
       uint32_t cur = a.ep;
-      float cur_dist = warp_l2_rows(a.base, a.d, cur, 1, s.qv, s.stage, lane);
+      float cur_dist = lane == 0 ? hn_dist(a.base, a.d, cur, s.qv) : 0.f;
       cur_dist = __shfl_sync(FULL, cur_dist, 0);
       dc++;
       uint32_t plen = 1;  // path entries so far (the last HN_PATH kept)
