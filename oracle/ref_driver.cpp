@@ -17,7 +17,7 @@
 // usage: ref_driver base.fvecs query.fvecs gt.ivecs outprefix key=val ... -- step ...
 //   steps: init_random | init_rand | nndescent | efanna | vamana | nsg | ssg | load:<kgraph|vamana|nsg|ssg|efanna>
 //          | hnsw | search_rand:<L> | search_centroid:<L> | search_sub:<L> | search_hnsw:<L>
-//          | search_nsw:<L> | rand_probe
+//          | search_nsw:<L> | policy:<rand|centroid>_<set_recall|ascend> | rand_probe
 //   (search_sub: SEARCH_ENTRY_SUB_CENTROID, the entry the reference's SSG
 //   test searches with, test/main.cpp:117)
 #include <bits/stdc++.h>
@@ -204,6 +204,42 @@ int main(int argc, char **argv) {
       fwrite(&hc, 4, 1, f);
       fclose(f);
       // components own (and would delete) the index; leak them as the reference does
+    } else if (step == "policy") {
+      // IndexBuilder::search (builder.cpp:187-487) with its L policy, entry
+      // rand or centroid, ROUTER_GREEDY: arg = "<rand|centroid>_<set_recall|ascend>".
+      // The loop prints each L, DistCount, HopCount and accuracy; they are
+      // captured from std::cout and dumped as (L, dist_count, hop_count, acc).
+      auto us = arg.find('_');
+      std::string ent = arg.substr(0, us), pol = arg.substr(us + 1);
+      idx->resetDistCount();  // the counters start from zero, as in a fresh search
+      idx->resetHopCount();
+      std::stringstream ss;
+      std::streambuf *old = std::cout.rdbuf(ss.rdbuf());
+      builder->search(ent == "rand" ? SEARCH_ENTRY_RAND : SEARCH_ENTRY_CENTROID, ROUTER_GREEDY,
+                      pol == "ascend" ? L_SEARCH_ASCEND : L_SEARCH_SET_RECALL);
+      std::cout.rdbuf(old);
+      std::vector<unsigned> Ls, dcs, hcs;
+      std::vector<float> accs;
+      std::string line;
+      while (std::getline(ss, line)) {
+        unsigned v;
+        float a;
+        if (sscanf(line.c_str(), "SEARCH_L : %u", &v) == 1) Ls.push_back(v);
+        else if (sscanf(line.c_str(), "DistCount: %u", &v) == 1) dcs.push_back(v);
+        else if (sscanf(line.c_str(), "HopCount: %u", &v) == 1) hcs.push_back(v);
+        else if (sscanf(line.c_str(), "10 NN accuracy: %f", &a) == 1) accs.push_back(a);
+      }
+      std::string out = prefix + ".policy_" + arg + ".bin";
+      FILE *f = fopen(out.c_str(), "wb");
+      unsigned cnt = (unsigned)Ls.size();
+      fwrite(&cnt, 4, 1, f);
+      for (unsigned i = 0; i < cnt; i++) {
+        unsigned rec[3] = {Ls[i], i < dcs.size() ? dcs[i] : 0u, i < hcs.size() ? hcs[i] : 0u};
+        float a = i < accs.size() ? accs[i] : -1.f;
+        fwrite(rec, 4, 3, f);
+        fwrite(&a, 4, 1, f);
+      }
+      fclose(f);
     } else if (step == "rand_probe") {
       // consumes one value of the process rand() stream and reports it
       printf("rand_probe %d\n", rand());

@@ -44,9 +44,10 @@ CASES = {
                                   alpha=1.2, A=60, n_try=5, max_m=8, max_m0=16, ef_construction=40, mult=0,
                                   n_threads=1),
                       pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:20", "search_rand:50",
-                                  "vamana", "load:vamana", "search_centroid:30", "search_rand:17"],
+                                  "vamana", "load:vamana", "search_centroid:30", "search_rand:17",
+                                  "policy:rand_set_recall"],
                                  ["init_random", "nndescent", "nsg", "load:nsg", "search_centroid:30",
-                                  "search_rand:40"],
+                                  "search_rand:40", "policy:centroid_ascend"],
                                  ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:30", "search_sub:30"],
                                  ["init_random", "efanna", "load:efanna", "search_rand:30"],
                                  ["hnsw", "search_hnsw:20", "search_hnsw:50", "search_nsw:30"]]),
@@ -66,7 +67,8 @@ CASES = {
                                    n_threads=1),
                        pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:20", "search_rand:40",
                                    "vamana", "load:vamana", "search_centroid:24"],
-                                  ["init_random", "nndescent", "nsg", "load:nsg", "search_centroid:20"],
+                                  ["init_random", "nndescent", "nsg", "load:nsg", "search_centroid:20",
+                                   "policy:rand_ascend"],
                                   ["init_random", "nndescent", "ssg", "load:ssg", "search_sub:20"],
                                   ["init_random", "efanna"],
                                   ["hnsw", "search_hnsw:16", "search_nsw:24"]]),
@@ -95,7 +97,7 @@ CASES = {
 def run_case(name, spec):
     base, query = spec["data"]()
     gt = ds.groundtruth_fp64(base, query, 20)
-    out = {"base": base, "query": query}
+    out = {"base": base, "query": query, "gt": gt.astype(np.uint32)}
     with tempfile.TemporaryDirectory() as tmp:
         bf, qf, gf = (os.path.join(tmp, x) for x in ("b.fvecs", "q.fvecs", "g.ivecs"))
         ds.write_vecs(bf, base)
@@ -128,7 +130,12 @@ def run_case(name, spec):
                 if not f.startswith(f"p{pi}.") or not f.endswith(".bin"):
                     continue
                 key = f[: -len(".bin")]
-                if key.endswith(".hnswgraph"):
+                if ".policy_" in key:
+                    raw = np.fromfile(os.path.join(tmp, f), np.uint32)
+                    rec = raw[1:].reshape(int(raw[0]), 4)
+                    out[key + ".steps"] = rec[:, :3].copy()
+                    out[key + ".acc"] = rec[:, 3].copy().view(np.float32)
+                elif key.endswith(".hnswgraph"):
                     out[f"p{pi}.hnsw.words"] = np.fromfile(os.path.join(tmp, f), np.uint32)
                 elif key.endswith(".ssgeps"):
                     out[key[: -len("eps")] + ".eps"] = np.fromfile(os.path.join(tmp, f), np.uint32)[1:]

@@ -90,6 +90,15 @@ def replay_oracle(f, pi, on_search=None, on_graph=None):
         elif kind == "hnsw":
             hwords = f[key + "hnsw.words"]
             continue
+        elif kind == "policy":
+            # IndexBuilder::search's L policy around the search of `loaded`
+            from weavess_gb300 import policy as P
+            entry, _, pol = arg.partition("_")
+            fn = ((lambda L: on_search(entry, L, loaded, rnd)) if on_search
+                  else (lambda L: O.search(base, query, loaded, L, rnd, entry=entry)))
+            got = P.set_recall(fn, f["gt"])[0] if pol == "set_recall" else P.ascend(fn, f["gt"])
+            yield s, f"{key}policy_{arg}", got
+            continue
         elif kind in ("search_hnsw", "search_nsw"):
             router, L = kind[len("search_"):], int(arg)
             got = (on_search(router, L, hwords, rnd) if on_search

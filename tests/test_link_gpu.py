@@ -57,6 +57,16 @@ def _replay(ctx, f, pi):
         elif kind == "load":
             ctx.load_built_graph()
             continue
+        elif kind == "policy":  # IndexBuilder::search with its L policy, on the context's rand stream
+            entry, _, pol = arg.partition("_")
+            got = ctx.search_policy(query, f["gt"], policy=pol, entry=entry)
+            steps = got[0] if pol == "set_recall" else got
+            k = f"{key}policy_{arg}"
+            have = np.array([[st["L"], st["dist_count"], st["hop_count"]] for st in steps], np.uint64)
+            assert np.array_equal(have, f[k + ".steps"].astype(np.uint64)), s
+            assert np.allclose([st["accuracy"] for st in steps], f[k + ".acc"], rtol=0, atol=5e-6), s
+            checked.append(s)
+            continue
         else:
             entry = {"search_rand": "rand", "search_centroid": "centroid", "search_sub": "sub_centroid"}[kind]
             res, dc, hc = ctx.search(query, int(arg), 10, entry=entry)

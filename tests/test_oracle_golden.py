@@ -10,6 +10,16 @@ import oracle as O
 from golden_util import cases, load, graph_of, rows_equal
 
 
+def check_policy(steps, f, key, where):
+    """The widths, DistCount and HopCount of every step equal the reference's
+    (its accuracy was printed with six significant digits)."""
+    want = f[key + ".steps"]
+    got = np.array([[st["L"], st["dist_count"], st["hop_count"]] for st in steps], np.uint64)
+    assert got.shape == want.shape and np.array_equal(got, want.astype(np.uint64)), (where, got, want)
+    acc = np.array([st["accuracy"] for st in steps])
+    assert np.allclose(acc, f[key + ".acc"], rtol=0, atol=5e-6), where
+
+
 def test_rand_stream_matches_glibc():
     libc = ctypes.CDLL("libc.so.6")
     libc.srand(1)
@@ -69,6 +79,13 @@ def test_oracle_replays_reference(name):
                 k = f"{key}{kind}_{arg}"
                 assert np.array_equal(res, f[k + ".res"]), (name, s)
                 assert [dc, hc] == f[k + ".counts"].tolist(), (name, s)
+                continue
+            elif kind == "policy":
+                from weavess_gb300 import policy as P
+                entry, _, pol = arg.partition("_")
+                fn = lambda L: O.search(base, query, loaded, L, rnd, entry=entry)  # noqa: E731
+                steps = P.set_recall(fn, f["gt"])[0] if pol == "set_recall" else P.ascend(fn, f["gt"])
+                check_policy(steps, f, f"{key}policy_{arg}", (name, s))
                 continue
             elif kind.startswith("search"):
                 entry = {"search_rand": "rand", "search_centroid": "centroid", "search_sub": "sub_centroid"}[kind]

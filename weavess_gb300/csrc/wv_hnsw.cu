@@ -189,7 +189,7 @@ __device__ int hn_chunk(const HnswArgs &a, WarpState &s, Bits &vis, const uint32
 
 // SearchAtLayer (component_route.cpp:85-131 / 214-260) from `entry`,
 // pushing into the result queue (size rs, lane 0's copy is authoritative)
-__device__ bool hn_search_layer(const HnswArgs &a, WarpState &s, Bits &vis, SplitHeap cand, uint32_t entry,
+__device__ void hn_search_layer(const HnswArgs &a, WarpState &s, Bits &vis, SplitHeap cand, uint32_t entry,
                                 uint32_t &rs, unsigned long long &dc, unsigned long long &hc, int lane) {
   // the entry's distance, then both queues hold it
   {
@@ -255,7 +255,6 @@ __device__ bool hn_search_layer(const HnswArgs &a, WarpState &s, Bits &vis, Spli
       __syncwarp();
     }
   }
-  return true;
 }
 
 __global__ void __launch_bounds__(HN_WARPS * 32) k_hnsw(HnswArgs a) {

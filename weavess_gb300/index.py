@@ -82,6 +82,27 @@ class Context:
             e = _u32(eps)
             self._check(self.L.wv_set_eps(self.h, e.ctypes.data, len(e)))
 
+    # -- IndexBuilder::search with its L policy (builder.cpp:187-487)
+    def search_policy(self, queries, gt, policy: str = "set_recall", entry: str = "rand", L: int = 0,
+                      router: str = "greedy"):
+        """The reference's search loop around this context's searches:
+        policy "set_recall" (L_SEARCH_SET_RECALL; returns (steps, L_min)),
+        "ascend" (L_SEARCH_ASCEND) or "assign" (L_SEARCH_ASSIGN with L);
+        router "greedy" (with `entry`) or "hnsw" / "nsw".  Each step records
+        L, the reference's 10-NN accuracy, DistCount, HopCount and seconds."""
+        from . import policy as P
+        if router == "greedy":
+            def fn(Lq):
+                return self.search(queries, Lq, P.K_SEARCH, entry=entry)
+        else:
+            def fn(Lq):
+                return self.search_hnsw(queries, Lq, P.K_SEARCH, router=router)
+        if policy == "set_recall":
+            return P.set_recall(fn, gt)
+        if policy == "ascend":
+            return P.ascend(fn, gt)
+        return P.assign(fn, L, gt)
+
     # -- HNSW / NSW routing over the reference's INDEX_HNSW graph
     def load_hnsw(self, words: np.ndarray):
         """The HNSW search graph from the words of an INDEX_HNSW file."""
