@@ -272,7 +272,10 @@ int wv_load_graph(wv_ctx *ctx, const char *path, int with_ep);
  * node 0 (WV_GRAPH_PLAIN) -- then each from the smallest unreached id, until
  * every node is reached) and, given an exact KNN graph (n rows of
  * exact_width ids, exact_deg valid), the mean share of each node's first 10
- * exact neighbours in its row (-1 when no exact graph is given). */
+ * exact neighbours in its row (-1 when no exact graph is given; an FP32 sum
+ * in node order, as the reference takes it).  WV_GRAPH_HNSW reports on the
+ * HNSW graph: layer-0 degrees and quality, conn walked over every layer from
+ * the enterpoint. */
 typedef struct {
   uint32_t max_out, min_out;
   double avg_out;

@@ -44,7 +44,9 @@ def host_conn(ids, deg, root):
 
 
 def host_quality(ids, deg, exact):
-    q = []
+    """graph_quality (builder.cpp:716-775): per node hits / min(10, degree,
+    exact-list length) in FP32, summed in FP32 in node order, over n."""
+    s = np.float32(0)
     for i in range(ids.shape[0]):
         v = list(exact[i])
         if v and v[0] == i:
@@ -52,8 +54,8 @@ def host_quality(ids, deg, exact):
         row = set(ids[i, :deg[i]].tolist())
         hits = sum(1 for j in range(min(10, len(v))) if v[j] in row)
         den = min(10, int(deg[i]), len(v))
-        q.append(hits / den if den else float("nan"))
-    return float(np.mean(q))
+        s = np.float32(s + (np.float32(hits) / np.float32(den) if den else np.float32("nan")))
+    return float(np.float32(s / np.float32(ids.shape[0])))
 
 
 @pytest.fixture(scope="module")
@@ -101,7 +103,7 @@ def test_index_info_matches_host(built, tmp_path):
     assert info["max_out"] == deg.max() and info["min_out"] == deg.min()
     assert abs(info["avg_out"] - deg.mean()) < 1e-9
     assert info["conn"] == host_conn(ids, deg, ep)
-    assert abs(info["quality"] - host_quality(ids, deg, exact)) < 1e-6
+    assert info["quality"] == host_quality(ids, deg, exact)
     # a graph cut in two pieces needs two traversals from node 0
     cut, deg = ids.copy(), deg.copy()
     half = ids.shape[0] // 2

@@ -112,3 +112,53 @@ def test_rejects_bad_graphs(ctx):
     ctx.load_hnsw(np.array(words, np.uint32))  # a ring: valid
     with pytest.raises(WeavessError):
         ctx.search_hnsw(base[:2], 5, 10)  # L < K
+
+
+def test_index_info_over_the_layers(ctx, layered20k):
+    """print_index_info for INDEX_HNSW: layer-0 degrees and quality, conn by a
+    walk over every layer from the enterpoint."""
+    from test_graph_io_gpu import host_quality
+    base, query, words = layered20k
+    n = base.shape[0]
+    ctx.upload_base(base)
+    ctx.load_hnsw(words)
+    # parse the words on the host
+    ep, p = int(words[0]), 2
+    fr = [None] * n
+    for _ in range(n):
+        v, t = int(words[p]), int(words[p + 1])
+        p += 2
+        fr[v] = []
+        for _l in range(t):
+            k = int(words[p])
+            fr[v].append(words[p + 1:p + 1 + k].astype(np.int64))
+            p += 1 + k
+    deg0 = np.array([len(f[0]) for f in fr])
+    w0 = int(deg0.max())
+    ids0 = np.zeros((n, w0), np.int64)
+    for v in range(n):
+        ids0[v, :deg0[v]] = fr[v][0]
+    # conn: passes from the enterpoint, then the smallest unreached id
+    seen = np.zeros(n, bool)
+    conn, root = 0, ep
+    while True:
+        conn += 1
+        stack = [root]
+        seen[root] = True
+        while stack:
+            u = stack.pop()
+            for lay in fr[u]:
+                for x in lay:
+                    if not seen[x]:
+                        seen[x] = True
+                        stack.append(int(x))
+        left = np.nonzero(~seen)[0]
+        if left.size == 0:
+            break
+        root = int(left[0])
+    exact = ds.groundtruth_fp64(base, base, 11)
+    info = ctx.index_info(use_ep="hnsw", exact_ids=exact)
+    assert info["max_out"] == deg0.max() and info["min_out"] == deg0.min()
+    assert abs(info["avg_out"] - deg0.mean()) < 1e-9
+    assert info["conn"] == conn
+    assert info["quality"] == host_quality(ids0, deg0, exact)

@@ -29,6 +29,41 @@ using namespace wv;
 
 namespace {
 
+// one BFS level over the HNSW graph: a node's friends on every layer (layer 0
+// rows of width w0; layers 1.. as (count, ids) records of wu + 1 words from
+// up_off), as IndexBuilder::DFS walks INDEX_HNSW (builder.cpp:603-625)
+__global__ void k_bfs_hnsw(const uint32_t *l0, const uint32_t *deg0, uint32_t w0, const uint32_t *up_off,
+                           const uint32_t *up, uint32_t wu, const uint32_t *layers, uint32_t n, const uint32_t *front,
+                           uint32_t nfront, uint32_t *bits, uint32_t *next, uint32_t *nnext, int *status) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t f = wid; f < nfront; f += nw) {
+    const uint32_t u = front[f];
+    const uint32_t t = layers[u] ? layers[u] : 1u;
+    for (uint32_t l = 0; l < t; l++) {
+      const uint32_t *row;
+      uint32_t dg;
+      if (l == 0) {
+        row = l0 + (size_t)u * w0;
+        dg = min(deg0[u], w0);
+      } else {
+        const uint32_t *rec = up + (size_t)up_off[u] + (size_t)(l - 1) * (wu + 1);
+        dg = min(rec[0], wu);
+        row = rec + 1;
+      }
+      for (uint32_t j = lane; j < dg; j += 32) {
+        const uint32_t v = row[j];
+        if (v >= n) {
+          set_err(status, DEV_BAD_ID);
+          continue;
+        }
+        const uint32_t bit = 1u << (v & 31);
+        if (!(atomicOr(bits + (v >> 5), bit) & bit)) next[atomicAdd(nnext, 1u)] = v;
+      }
+    }
+  }
+}
+
 // per node: share of its first 10 exact neighbours (itself skipped) in its row
 __global__ void k_quality(const uint32_t *ids, const uint32_t *deg, uint32_t w, const uint32_t *ex,
                           const uint32_t *exdeg, uint32_t ew, uint32_t n, float *q) {
@@ -63,6 +98,8 @@ extern "C" {
 
 int wv_save_graph(wv_ctx *c, const char *path, int with_ep) {
   if (!c || !path) return WV_ERR_ARG;
+  WV_CHECK(c, with_ep >= WV_GRAPH_PLAIN && with_ep <= WV_GRAPH_EPS, WV_ERR_ARG,
+           "header form %d cannot be saved (HNSW graphs are load-only here)", with_ep);
   WV_CHECK(c, c->fg_n > 0, WV_ERR_STATE, "no built graph");
   const size_t n = c->fg_n, w = c->fg_w;
   std::vector<uint32_t> ids(n * w), deg(n);
@@ -148,11 +185,17 @@ int wv_load_graph(wv_ctx *c, const char *path, int with_ep) {
 int wv_index_info(wv_ctx *c, int use_ep, const uint32_t *exact_ids, const uint32_t *exact_deg, uint32_t exact_width,
                   wv_index_stats *out) {
   if (!c || !out) return WV_ERR_ARG;
-  WV_CHECK(c, c->gn == c->n && c->n > 0, WV_ERR_STATE, "no search graph");
+  // the HNSW graph: layer-0 degrees and quality, reach over every layer
+  // (degree_info / conn_info / graph_quality, builder.cpp:519-527, 573-579, 719-736)
+  const bool hnsw = use_ep == WV_GRAPH_HNSW;
+  if (hnsw) WV_CHECK(c, c->hnsw.n == c->n && c->n > 0, WV_ERR_STATE, "no HNSW graph");
+  else WV_CHECK(c, c->gn == c->n && c->n > 0, WV_ERR_STATE, "no search graph");
   WV_CUDA(c, cudaSetDevice(c->device));
-  const uint32_t n = c->n, w = c->gw;
+  const uint32_t n = c->n, w = hnsw ? c->hnsw.w0 : c->gw;
+  const uint32_t *gids = hnsw ? c->work["hn_l0"].as<uint32_t>() : c->gids.as<uint32_t>();
+  const uint32_t *gdeg = hnsw ? c->work["hn_deg0"].as<uint32_t>() : c->gdeg.as<uint32_t>();
   std::vector<uint32_t> deg(n);
-  WV_CUDA(c, cudaMemcpyAsync(deg.data(), c->gdeg.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaMemcpyAsync(deg.data(), gdeg, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
   WV_CUDA(c, cudaStreamSynchronize(c->stream));
   wv_index_stats r{};
   r.min_out = 1000000u;
@@ -176,6 +219,7 @@ int wv_index_info(wv_ctx *c, int use_ep, const uint32_t *exact_ids, const uint32
   // builder.cpp:569-595)
   std::vector<uint32_t> roots;
   if (use_ep == WV_GRAPH_EPS) roots = c->eps;
+  else if (hnsw) roots.push_back(c->hnsw.ep);
   else roots.push_back(use_ep ? c->ep : 0u);
   WV_CHECK(c, !roots.empty(), WV_ERR_STATE, "the search graph has no root list");
   for (uint32_t x : roots) WV_CHECK(c, x < n, WV_ERR_ARG, "root %u >= n", x);
@@ -200,8 +244,13 @@ int wv_index_info(wv_ctx *c, int use_ep, const uint32_t *exact_ids, const uint32
     while (nf) {
       WV_CUDA(c, cudaMemsetAsync(cnt, 0, 4, c->stream));
       const uint32_t blocks = std::min<uint32_t>((nf + 7) / 8, (uint32_t)c->sms * 32);
-      k_bfs_level<<<blocks, 256, 0, c->stream>>>(c->gids.as<uint32_t>(), c->gdeg.as<uint32_t>(), w, n, fa, nf, bits, fb,
-                                                cnt, c->d_status());
+      if (hnsw)
+        k_bfs_hnsw<<<blocks, 256, 0, c->stream>>>(gids, gdeg, w, c->work["hn_upoff"].as<uint32_t>(),
+                                                  c->work["hn_up"].as<uint32_t>(), c->hnsw.wu,
+                                                  c->work["hn_layers"].as<uint32_t>(), n, fa, nf, bits, fb, cnt,
+                                                  c->d_status());
+      else
+        k_bfs_level<<<blocks, 256, 0, c->stream>>>(gids, gdeg, w, n, fa, nf, bits, fb, cnt, c->d_status());
       WV_CUDA(c, cudaGetLastError());
       WV_CUDA(c, cudaMemcpyAsync(&nf, cnt, 4, cudaMemcpyDeviceToHost, c->stream));
       WV_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -224,15 +273,14 @@ int wv_index_info(wv_ctx *c, int use_ep, const uint32_t *exact_ids, const uint32
     WV_CUDA(c, e);
     WV_CUDA(c, cudaMemcpyAsync(dex, exact_ids, (size_t)n * exact_width * 4, cudaMemcpyHostToDevice, c->stream));
     WV_CUDA(c, cudaMemcpyAsync(dexd, exact_deg, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
-    k_quality<<<c->sms * 8, 256, 0, c->stream>>>(c->gids.as<uint32_t>(), c->gdeg.as<uint32_t>(), w, dex, dexd,
-                                                 exact_width, n, q);
+    k_quality<<<c->sms * 8, 256, 0, c->stream>>>(gids, gdeg, w, dex, dexd, exact_width, n, q);
     WV_CUDA(c, cudaGetLastError());
     std::vector<float> hq(n);
     WV_CUDA(c, cudaMemcpyAsync(hq.data(), q, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
     WV_CUDA(c, cudaStreamSynchronize(c->stream));
-    double s = 0.0;
+    float s = 0.f;  // mean_quality: a float sum in node order, then / node count (builder.cpp:716-775)
     for (float x : hq) s += x;
-    r.quality = s / n;
+    r.quality = s / (float)n;
   }
   *out = r;
   return check_device_status(c, "index info");

@@ -432,7 +432,9 @@ int wv_load_hnsw(wv_ctx *c, const uint32_t *words, size_t count) {
   uint32_t *d_deg0 = c->buf<uint32_t>("hn_deg0", n, &e);
   uint32_t *d_upoff = c->buf<uint32_t>("hn_upoff", n, &e);
   uint32_t *d_up = c->buf<uint32_t>("hn_up", up.size(), &e);
+  uint32_t *d_layers = c->buf<uint32_t>("hn_layers", n, &e);
   WV_CUDA(c, e);
+  WV_CUDA(c, cudaMemcpyAsync(d_layers, layers.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
   WV_CUDA(c, cudaMemcpyAsync(d_l0, l0.data(), l0.size() * 4, cudaMemcpyHostToDevice, c->stream));
   WV_CUDA(c, cudaMemcpyAsync(d_deg0, deg0.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
   WV_CUDA(c, cudaMemcpyAsync(d_upoff, up_off.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
