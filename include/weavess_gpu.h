@@ -111,6 +111,12 @@ int wv_load_built_graph(wv_ctx *ctx);
  * neighbours per node from one mt19937 seeded by one rand() draw, sorted by
  * distance.  Result: the current graph (width S). */
 int wv_init_random(wv_ctx *ctx, uint32_t S, wv_build_stats *stats);
+/* ComponentInitRand::InitInner (component_init.cpp:979-1025), the init of the
+ * reference's Vamana pipeline: L random neighbours per node from one mt19937
+ * seeded by one rand() draw (GenRandom, node order; the node itself
+ * skipped), each pool make_heap'd then sorted by distance as the reference
+ * does.  Result: the current graph (width L, 1 <= L <= 1024). */
+int wv_init_rand(wv_ctx *ctx, uint32_t L, wv_build_stats *stats);
 
 /* ComponentRefineNNDescent::RefineInner (component_refine.cpp:12-239) on the
  * current graph: ITER rounds of join + update with pool size L, sample S,

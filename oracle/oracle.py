@@ -45,6 +45,7 @@ def lib():
         L.orc_rand_fill.argtypes = [C.c_void_p, i32p, C.c_uint]
         L.orc_l2_rows.argtypes = [f32p, f32p, C.c_uint, C.c_uint, f32p]
         L.orc_init_random.argtypes = [f32p, C.c_uint, C.c_uint, C.c_uint, C.c_void_p, u32p, f32p, u32p]
+        L.orc_init_rand.argtypes = [f32p, C.c_uint, C.c_uint, C.c_uint, C.c_void_p, u32p, f32p, u32p]
         L.orc_nndescent.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint, C.c_uint,
                                     C.c_uint, C.c_uint, C.c_uint, C.c_void_p, C.c_int, u32p, f32p, u32p, u64p]
         L.orc_efanna.argtypes = L.orc_nndescent.argtypes[:12] + [C.c_void_p, u32p, f32p, u32p, u64p]
@@ -115,6 +116,17 @@ def l2_rows(a, b):
     out = np.empty(a.shape[0], dtype=np.float32)
     lib().orc_l2_rows(a, b, a.shape[0], a.shape[1], out)
     return out
+
+
+def init_rand(base, L, rnd: Rand) -> Graph:
+    """INIT_RAND (the Vamana init): L random neighbours per node, sorted."""
+    base = _c(base, np.float32)
+    n, d = base.shape
+    ids = np.zeros((n, L), np.uint32)
+    dist = np.zeros((n, L), np.float32)
+    deg = np.zeros(n, np.uint32)
+    assert lib().orc_init_rand(base, n, d, L, rnd.h, ids, dist, deg) == 0
+    return Graph(ids, dist, deg)
 
 
 def init_random(base, S, rnd: Rand) -> Graph:

@@ -384,6 +384,32 @@ FinalGraph init_random(const Data &D, unsigned S, GlibcRand &rnd) {
   return g;
 }
 
+// ComponentInitRand::InitInner (component_init.cpp:979-1025), the Vamana
+// init: one rand() seeds an mt19937 from which every node, in node order,
+// draws L ids (GenRandom); the node itself is skipped; the pool (Neighbor,
+// flag true) is make_heap'd, then std::sort'ed -- the heap arrangement is
+// the order the sort starts from, which decides equal distances
+FinalGraph init_rand(const Data &D, unsigned L, GlibcRand &rnd) {
+  FinalGraph g(D.n);
+  std::mt19937 rng(rnd.next());
+  std::vector<unsigned> tmp(L);
+  std::vector<Neighbor> pool;
+  for (unsigned i = 0; i < D.n; i++) {
+    gen_random(rng, tmp.data(), L, D.n);
+    pool.clear();
+    for (unsigned j = 0; j < L; j++) {
+      const unsigned id = tmp[j];
+      if (id == i) continue;
+      pool.emplace_back(id, l2(D.row(i), D.row(id), D.d), true);
+    }
+    std::make_heap(pool.begin(), pool.end());
+    std::sort(pool.begin(), pool.end());
+    g[i].reserve(pool.size());
+    for (auto &x : pool) g[i].emplace_back(x.id, x.distance);
+  }
+  return g;
+}
+
 // ---------------------------------------------------------------- greedy searches
 // Seeds for a build-time greedy search: the first L ids of `enter`'s row, then
 // rand() % N draws that skip flagged ids (component_candidate.cpp:17-31,
@@ -1132,6 +1158,14 @@ void orc_rand_fill(void *r, int *out, unsigned n) {
 // L2 in the reference's summation order, row by row (for tests)
 void orc_l2_rows(const float *a, const float *b, unsigned n, unsigned d, float *out) {
   for (unsigned i = 0; i < n; i++) out[i] = l2(a + (size_t)i * d, b + (size_t)i * d, d);
+}
+
+// INIT_RAND: out rows of width L (self hits dropped, so deg may be L-1)
+int orc_init_rand(const float *base, unsigned n, unsigned d, unsigned L, void *rnd, unsigned *ids, float *dist,
+                  unsigned *deg) {
+  Data D{base, n, d};
+  FinalGraph g = init_rand(D, L, *(GlibcRand *)rnd);
+  return graph_to_arrays(g, ids, dist, deg, L);
 }
 
 // INIT_RANDOM: out rows of width S (self hits dropped, so deg may be S-1)

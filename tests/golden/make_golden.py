@@ -50,7 +50,9 @@ CASES = {
                                   "search_rand:40", "policy:centroid_ascend"],
                                  ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:30", "search_sub:30"],
                                  ["init_random", "efanna", "load:efanna", "search_rand:30"],
-                                 ["hnsw", "search_hnsw:20", "search_hnsw:50", "search_nsw:30"]]),
+                                 ["hnsw", "search_hnsw:20", "search_hnsw:50", "search_nsw:30"],
+                                 ["init_rand", "vamana", "vamana", "load:vamana", "search_centroid:30",
+                                  "policy:centroid_set_recall"]]),
     # S > 16 and L_refine > K: introsort on ties, rand() seed fill in the
     # candidate search, heavy reverse-list overflow (R=12)
     "int_n1500_s20": dict(data=lambda: ds.int_mixture(1500, 128, 4, seed=3, n_query=40),
@@ -71,7 +73,8 @@ CASES = {
                                    "policy:rand_ascend"],
                                   ["init_random", "nndescent", "ssg", "load:ssg", "search_sub:20"],
                                   ["init_random", "efanna"],
-                                  ["hnsw", "search_hnsw:16", "search_nsw:24"]]),
+                                  ["hnsw", "search_hnsw:16", "search_nsw:24"],
+                                  ["init_rand", "vamana", "load:vamana", "search_centroid:20"]]),
     # real-valued unit vectors (FP32 summation order matters), d=32
     "unit_n1200": dict(data=lambda: ds.unit_mixture(1200, 32, 20, seed=2, n_query=40),
                        params=dict(S=10, K=20, L=40, ITER=6, R=50, L_refine=40, R_refine=16, C_refine=120,
@@ -81,7 +84,8 @@ CASES = {
                                    "vamana", "load:vamana", "search_centroid:30"],
                                   ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:24", "search_sub:24"],
                                   ["init_random", "efanna", "load:efanna", "search_rand:20"],
-                                  ["hnsw", "search_hnsw:24", "search_nsw:24"]]),
+                                  ["hnsw", "search_hnsw:24", "search_nsw:24"],
+                                  ["init_rand", "vamana", "vamana", "load:vamana", "search_centroid:24"]]),
     # tiny graph: GenRandom wrap-around, self hits, L = N-1 style edges
     "tiny_n60": dict(data=lambda: ds.int_mixture(60, 8, 3, seed=9, n_query=10),
                      params=dict(S=10, K=8, L=16, ITER=4, R=6, L_refine=12, R_refine=6, C_refine=30, alpha=1.2,
@@ -90,7 +94,8 @@ CASES = {
                                  "vamana", "load:vamana", "search_centroid:12"],
                                 ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:10", "search_sub:10"],
                                 ["init_random", "efanna"],
-                                ["hnsw", "search_hnsw:10", "search_hnsw:30", "search_nsw:12"]]),
+                                ["hnsw", "search_hnsw:10", "search_hnsw:30", "search_nsw:12"],
+                                ["init_rand", "vamana", "vamana", "load:vamana", "search_centroid:12"]]),
 }
 
 

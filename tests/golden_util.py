@@ -66,6 +66,9 @@ def replay_oracle(f, pi, on_search=None, on_graph=None):
         if kind == "init_random":
             g = O.init_random(base, p["S"], rnd)
             exp = key + "init"
+        elif kind == "init_rand":
+            g = O.init_rand(base, p["L"], rnd)
+            exp = key + "initrand"
         elif kind == "nndescent":
             g = O.nndescent(base, g, p["S"], p["K"], p["L"], p["ITER"], p["R"], rnd)
             exp = key + "nnd"

@@ -35,6 +35,9 @@ def _replay(ctx, f, pi):
         if kind == "init_random":
             ctx.init_random(p["S"])
             exp = key + "init"
+        elif kind == "init_rand":
+            ctx.init_rand(p["L"])
+            exp = key + "initrand"
         elif kind == "nndescent":
             ctx.nnd_refine(p["S"], p["K"], p["L"], p["ITER"], p["R"])
             exp = key + "nnd"
@@ -181,3 +184,27 @@ def test_ssg_graph_file_and_conn(ctx, mix20k, tmp_path):
     info = ctx.index_info(use_ep="eps")
     assert info["conn"] == 1
     assert info["max_out"] == int(deg.max()) and info["min_out"] == int(deg.min())
+
+
+@pytest.mark.parametrize("L", [64])
+def test_vamana_pipeline_matches_oracle_20k(ctx, mix20k, L):
+    """The reference's Vamana build (test/main.cpp:168-172): INIT_RAND, then
+    REFINE_VAMANA twice (alpha 1.2, then 2 as the reference leaves it), then
+    a centroid-entry search."""
+    base, query, _ = mix20k
+    ctx.upload_base(base)
+    ctx.srand(1)
+    st = ctx.init_rand(L)
+    ro = O.Rand(1)
+    g = O.init_rand(base, L, ro)
+    ids, dist, deg, _ = ctx.get_graph()
+    assert rows_equal(ids, dist, deg, g.ids, g.dist, g.deg) == 0, st
+    for alpha in (1.2, 2.0):
+        ctx.vamana_refine(40, 32, alpha, 0)
+        g = O.vamana(base, g, 40, 32, alpha, ro)
+        ids, dist, deg, ep = ctx.get_graph()
+        assert ep == g.ep and rows_equal(ids, dist, deg, g.ids, g.dist, g.deg) == 0
+    ctx.load_built_graph()
+    res, dc, hc = ctx.search(query, 64, 10, entry="centroid")
+    eres, edc, ehc = O.search(base, query, g, 64, ro, entry="centroid")
+    assert np.array_equal(res, eres) and (dc, hc) == (edc, ehc)

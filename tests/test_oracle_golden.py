@@ -48,6 +48,9 @@ def test_oracle_replays_reference(name):
             if kind == "init_random":
                 g = O.init_random(base, p["S"], rnd)
                 exp = graph_of(f, key + "init")
+            elif kind == "init_rand":
+                g = O.init_rand(base, p["L"], rnd)
+                exp = graph_of(f, key + "initrand")
             elif kind == "nndescent":
                 g = O.nndescent(base, g, p["S"], p["K"], p["L"], p["ITER"], p["R"], rnd)
                 exp = graph_of(f, key + "nnd")

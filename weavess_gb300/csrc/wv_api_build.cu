@@ -99,6 +99,19 @@ int wv_init_random(wv_ctx *c, uint32_t S, wv_build_stats *stats) {
   return rc;
 }
 
+int wv_init_rand(wv_ctx *c, uint32_t L, wv_build_stats *stats) {
+  if (!c) return WV_ERR_ARG;
+  WV_CUDA(c, cudaSetDevice(c->device));
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = init_rand_gpu(c, L);
+  if (stats) {
+    *stats = wv_build_stats{};
+    stats->rand_draws = 1;
+    stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return rc;
+}
+
 int wv_nnd_refine(wv_ctx *c, uint32_t S, uint32_t K, uint32_t L, uint32_t ITER, uint32_t R, wv_build_stats *stats) {
   if (!c) return WV_ERR_ARG;
   WV_CUDA(c, cudaSetDevice(c->device));

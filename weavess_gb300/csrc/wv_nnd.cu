@@ -161,6 +161,70 @@ __global__ void __launch_bounds__(INIT_WARPS * 32)
   }
 }
 
+// ---------------------------------------------------------------- INIT_RAND
+// ComponentInitRand::InitInner (component_init.cpp:979-1025): node i draws L
+// ids by GenRandom from the shared mt19937 stream (outputs [i (L + 1),
+// (i + 1)(L + 1))), skips itself, takes the distances (exact reference order,
+// a lane per row), and its pool goes through make_heap then std::sort (the
+// heap arrangement is where the sort starts, which settles equal
+// distances); one warp per node, the two sequential steps on one lane.
+constexpr int IR_WARPS = 4;
+__host__ __device__ inline size_t init_rand_warp_bytes(uint32_t L, uint32_t d) {
+  // a multiple of 16 bytes, so that every warp's query copy starts 16-byte aligned
+  const size_t b = (size_t)pow2_ge(L) * 4 + (size_t)L * 4 + (size_t)L * sizeof(DI) + (((size_t)d * 4 + 15) & ~size_t(15));
+  return (b + 15) & ~size_t(15);
+}
+__global__ void __launch_bounds__(IR_WARPS * 32)
+    k_init_rand(const float *__restrict__ base, uint32_t n, uint32_t d, uint32_t L, const uint32_t *__restrict__ mt,
+                uint32_t *ids, float *dist, uint32_t *deg) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint8_t *p = smem + (size_t)warp * init_rand_warp_bytes(L, d);
+  float *qv = reinterpret_cast<float *>(p);
+  p += ((size_t)d * 4 + 15) & ~size_t(15);
+  DI *pool = reinterpret_cast<DI *>(p);
+  p += (size_t)L * sizeof(DI);
+  uint32_t *gen = reinterpret_cast<uint32_t *>(p);
+  p += (size_t)L * 4;
+  uint32_t *key = reinterpret_cast<uint32_t *>(p);
+  const unsigned lt = (1u << lane) - 1u;
+  for (uint32_t i = blockIdx.x * IR_WARPS + warp; i < n; i += gridDim.x * IR_WARPS) {
+    const uint32_t *r = mt + (size_t)i * (L + 1);
+    for (uint32_t j = lane; j < L; j += 32) key[j] = r[j] % (n - L);
+    for (uint32_t k = lane; k < d; k += 32) qv[k] = base[(size_t)i * d + k];
+    __syncwarp();
+    warp_gen_random_tail(key, L, r[L] % n, n, gen, lane);
+    // the pool in draw order without the node itself
+    uint32_t cnt = 0;
+    for (uint32_t b = 0; b < L; b += 32) {
+      const uint32_t j = b + lane;
+      const uint32_t id = j < L ? gen[j] : i;
+      const bool keep = j < L && id != i;
+      const unsigned km = __ballot_sync(FULL, keep);
+      if (keep) {
+        const float4 *x = reinterpret_cast<const float4 *>(qv);
+        const float4 *y = reinterpret_cast<const float4 *>(base + (size_t)id * d);
+        float acc = 0.f;
+        for (uint32_t g = 0; g < (d >> 2); g++) acc = __fadd_rn(acc, group4(x[g], __ldg(y + g)));
+        pool[cnt + __popc(km & lt)] = DI{acc, id};
+      }
+      cnt += __popc(km);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      stl::make_heap(pool, (int)cnt, DILess());
+      stl::sort(pool, (int)cnt, DILess());
+    }
+    __syncwarp();
+    for (uint32_t j = lane; j < cnt; j += 32) {
+      ids[(size_t)i * L + j] = pool[j].i;
+      dist[(size_t)i * L + j] = pool[j].d;
+    }
+    if (lane == 0) deg[i] = cnt;
+    __syncwarp();
+  }
+}
+
 // ---------------------------------------------------------------- NN-Descent state
 struct Nnd {
   uint32_t n, d, S, K, L, R, capn, capo;
@@ -705,6 +769,37 @@ int init_random_gpu(wv_ctx *c, uint32_t S) {
   c->fg_has_ep = false;
   c->fg_eps.clear();
   return check_device_status(c, "init_random");
+}
+
+int init_rand_gpu(wv_ctx *c, uint32_t L) {
+  WV_CHECK(c, c->n > 0, WV_ERR_STATE, "no base uploaded");
+  WV_CHECK(c, L >= 1 && L <= 1024, WV_ERR_LIMIT, "L=%u: this build supports 1 <= L <= 1024", L);
+  WV_CHECK(c, L < c->n, WV_ERR_ARG, "L=%u must be smaller than n=%u", L, c->n);
+  WV_CHECK(c, c->d % 4 == 0, WV_ERR_LIMIT, "dimension %u is not a multiple of 4", c->d);
+  cudaError_t e = cudaSuccess;
+  const size_t count = (size_t)c->n * (L + 1);
+  uint32_t *mt = c->buf<uint32_t>("mt", count, &e);
+  WV_CUDA(c, e);
+  // `std::mt19937 rng(rand())`: one draw from the process rand() stream
+  const uint32_t seed = (uint32_t)c->rnd.next();
+  int rc = mt19937_gpu(c, seed, mt, count);
+  if (rc) return rc;
+  WV_CUDA(c, c->fg_ids.ensure((size_t)c->n * L * 4));
+  WV_CUDA(c, c->fg_dist.ensure((size_t)c->n * L * 4));
+  WV_CUDA(c, c->fg_deg.ensure((size_t)c->n * 4));
+  const size_t smem = IR_WARPS * init_rand_warp_bytes(L, c->d);
+  WV_CHECK(c, smem <= 227 * 1024, WV_ERR_LIMIT, "L=%u d=%u need %zu bytes of shared memory", L, c->d, smem);
+  WV_CUDA(c, cudaFuncSetAttribute(k_init_rand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int blocks = (int)std::min<size_t>((c->n + IR_WARPS - 1) / IR_WARPS, (size_t)c->sms * 16);
+  k_init_rand<<<blocks, IR_WARPS * 32, smem, c->stream>>>(c->base.as<float>(), c->n, c->d, L, mt,
+                                                           c->fg_ids.as<uint32_t>(), c->fg_dist.as<float>(),
+                                                           c->fg_deg.as<uint32_t>());
+  WV_CUDA(c, cudaGetLastError());
+  c->fg_n = c->n;
+  c->fg_w = L;
+  c->fg_has_ep = false;
+  c->fg_eps.clear();
+  return check_device_status(c, "init_rand");
 }
 
 int nndescent_gpu(wv_ctx *c, const NndParams &p, NndStats *st) {

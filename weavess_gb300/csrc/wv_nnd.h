@@ -1,4 +1,4 @@
-// Graph construction on the GPU: INIT_RANDOM and REFINE_NN_DESCENT.
+// Graph construction on the GPU: INIT_RANDOM, INIT_RAND, REFINE_NN_DESCENT and REFINE_EFANNA.
 #pragma once
 #include <cstdint>
 
@@ -23,6 +23,8 @@ struct NndStats {
 
 // ComponentInitRandom::InitInner: rows of width S into ctx->fg_*
 int init_random_gpu(wv_ctx *c, uint32_t S);
+// ComponentInitRand::InitInner (the Vamana init): rows of width L into ctx->fg_*
+int init_rand_gpu(wv_ctx *c, uint32_t L);
 // ComponentRefineNNDescent::RefineInner / ComponentRefineEFANNA::RefineInner:
 // ctx->fg_* (init graph) -> ctx->fg_* (width K)
 int nndescent_gpu(wv_ctx *c, const NndParams &p, NndStats *st);

@@ -156,6 +156,12 @@ class Context:
         self._check(self.L.wv_init_random(self.h, S, C.byref(st)))
         return st.as_dict()
 
+    def init_rand(self, L: int):
+        """INIT_RAND (the Vamana pipeline's init): L random neighbours per node."""
+        st = _lib.BuildStats()
+        self._check(self.L.wv_init_rand(self.h, L, C.byref(st)))
+        return st.as_dict()
+
     def nnd_refine(self, S: int, K: int, L: int, ITER: int, R: int):
         st = _lib.BuildStats()
         self._check(self.L.wv_nnd_refine(self.h, S, K, L, ITER, R, C.byref(st)))
