@@ -264,16 +264,32 @@ def run_learned(ctx, cfg, base, query, gt, args, dev, stream, flush):
     log(f"learn_fit {fit_s:.1f}s {rep}")
     gtv = knn_fp64(base, val, 10)
     ctx.set_precision("bf16", rerank=0)
-    chosen = None
-    for m in (0.5, 0.75, 1.0, 1.25, 1.5, 2.0, 2.5, 3.0, 4.0, 6.0, 8.0):
+    def val_recall(m):
         ctx.learn_set_margin(m)
         ctx.srand(4321)
         rv, _, _ = ctx.search_learned(val, cfg["k"])
         r = recall(rv, gtv, cfg["k"])
-        log(f"margin {m:.2f} val recall {r:.4f}")
+        log(f"margin {m:.3f} val recall {r:.4f}")
+        return r
+
+    # the smallest margin of a coarse grid whose validation recall clears the
+    # target (with 0.005 to spare), then bisected against the grid point below
+    goal = cfg["target_recall"] + 0.005
+    chosen, below = None, None
+    for m in (0.5, 0.75, 1.0, 1.25, 1.5, 2.0, 2.5, 3.0, 4.0, 6.0, 8.0):
         chosen = m
-        if r >= cfg["target_recall"] + 0.005:
+        if val_recall(m) >= goal:
             break
+        below = m
+    if below is not None and chosen != below:
+        lo, hi = below, chosen
+        for _ in range(3):
+            mid = (lo + hi) / 2
+            if val_recall(mid) >= goal:
+                hi = mid
+            else:
+                lo = mid
+        chosen = hi
     ctx.learn_set_margin(chosen)
     nq, K = query.shape[0], cfg["k"]
     # the batched form: a plan bound to device buffers, launch shape tuned on
