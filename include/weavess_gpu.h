@@ -265,6 +265,7 @@ int wv_draw_seeds_device(wv_ctx *ctx, uint32_t nq, uint32_t L, uint32_t *d_seeds
 #define WV_GRAPH_EP 1    /* one entry point ep_ (INDEX_NSG, INDEX_VAMANA) */
 #define WV_GRAPH_EPS 2   /* root count, then the roots eps_ (INDEX_SSG) */
 #define WV_GRAPH_HNSW 3  /* the INDEX_HNSW file (load only, into the HNSW search graph) */
+#define WV_GRAPH_NSW 4   /* the INDEX_NSW file (load only: a one-layer HNSW graph, node 0 first) */
 /* The per-node graph file of IndexBuilder::save_graph / load_graph
  * (src/builder.cpp:918-1095): the header (WV_GRAPH_*), then, per node, its
  * degree and ids (u32 each).  Save writes the built graph (final_graph_);

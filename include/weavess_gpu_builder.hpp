@@ -20,7 +20,7 @@
 // REFINE_VAMANA, REFINE_SSG, REFINE_EFANNA; search entries RAND, CENTROID,
 // SUB_CENTROID (ROUTER_GREEDY) and NONE (ROUTER_HNSW, ROUTER_NSW); the three
 // L policies; graph files KGRAPH / EFANNA (no header), NSG / VAMANA (entry
-// point), SSG (roots), HNSW (load only).  The rand() values the components
+// point), SSG (roots), HNSW and NSW (load only).  The rand() values the components
 // draw come from the process's own rand(), as in the reference.
 #pragma once
 
@@ -251,6 +251,7 @@ class IndexBuilder {
     if (type == INDEX_NSG || type == INDEX_VAMANA) hdr = WV_GRAPH_EP;
     else if (type == INDEX_SSG) hdr = WV_GRAPH_EPS;
     else if (type == INDEX_HNSW) hdr = WV_GRAPH_HNSW;
+    else if (type == INDEX_NSW) hdr = WV_GRAPH_NSW;
     else if (type == INDEX_EXACT_KNNG) return load_exact(graph_file);
     else if (type != INDEX_KGRAPH && type != INDEX_EFANNA) detail::die("load_graph: type not supported here");
     {

@@ -269,6 +269,23 @@ def search_hnsw(base, query, words, L, K=10, router="hnsw"):
     return res, int(cnt[0]), int(cnt[1])
 
 
+def nsw_to_hnsw_words(words, n):
+    """An INDEX_NSW file's words (records of node id, count, ids; a node's
+    friends appended in file order, builder.cpp:1171-1189) as a one-layer
+    INDEX_HNSW graph with node 0 as its enterpoint (where ROUTER_NSW starts)."""
+    w = np.asarray(words, np.uint32)
+    fr = [[] for _ in range(n)]
+    p = 0
+    while p + 2 <= w.size:
+        v, k = int(w[p]), int(w[p + 1])
+        fr[v] += w[p + 2:p + 2 + k].tolist()
+        p += 2 + k
+    out = [0, 0]
+    for v in range(n):
+        out += [v, 1, len(fr[v])] + fr[v]
+    return np.array(out, np.uint32)
+
+
 def search_seeds(n, nq, g: Graph, L, rnd: Rand, entry="rand"):
     seeds = np.zeros((nq, L), np.uint32)
     eps, ne = _eps(g, entry)

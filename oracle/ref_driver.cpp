@@ -17,7 +17,8 @@
 // usage: ref_driver base.fvecs query.fvecs gt.ivecs outprefix key=val ... -- step ...
 //   steps: init_random | init_rand | nndescent | efanna | vamana | nsg | ssg | load:<kgraph|vamana|nsg|ssg|efanna>
 //          | hnsw | search_rand:<L> | search_centroid:<L> | search_sub:<L> | search_hnsw:<L>
-//          | search_nsw:<L> | policy:<rand|centroid>_<set_recall|ascend> | rand_probe
+//          | search_nsw:<L> | nsw | search_nswidx:<L> | policy:<rand|centroid>_<set_recall|ascend>
+//          | rand_probe
 //   (search_sub: SEARCH_ENTRY_SUB_CENTROID, the entry the reference's SSG
 //   test searches with, test/main.cpp:117)
 #include <bits/stdc++.h>
@@ -115,6 +116,38 @@ int main(int argc, char **argv) {
       builder->init(INIT_HNSW, false);
       std::string gf = prefix + ".hnswgraph.bin";
       builder->save_graph(INDEX_HNSW, &gf[0]);
+    } else if (step == "nsw") {
+      // INIT_NSW (component_init.cpp:1242-1340), one thread; the INDEX_NSW file
+      // the reference writes for it (builder.cpp:987-999) dumped byte for byte
+      builder->init(INIT_NSW, false);
+      std::string gf = prefix + ".nswgraph.bin";
+      builder->save_graph(INDEX_NSW, &gf[0]);
+    } else if (step == "search_nswidx") {
+      // ROUTER_NSW over the graph load_graph(INDEX_NSW) reads back (builder.cpp:1171-1189)
+      std::string gf = prefix + ".nswgraph.bin";
+      builder->load_graph(INDEX_NSW, &gf[0]);
+      unsigned L = (unsigned)std::stoul(arg);
+      idx->getParam().set<unsigned>("K_search", 10);
+      idx->getParam().set<unsigned>("L_search", L);
+      auto *r = new ComponentSearchRouteNSW(idx);
+      idx->resetDistCount();
+      idx->resetHopCount();
+      unsigned nq = idx->getQueryLen();
+      std::vector<std::vector<unsigned>> res(nq);
+      for (unsigned i = 0; i < nq; i++) {
+        std::vector<Index::Neighbor> pool;
+        r->RouteInner(i, pool, res[i]);
+      }
+      std::string out = prefix + "." + step + "_" + arg + ".bin";
+      FILE *f = fopen(out.c_str(), "wb");
+      fwrite(&nq, 4, 1, f);
+      unsigned k = 10;
+      fwrite(&k, 4, 1, f);
+      for (unsigned i = 0; i < nq; i++) fwrite(res[i].data(), 4, 10, f);
+      unsigned dc = idx->getDistCount(), hc = idx->getHopCount();
+      fwrite(&dc, 4, 1, f);
+      fwrite(&hc, 4, 1, f);
+      fclose(f);
     } else if (step == "search_hnsw" || step == "search_nsw") {
       // ROUTER_HNSW / ROUTER_NSW (component_route.cpp:56-260) over the graph
       // as load_graph(INDEX_HNSW) reads it back

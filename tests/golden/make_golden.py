@@ -42,7 +42,7 @@ CASES = {
     "int_n2000": dict(data=lambda: ds.int_mixture(2000, 128, 8, seed=1, n_query=50),
                       params=dict(S=10, K=20, L=40, ITER=8, R=100, L_refine=40, R_refine=16, C_refine=200,
                                   alpha=1.2, A=60, n_try=5, max_m=8, max_m0=16, ef_construction=40, mult=0,
-                                  n_threads=1),
+                                  n_threads=1, NN=10),
                       pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:20", "search_rand:50",
                                   "vamana", "load:vamana", "search_centroid:30", "search_rand:17",
                                   "policy:rand_set_recall"],
@@ -52,7 +52,8 @@ CASES = {
                                  ["init_random", "efanna", "load:efanna", "search_rand:30"],
                                  ["hnsw", "search_hnsw:20", "search_hnsw:50", "search_nsw:30"],
                                  ["init_rand", "vamana", "vamana", "load:vamana", "search_centroid:30",
-                                  "policy:centroid_set_recall"]]),
+                                  "policy:centroid_set_recall"],
+                                 ["nsw", "search_nswidx:20", "search_nswidx:50"]]),
     # S > 16 and L_refine > K: introsort on ties, rand() seed fill in the
     # candidate search, heavy reverse-list overflow (R=12)
     "int_n1500_s20": dict(data=lambda: ds.int_mixture(1500, 128, 4, seed=3, n_query=40),
@@ -89,13 +90,14 @@ CASES = {
     # tiny graph: GenRandom wrap-around, self hits, L = N-1 style edges
     "tiny_n60": dict(data=lambda: ds.int_mixture(60, 8, 3, seed=9, n_query=10),
                      params=dict(S=10, K=8, L=16, ITER=4, R=6, L_refine=12, R_refine=6, C_refine=30, alpha=1.2,
-                                 A=60, n_try=3, max_m=4, max_m0=8, ef_construction=16, mult=0, n_threads=1),
+                                 A=60, n_try=3, max_m=4, max_m0=8, ef_construction=16, mult=0, n_threads=1, NN=5),
                      pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:10", "search_rand:20",
                                  "vamana", "load:vamana", "search_centroid:12"],
                                 ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:10", "search_sub:10"],
                                 ["init_random", "efanna"],
                                 ["hnsw", "search_hnsw:10", "search_hnsw:30", "search_nsw:12"],
-                                ["init_rand", "vamana", "vamana", "load:vamana", "search_centroid:12"]]),
+                                ["init_rand", "vamana", "vamana", "load:vamana", "search_centroid:12"],
+                                ["nsw", "search_nswidx:10", "search_nswidx:30"]]),
 }
 
 
@@ -142,6 +144,8 @@ def run_case(name, spec):
                     out[key + ".acc"] = rec[:, 3].copy().view(np.float32)
                 elif key.endswith(".hnswgraph"):
                     out[f"p{pi}.hnsw.words"] = np.fromfile(os.path.join(tmp, f), np.uint32)
+                elif key.endswith(".nswgraph"):
+                    out[f"p{pi}.nsw.words"] = np.fromfile(os.path.join(tmp, f), np.uint32)
                 elif key.endswith(".ssgeps"):
                     out[key[: -len("eps")] + ".eps"] = np.fromfile(os.path.join(tmp, f), np.uint32)[1:]
                 elif "search" in key:

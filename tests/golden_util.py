@@ -102,8 +102,11 @@ def replay_oracle(f, pi, on_search=None, on_graph=None):
             got = P.set_recall(fn, f["gt"])[0] if pol == "set_recall" else P.ascend(fn, f["gt"])
             yield s, f"{key}policy_{arg}", got
             continue
-        elif kind in ("search_hnsw", "search_nsw"):
-            router, L = kind[len("search_"):], int(arg)
+        elif kind == "nsw":
+            hwords = O.nsw_to_hnsw_words(f[key + "nsw.words"], base.shape[0])
+            continue
+        elif kind in ("search_hnsw", "search_nsw", "search_nswidx"):
+            router, L = ("hnsw" if kind == "search_hnsw" else "nsw"), int(arg)
             got = (on_search(router, L, hwords, rnd) if on_search
                    else O.search_hnsw(base, query, hwords, L, router=router))
             yield s, f"{key}{kind}_{arg}", got

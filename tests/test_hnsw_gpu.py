@@ -18,14 +18,31 @@ def ctx():
     return Context(0)
 
 
-def _hnsw_cases():
+def _hnsw_cases(first="hnsw"):
     out = []
     for name in cases():
         f = load(name)
         for pi, steps in enumerate(f["pipelines"]):
-            if steps[0] == "hnsw":
+            if steps[0] == first:
                 out.append((name, pi))
     return out
+
+
+@pytest.mark.parametrize("name,pi", _hnsw_cases("nsw"))
+def test_nsw_index_matches_reference_golden(ctx, name, pi, tmp_path):
+    """INIT_NSW graphs in the reference's INDEX_NSW file, read by the library,
+    routed by ROUTER_NSW."""
+    f = load(name)
+    ctx.upload_base(f["base"])
+    path = str(tmp_path / "g.nsw")
+    f[f"p{pi}.nsw.words"].astype(np.uint32).tofile(path)
+    ctx.load_graph(path, with_ep="nsw")
+    for s in f["pipelines"][pi][1:]:
+        kind, _, arg = s.partition(":")
+        res, dc, hc = ctx.search_hnsw(f["query"], int(arg), 10, router="nsw")
+        k = f"p{pi}.{kind}_{arg}"
+        assert np.array_equal(res, f[k + ".res"]), (name, s)
+        assert [dc, hc] == f[k + ".counts"].tolist(), (name, s)
 
 
 @pytest.mark.parametrize("name,pi", _hnsw_cases())

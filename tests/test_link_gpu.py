@@ -91,8 +91,8 @@ def _replay(ctx, f, pi):
 def test_full_pipelines_match_reference_golden(ctx, name):
     f = load(name)
     for pi, steps in enumerate(f["pipelines"]):
-        if steps[0] == "hnsw":
-            continue  # HNSW routing over the reference's graph: tests/test_hnsw_gpu.py
+        if steps[0] in ("hnsw", "nsw"):
+            continue  # HNSW / NSW routing over the reference's graphs: tests/test_hnsw_gpu.py
         assert _replay(ctx, f, pi)
 
 

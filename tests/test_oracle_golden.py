@@ -77,8 +77,12 @@ def test_oracle_replays_reference(name):
             elif kind == "hnsw":
                 hwords = f[key + "hnsw.words"]
                 continue
-            elif kind in ("search_hnsw", "search_nsw"):
-                res, dc, hc = O.search_hnsw(base, query, hwords, int(arg), router=kind[len("search_"):])
+            elif kind == "nsw":
+                hwords = O.nsw_to_hnsw_words(f[key + "nsw.words"], base.shape[0])
+                continue
+            elif kind in ("search_hnsw", "search_nsw", "search_nswidx"):
+                router = "hnsw" if kind == "search_hnsw" else "nsw"
+                res, dc, hc = O.search_hnsw(base, query, hwords, int(arg), router=router)
                 k = f"{key}{kind}_{arg}"
                 assert np.array_equal(res, f[k + ".res"]), (name, s)
                 assert [dc, hc] == f[k + ".counts"].tolist(), (name, s)

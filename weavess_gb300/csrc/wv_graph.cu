@@ -130,13 +130,36 @@ int wv_load_graph(wv_ctx *c, const char *path, int with_ep) {
   WV_CHECK(c, c->n > 0, WV_ERR_STATE, "upload the base first (the graph's node count must match it)");
   FILE *f = fopen(path, "rb");
   WV_CHECK(c, f, WV_ERR_ARG, "cannot open %s", path);
-  if (with_ep == WV_GRAPH_HNSW) {  // the whole file, as words
+  if (with_ep == WV_GRAPH_HNSW || with_ep == WV_GRAPH_NSW) {  // the whole file, as words
     std::vector<uint32_t> w;
     uint32_t buf[4096];
     size_t got;
     while ((got = fread(buf, 4, 4096, f)) > 0) w.insert(w.end(), buf, buf + got);
     fclose(f);
-    return wv_load_hnsw(c, w.data(), w.size());
+    if (with_ep == WV_GRAPH_HNSW) return wv_load_hnsw(c, w.data(), w.size());
+    // INDEX_NSW (builder.cpp:987-999, 1171-1189): records of (node id, count,
+    // ids) until the end; a node's friends are appended in file order.  It
+    // becomes a one-layer HNSW graph whose enterpoint is node 0, the node
+    // ROUTER_NSW starts from
+    const uint32_t n = c->n;
+    std::vector<std::vector<uint32_t>> fr(n);
+    size_t p = 0;
+    while (p + 2 <= w.size()) {
+      const uint32_t id = w[p], gk = w[p + 1];
+      p += 2;
+      WV_CHECK(c, id < n && p + gk <= w.size(), WV_ERR_ARG, "%s: bad NSW record at word %zu", path, p - 2);
+      for (uint32_t k = 0; k < gk; k++) WV_CHECK(c, w[p + k] < n, WV_ERR_ARG, "%s: id %u >= n", path, w[p + k]);
+      fr[id].insert(fr[id].end(), w.begin() + p, w.begin() + p + gk);
+      p += gk;
+    }
+    std::vector<uint32_t> hw{0u, 0u};
+    for (uint32_t v = 0; v < n; v++) {
+      hw.push_back(v);
+      hw.push_back(1u);
+      hw.push_back((uint32_t)fr[v].size());
+      hw.insert(hw.end(), fr[v].begin(), fr[v].end());
+    }
+    return wv_load_hnsw(c, hw.data(), hw.size());
   }
   uint32_t ep = 0;
   std::vector<uint32_t> eps;

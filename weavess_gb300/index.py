@@ -301,7 +301,7 @@ class Context:
     # graph-file headers: False / "plain" (none), True / "ep" (ep_), "eps" (SSG roots)
     @staticmethod
     def _hdr(with_ep):
-        return {False: 0, True: 1, "plain": 0, "ep": 1, "eps": 2, "hnsw": 3}[with_ep]
+        return {False: 0, True: 1, "plain": 0, "ep": 1, "eps": 2, "hnsw": 3, "nsw": 4}[with_ep]
 
     def save_graph(self, path: str, with_ep=False):
         self._check(self.L.wv_save_graph(self.h, path.encode(), self._hdr(with_ep)))
