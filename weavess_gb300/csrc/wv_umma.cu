@@ -16,7 +16,9 @@
 //    complete; a stage is refilled only after its previous commit arrived;
 //  * the accumulator (128 lanes x 128 FP32 columns of tensor memory, taken
 //    with tcgen05.alloc) is read back by the 4 warps with tcgen05.ld (warp w
-//    owns lanes 32w..32w+31 = rows of the tile) for the epilogue.
+//    owns lanes 32w..32w+31 = rows of the tile) and turned through shared
+//    memory so that the epilogue (bias, ReLU, FP32 / BF16 stores) writes
+//    whole rows with the lanes along the columns.
 // Every mbarrier wait is bounded: on time-out the kernel sets an error flag,
 // waits (bounded) for its outstanding MMAs, frees its tensor memory and
 // returns.
@@ -180,8 +182,12 @@ __global__ void __launch_bounds__(128) k_gemm_umma(GemmArgs g, int *status) {
   if (!ok && tid == 0) set_err(status, DEV_TIMEOUT);
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (ok) {
-    // epilogue: warp w reads lanes 32w.. (tile rows), 16 columns at a time
-    const int row = m0 + warp * 32 + lane;
+    // epilogue: warp w reads lanes 32w.. (its 32 tile rows), 16 columns at a
+    // time, into its own slice of shared memory (the stages are free now;
+    // rows TN + 1 floats apart, so both the column writes here and the row
+    // reads below avoid bank conflicts), then writes the rows out with the
+    // lanes along the columns (coalesced), adding the bias and the ReLU
+    float *ot = reinterpret_cast<float *>(smem) + (size_t)warp * 32 * (TN + 1);
     for (int c0 = 0; c0 < TN; c0 += 16) {
       uint32_t v[16];
       const uint32_t addr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
@@ -191,17 +197,21 @@ __global__ void __launch_bounds__(128) k_gemm_umma(GemmArgs g, int *status) {
             "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
           : "r"(addr));
       asm volatile("tcgen05.wait::ld.sync.aligned;");
-      if (row < g.M) {
 #pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const int col = n0 + c0 + j;
-          if (col < g.N) {
-            float x = __uint_as_float(v[j]);
-            if (g.bias) x += g.bias[col];
-            if (g.relu) x = fmaxf(x, 0.f);
-            if (g.C) g.C[(long long)row * g.ldc + col] = x;
-            if (g.Cb) g.Cb[(long long)row * g.ldc + col] = __float2bfloat16_rn(x);
-          }
+      for (int j = 0; j < 16; j++) ot[lane * (TN + 1) + c0 + j] = __uint_as_float(v[j]);
+    }
+    __syncwarp();
+    for (int r = 0; r < 32; r++) {
+      const int row = m0 + warp * 32 + r;
+      if (row >= g.M) break;
+      for (int cb = 0; cb < TN; cb += 32) {
+        const int col = n0 + cb + lane;
+        if (col < g.N) {
+          float x = ot[r * (TN + 1) + cb + lane];
+          if (g.bias) x += g.bias[col];
+          if (g.relu) x = fmaxf(x, 0.f);
+          if (g.C) g.C[(long long)row * g.ldc + col] = x;
+          if (g.Cb) g.Cb[(long long)row * g.ldc + col] = __float2bfloat16_rn(x);
         }
       }
     }
@@ -213,7 +223,11 @@ __global__ void __launch_bounds__(128) k_gemm_umma(GemmArgs g, int *status) {
 
 }  // namespace
 
-size_t gemm_umma_smem() { return 2 * (size_t)(STAGE_A + STAGE_B); }
+// the two operand stages, or the epilogue's row buffers if larger
+size_t gemm_umma_smem() {
+  const size_t stages = 2 * (size_t)(STAGE_A + STAGE_B), out = 4 * 32 * (size_t)(TN + 1) * sizeof(float);
+  return stages > out ? stages : out;
+}
 
 cudaError_t gemm_bf16_umma(const GemmArgs &g, int *status, cudaStream_t s) {
   if (g.M <= 0 || g.N <= 0) return cudaSuccess;
