@@ -468,10 +468,11 @@ def run_ours(args):
                 "alg_bytes_per_launch": int(alg), "dist_count": ldc, "hop_count": lhc,
                 "kernel": "k_search (learned seeds, per-query L, bf16 candidate rows)",
                 "kernel_ms": round(learned["search_kernel_ms"], 4),
-                "timing": "CUDA events captured around the search kernel in each timed replay"}
+                "timing": "CUDA events captured around the search (dispatch-order and search kernels) in each timed replay"}
         # queries, the replay's query count, the rand() values of the plain seeds (if any)
         h2d = nq * d * 4 + 4 + (nq * 4 if learned["plain_seeds_per_query"] else 0)
-        launches = args.steps * 6  # query normalisation, 3 GEMMs, the seed kernel, the search per step
+        # query normalisation, 3 GEMMs, the seed kernel, the widest-first dispatch order, the search per step
+        launches = args.steps * 7
     else:
         head_qps, head_ms, head_e2e = value, ms, e2e_qps
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",

@@ -140,6 +140,31 @@ def test_search_batch_mixed_L_K(ctx, kgraph20k):
     assert (dc, hc) == (tdc, thc)
 
 
+def test_search_batch_widest_first_many_rounds(ctx, kgraph20k):
+    """Per-query beams dispatch the widest queries first (a counting sort on
+    the device): with more queries than resident warps, every query's ids and
+    the summed counters still equal the oracle's per-query searches."""
+    base, _, g = kgraph20k
+    b2, query = ds.int_mixture(20000, 128, 32, seed=21, n_query=3000)
+    assert np.array_equal(b2, base)
+    ctx.upload_base(base)
+    ctx.upload_graph(g.ids, g.deg, 0)
+    rng = np.random.default_rng(3)
+    nq = query.shape[0]
+    L = rng.integers(10, 200, size=nq).astype(np.uint32)
+    K = np.full(nq, 10, np.uint32)
+    ctx.srand(12)
+    out, dc, hc = ctx.search_batch(query, L, K)
+    r = O.Rand(12)
+    tdc = thc = 0
+    for i in range(nq):
+        e, c1, c2 = O.search(base, query[i:i + 1], g, int(L[i]), r, K=10)
+        assert np.array_equal(out[i], e[0]), i
+        tdc += c1
+        thc += c2
+    assert (dc, hc) == (tdc, thc)
+
+
 def test_search_edge_rows(ctx):
     """Duplicate ids inside a row, empty rows, a self loop and the widest rows."""
     rng = np.random.default_rng(4)

@@ -135,6 +135,11 @@ int wv::run_search_device(wv_ctx *c, const float *d_q, uint32_t nq, const uint32
   SearchArgs a =
       search_args(c, d_q, nq, nullptr, d_seeds, seed_stride, d_L, d_K, L, K, Lmax, d_out, d_dist, out_stride);
   a.seed_shift = shift_seeds ? 1 : 0;
+  if (d_L) {
+    cudaError_t e = cudaSuccess;
+    a.order = c->buf<uint32_t>("search_order", nq, &e);
+    WV_CUDA(c, e);
+  }
   int nb = std::min<long>(blocks, ((long)nq + sh.wpb - 1) / sh.wpb);
   if (nb < 1) nb = 1;
   rc = search_enqueue(c, a, sh, nb);

@@ -722,6 +722,7 @@ int learn_prepare(wv_ctx *c, const char *pfx, uint32_t nq_max, uint32_t *Lcap, u
   *stride = std::max(S.Lmax, S.L_plain);
   c->buf<uint32_t>((p + "seeds").c_str(), (size_t)nq_max * *stride, &e);
   c->buf<uint32_t>((p + "Lq").c_str(), nq_max, &e);
+  c->buf<uint32_t>((p + "order").c_str(), nq_max, &e);
   c->buf<uint32_t>((p + "fb").c_str(), 4, &e);
   WV_CUDA(c, e);
   Work w;
@@ -741,6 +742,7 @@ int learn_enqueue(wv_ctx *c, const char *pfx, const float *dq, uint32_t nq_max, 
   const uint32_t stride = std::max(S.Lmax, S.L_plain);
   uint32_t *seeds = c->buf<uint32_t>((p + "seeds").c_str(), (size_t)nq_max * stride, &e);
   uint32_t *Lq = c->buf<uint32_t>((p + "Lq").c_str(), nq_max, &e);
+  uint32_t *order = c->buf<uint32_t>((p + "order").c_str(), nq_max, &e);
   uint32_t *fb = c->buf<uint32_t>((p + "fb").c_str(), 4, &e);
   WV_CUDA(c, e);
   Work w;
@@ -755,6 +757,7 @@ int learn_enqueue(wv_ctx *c, const char *pfx, const float *dq, uint32_t nq_max, 
   WV_CUDA(c, cudaGetLastError());
   const uint32_t Lcap = S.fallback_p > 0.f ? stride : S.Lmax;
   SearchArgs a = search_args(c, dq, nq_max, d_nq, seeds, stride, Lq, d_K, 0, K, Lcap, dout, ddist, out_stride);
+  a.order = order;
   if (scr.visited) {
     a.visited = scr.visited;
     a.touched = scr.touched;

@@ -101,6 +101,11 @@ SearchArgs plan_args(wv_plan *p, uint32_t nq, const uint32_t *nq_dev, int *rc) {
     a = search_args(c, p->d_q, nq, nq_dev, seeds, p->p.L_max, p->d_L, p->d_K, p->p.L_max, p->p.K_max, p->p.L_max,
                     p->d_out, p->d_dist, p->p.out_stride);
   }
+  if (a.Lq) {
+    cudaError_t e = cudaSuccess;
+    a.order = c->buf<uint32_t>((p->pfx + "order").c_str(), p->p.nq_max, &e);
+    if (e != cudaSuccess) *rc = fail(c, WV_ERR_NOMEM, "plan work buffers");
+  }
   const SearchScratch s = scratch(p);
   a.visited = s.visited;
   a.touched = s.touched;

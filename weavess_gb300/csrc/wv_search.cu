@@ -546,7 +546,10 @@ __global__ void __maxnreg__(128) k_search(SearchArgs a) {
 
   while (true) {
     uint32_t q = 0;
-    if (lane == 0) q = atomicAdd(a.next_query, 1u);
+    if (lane == 0) {
+      q = atomicAdd(a.next_query, 1u);
+      if (q < nq && a.order) q = q < a.nq ? a.order[q] : nq;  // (order holds a.nq entries)
+    }
     q = __shfl_sync(FULL, q, 0);
     if (q >= nq) break;
     const int L = (int)(a.Lq ? a.Lq[q] : a.L);
@@ -906,9 +909,65 @@ int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device) {
   return search_grid(d, Lmax, cap, device, SearchShape{});
 }
 
+// the dispatch order of a launch with per-query beams: a counting sort of
+// the query indices by beam width, widest first (one block; beams above Lmax
+// count as Lmax, the search kernel rejects them).  Within one width the order
+// is that of the shared-memory atomics, which no result depends on.
+constexpr int ORDER_BUCKETS = 4096, ORDER_THREADS = 1024;
+static __global__ void __launch_bounds__(ORDER_THREADS)
+    k_order_by_beam(const uint32_t *Lq, uint32_t nq, const uint32_t *nq_dev, uint32_t Lmax, uint32_t *order) {
+  __shared__ uint32_t cnt[ORDER_BUCKETS];
+  __shared__ uint32_t wsum[ORDER_THREADS / 32];
+  const uint32_t t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const uint32_t n = nq_dev ? min(*nq_dev, nq) : nq;
+  uint32_t shift = 0;
+  while ((Lmax >> shift) >= (uint32_t)ORDER_BUCKETS) shift++;
+  for (uint32_t i = t; i < ORDER_BUCKETS; i += ORDER_THREADS) cnt[i] = 0;
+  __syncthreads();
+  // bucket ORDER_BUCKETS - 1 - width: ascending buckets are descending widths
+  for (uint32_t q = t; q < n; q += ORDER_THREADS) atomicAdd(&cnt[ORDER_BUCKETS - 1 - (min(Lq[q], Lmax) >> shift)], 1u);
+  __syncthreads();
+  constexpr int PER = ORDER_BUCKETS / ORDER_THREADS;
+  uint32_t v[PER], run = 0;
+  for (int i = 0; i < PER; i++) {
+    v[i] = cnt[t * PER + i];
+    run += v[i];
+  }
+  uint32_t incl = run;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(FULL, incl, o);
+    if ((int)lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t x = wsum[lane], xi = x;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(FULL, xi, o);
+      if ((int)lane >= o) xi += y;
+    }
+    wsum[lane] = xi - x;  // exclusive prefix of the warps' totals
+  }
+  __syncthreads();
+  uint32_t off = wsum[w] + incl - run;
+  for (int i = 0; i < PER; i++) {
+    cnt[t * PER + i] = off;
+    off += v[i];
+  }
+  __syncthreads();
+  for (uint32_t q = t; q < n; q += ORDER_THREADS)
+    order[atomicAdd(&cnt[ORDER_BUCKETS - 1 - (min(Lq[q], Lmax) >> shift)], 1u)] = q;
+}
+
 cudaError_t launch_search(const SearchArgs &a, SearchShape sh, int blocks, cudaStream_t stream) {
   if (!shape_ok(sh)) return cudaErrorInvalidValue;
+  if (a.order && a.Lq && !a.vis) {
+    k_order_by_beam<<<1, ORDER_THREADS, 0, stream>>>(a.Lq, a.nq, a.nq_dev, a.Lmax, a.order);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   SearchArgs b = a;
+  if (!b.Lq || b.vis) b.order = nullptr;
   b.hcap = sh.hcap;
   b.wide_hash = sh.wide ? 1 : 0;
   const size_t smem = search_block_smem(a.d, a.Lmax, a.cap, sh);

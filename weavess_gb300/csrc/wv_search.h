@@ -20,6 +20,12 @@ struct SearchArgs {
   const uint32_t *seeds;  // nq x seed_stride
   uint32_t seed_stride;
   const uint32_t *Lq;  // per-query beam width (or null: L)
+  // (nullable, nq words) dispatch order: with per-query beams the launch
+  // first fills it with the query indices by beam width, widest first, and
+  // the warps take queries in that order (the longest searches start first,
+  // so the launch does not end on a few late wide queries); the results of
+  // a query do not depend on the warp that runs it
+  uint32_t *order;
   const uint32_t *Kq;  // per-query result size (or null: K)
   uint32_t L, K, Lmax;
   uint32_t *out_ids;
