@@ -61,6 +61,11 @@ def lib():
                               C.c_uint, C.c_void_p, u32p, f32p, u32p, C.c_uint, u32p, u32p]
         L.orc_search.argtypes = [f32p, C.c_uint, C.c_uint, f32p, C.c_uint, u32p, u32p, C.c_uint, C.c_uint,
                                  C.c_int, C.c_uint, C.c_uint, C.c_void_p, C.c_int, u32p, u64p, u32p, C.c_uint]
+        i32p_ = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+        L.orc_init_kdt.argtypes = [f32p, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_void_p, u32p, f32p,
+                                   u32p, C.c_uint, i32p_, u32p, u32p]
+        L.orc_search_kdt.argtypes = [f32p, C.c_uint, C.c_uint, f32p, C.c_uint, u32p, u32p, C.c_uint, C.c_uint,
+                                     C.c_uint, i32p_, u32p, u32p, C.c_uint, C.c_uint, C.c_void_p, u32p, u64p, u32p]
         L.orc_search_seeds.argtypes = [C.c_uint, C.c_uint, u32p, u32p, C.c_uint, C.c_uint, C.c_int, C.c_uint,
                                        C.c_void_p, u32p, u32p, C.c_uint]
         _lib = L
@@ -168,6 +173,47 @@ def efanna(base, init: Graph, S, K, L, ITER, R, rnd: Rand):
     g = Graph(ids, dist, deg)
     g.overflow_events = int(stats[0])
     return g
+
+
+class KdtForest:
+    """The trees of INIT_KDT: nodes[t, j] = (div_dim, div_val bits, start, end,
+    left, right) for j < cnt[t] (node 0 the root; -1 children: a leaf), and
+    the shuffled id lists leaf[t, :]."""
+
+    def __init__(self, n, T, ncap):
+        self.n, self.T, self.ncap = n, T, ncap
+        self.nodes = np.zeros((T, ncap, 6), np.int32)
+        self.cnt = np.zeros(T, np.uint32)
+        self.leaf = np.zeros((T, n), np.uint32)
+
+
+def init_kdt(base, nTrees, K, mLevel, rnd: Rand):
+    """INIT_KDT: (graph with rows of K ascending, KdtForest)."""
+    base = _c(base, np.float32)
+    n, d = base.shape
+    F = KdtForest(n, nTrees, 2 * n)
+    ids = np.zeros((n, K), np.uint32)
+    dist = np.zeros((n, K), np.float32)
+    deg = np.zeros(n, np.uint32)
+    rc = lib().orc_init_kdt(base, n, d, nTrees, K, mLevel, rnd.h, ids, dist, deg, F.ncap, F.nodes, F.cnt, F.leaf)
+    assert rc == 0, rc
+    return Graph(ids, dist, deg), F
+
+
+def search_kdt(base, query, g: Graph, F: KdtForest, L, rnd: Rand, K=10, return_seeds=False):
+    """SEARCH_ENTRY_KDT + ROUTER_GREEDY (queries in order)."""
+    base, query = _c(base, np.float32), _c(query, np.float32)
+    n, d = base.shape
+    nq = query.shape[0]
+    res = np.zeros((nq, K), np.uint32)
+    cnt = np.zeros(2, np.uint64)
+    seeds = np.zeros((nq, L), np.uint32)
+    rc = lib().orc_search_kdt(base, n, d, query, nq, _c(g.ids, np.uint32), _c(g.deg, np.uint32), g.width, F.T,
+                              F.ncap, F.nodes, F.cnt, F.leaf, L, K, rnd.h, res, cnt, seeds)
+    assert rc == 0, rc
+    if return_seeds:
+        return res, int(cnt[0]), int(cnt[1]), seeds
+    return res, int(cnt[0]), int(cnt[1])
 
 
 def nndescent_pools(base, init: Graph, S, L, iters, R, rnd: Rand):

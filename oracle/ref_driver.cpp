@@ -15,8 +15,8 @@
 // deterministic.
 //
 // usage: ref_driver base.fvecs query.fvecs gt.ivecs outprefix key=val ... -- step ...
-//   steps: init_random | init_rand | nndescent | efanna | vamana | nsg | ssg | load:<kgraph|vamana|nsg|ssg|efanna>
-//          | hnsw | search_rand:<L> | search_centroid:<L> | search_sub:<L> | search_hnsw:<L>
+//   steps: init_random | init_rand | init_kdt | nndescent | efanna | vamana | nsg | ssg | load:<kgraph|vamana|nsg|ssg|efanna>
+//          | hnsw | search_rand:<L> | search_centroid:<L> | search_sub:<L> | search_kdt:<L> | search_hnsw:<L>
 //          | search_nsw:<L> | nsw | search_nswidx:<L> | policy:<rand|centroid>_<set_recall|ascend>
 //          | rand_probe
 //   (search_sub: SEARCH_ENTRY_SUB_CENTROID, the entry the reference's SSG
@@ -102,6 +102,16 @@ int main(int argc, char **argv) {
     if (step == "init_random") {
       builder->init(INIT_RANDOM, false);
       write_final_graph(prefix + ".init.bin", idx, false);
+    } else if (step == "init_kdt") {
+      // INIT_KDT (component_init.cpp:500-640): the graph and the trees' id lists
+      builder->init(INIT_KDT, false);
+      write_final_graph(prefix + ".initkdt.bin", idx, false);
+      FILE *f = fopen((prefix + ".kdtleaf.bin").c_str(), "wb");
+      unsigned T = (unsigned)idx->LeafLists.size(), n = idx->getBaseLen();
+      fwrite(&T, 4, 1, f);
+      fwrite(&n, 4, 1, f);
+      for (unsigned t = 0; t < T; t++) fwrite(idx->LeafLists[t].data(), 4, n, f);
+      fclose(f);
     } else if (step == "init_rand") {
       builder->init(INIT_RAND, false);
       write_final_graph(prefix + ".initrand.bin", idx, false);
@@ -208,13 +218,14 @@ int main(int argc, char **argv) {
       builder->save_graph(t, &gf[0]);
       idx->getLoadGraph().clear();
       builder->load_graph(t, &gf[0]);
-    } else if (step == "search_rand" || step == "search_centroid" || step == "search_sub") {
+    } else if (step == "search_rand" || step == "search_centroid" || step == "search_sub" || step == "search_kdt") {
       unsigned L = (unsigned)std::stoul(arg);
       idx->getParam().set<unsigned>("K_search", 10);
       idx->getParam().set<unsigned>("L_search", L);
       ComponentSearchEntry *e =
           step == "search_rand"       ? (ComponentSearchEntry *)new ComponentSearchEntryRand(idx)
           : step == "search_centroid" ? (ComponentSearchEntry *)new ComponentSearchEntryCentroid(idx)
+          : step == "search_kdt"      ? (ComponentSearchEntry *)new ComponentSearchEntryKDT(idx)
                                       : (ComponentSearchEntry *)new ComponentSearchEntrySubCentroid(idx);
       auto *r = new ComponentSearchRouteGreedy(idx);
       idx->resetDistCount();

@@ -21,6 +21,7 @@
 #include <random>
 #include <stack>
 #include <queue>
+#include <set>
 #include <vector>
 #include <omp.h>
 
@@ -1124,6 +1125,402 @@ void route_nsw(RouteCtx &c, unsigned K, unsigned *res) {
   take_k(result, K, res);
 }
 
+
+// ---------------------------------------------------------------- INIT_KDT
+// ComponentInitKDT (component_init.cpp:500-912): nTrees randomised KD-trees
+// over rand()-shuffled id lists, leaf-to-leaf merges below depth mLevel into
+// per-point bounded candidate sets, then the final graph.  One thread, as the
+// reference's results with IndexBuilder(1): every split's std::mt19937 is
+// seeded 1998 ^ omp_get_thread_num() = 1998.
+struct KdtNode {
+  int div_dim = -1;
+  float div_val = 0.f;
+  unsigned start = 0, end = 0;
+  int left = -1, right = -1;  // -1: leaf
+};
+struct KdtForest {
+  unsigned n = 0, T = 0;
+  std::vector<std::vector<unsigned>> leaf;  // LeafLists
+  std::vector<std::vector<KdtNode>> nodes;  // node 0 = root of the tree
+};
+constexpr unsigned KDT_TNS = 10, KDT_SAMPLE = 100, KDT_RAND_DIM = 5, KDT_ACTIVE_MAX = 1100;
+
+// selectDivision (component_init.cpp:732-756): one of the RAND_DIM largest
+// variances, by the first rng() output % their count
+unsigned kdt_select_division(std::mt19937 &rng, const float *v, unsigned d) {
+  int num = 0;
+  size_t top[KDT_RAND_DIM];
+  for (size_t i = 0; i < d; ++i) {
+    if (num < (int)KDT_RAND_DIM || v[i] > v[top[num - 1]]) {
+      if (num < (int)KDT_RAND_DIM) top[num++] = i;
+      else top[num - 1] = i;
+      int j = num - 1;
+      while (j > 0 && v[top[j]] > v[top[j - 1]]) {
+        std::swap(top[j], top[j - 1]);
+        --j;
+      }
+    }
+  }
+  return (unsigned)top[rng() % (unsigned)num];
+}
+
+// planeSplit (component_init.cpp:698-730): Hoare partitions by < cutval, then
+// by <= cutval from lim1 (the element reads are guarded where the reference
+// reads one past the range without using the value)
+void kdt_plane_split(const Data &D, unsigned *ids, unsigned count, unsigned cutdim, float cutval, unsigned &lim1,
+                     unsigned &lim2) {
+  auto val = [&](int i) { return D.base[(size_t)ids[i] * D.d + cutdim]; };
+  int left = 0, right = (int)count - 1;
+  for (;;) {
+    while (left <= right && val(left) < cutval) ++left;
+    while (left <= right && val(right) >= cutval) --right;
+    if (left > right) break;
+    std::swap(ids[left], ids[right]);
+    ++left;
+    --right;
+  }
+  lim1 = (unsigned)left;
+  right = (int)count - 1;
+  for (;;) {
+    while (left <= right && val(left) <= cutval) ++left;
+    while (left <= right && val(right) > cutval) --right;
+    if (left > right) break;
+    std::swap(ids[left], ids[right]);
+    ++left;
+    --right;
+  }
+  lim2 = (unsigned)left;
+}
+
+// meanSplit (component_init.cpp:648-696): mean and variance of the first
+// SAMPLE_NUM + 1 ids, the cut at the mean of a high-variance dimension
+void kdt_mean_split(const Data &D, std::mt19937 &rng, unsigned *ids, unsigned count, unsigned &index1,
+                    unsigned &cutdim, float &cutval) {
+  std::vector<float> mean(D.d, 0.f), var(D.d, 0.f);
+  const unsigned cnt = std::min(KDT_SAMPLE + 1, count);
+  for (unsigned j = 0; j < cnt; ++j) {
+    const float *v = D.base + (size_t)ids[j] * D.d;
+    for (unsigned k = 0; k < D.d; ++k) mean[k] += v[k];
+  }
+  const float div_factor = float(1) / cnt;
+  for (unsigned k = 0; k < D.d; ++k) mean[k] *= div_factor;
+  for (unsigned j = 0; j < cnt; ++j) {
+    const float *v = D.base + (size_t)ids[j] * D.d;
+    for (unsigned k = 0; k < D.d; ++k) {
+      const float dd = v[k] - mean[k];
+      var[k] += dd * dd;
+    }
+  }
+  cutdim = kdt_select_division(rng, var.data(), D.d);
+  cutval = mean[cutdim];
+  unsigned lim1, lim2;
+  kdt_plane_split(D, ids, count, cutdim, cutval, lim1, lim2);
+  if (lim1 > count / 2) index1 = lim1;
+  else if (lim2 < count / 2) index1 = lim2;
+  else index1 = count / 2;
+  if (lim1 == count || lim2 == 0) index1 = count / 2;
+}
+
+int kdt_new_node(std::vector<KdtNode> &nodes, unsigned start, unsigned end) {
+  KdtNode x;
+  x.start = start;
+  x.end = end;
+  nodes.push_back(x);
+  return (int)nodes.size() - 1;
+}
+
+// DFSbuild (component_init.cpp:758-787); nodes of TNS ids or fewer are leaves
+void kdt_dfs_build(const Data &D, std::vector<KdtNode> &nodes, std::vector<unsigned> &leaf, int nd,
+                   std::mt19937 &rng) {
+  const unsigned start = nodes[nd].start, count = nodes[nd].end - nodes[nd].start;
+  if (count <= KDT_TNS) return;
+  unsigned idx, cutdim;
+  float cutval;
+  kdt_mean_split(D, rng, leaf.data() + start, count, idx, cutdim, cutval);
+  nodes[nd].div_dim = (int)cutdim;
+  nodes[nd].div_val = cutval;
+  const int l = kdt_new_node(nodes, start, start + idx);
+  const int r = kdt_new_node(nodes, start + idx, start + count);
+  nodes[nd].left = l;
+  nodes[nd].right = r;
+  kdt_dfs_build(D, nodes, leaf, l, rng);
+  kdt_dfs_build(D, nodes, leaf, r, rng);
+}
+
+// the trees of InitInner (component_init.cpp:500-580): shuffled id lists
+// (std::random_shuffle on rand(), tree by tree), level-by-level splits while
+// fewer than 1,100 nodes are active (children of more than K ids stay
+// active; each split with a fresh rng), then DFSbuild below each active node
+// (one fresh rng per active node, shared down its subtree)
+KdtForest kdt_build(const Data &D, unsigned T, unsigned K, GlibcRand &rnd) {
+  KdtForest F;
+  F.n = D.n;
+  F.T = T;
+  F.leaf.assign(T, std::vector<unsigned>(D.n));
+  F.nodes.assign(T, std::vector<KdtNode>());
+  std::vector<std::pair<unsigned, int>> active, next;
+  for (unsigned t = 0; t < T; t++) {
+    kdt_new_node(F.nodes[t], 0, D.n);
+    active.emplace_back(t, 0);
+  }
+  for (unsigned t = 0; t < T; t++) {
+    std::vector<unsigned> &ids = F.leaf[t];
+    for (unsigned i = 0; i < D.n; i++) ids[i] = i;
+    for (unsigned i = 1; i < D.n; i++) {
+      const unsigned j = (unsigned)((long)rnd.next() % (long)(i + 1));
+      if (i != j) std::swap(ids[i], ids[j]);
+    }
+  }
+  while (!active.empty() && active.size() < KDT_ACTIVE_MAX) {
+    next.clear();
+    for (auto &a : active) {
+      std::vector<KdtNode> &nodes = F.nodes[a.first];
+      const unsigned start = nodes[a.second].start, count = nodes[a.second].end - start;
+      std::mt19937 rng(1998);
+      unsigned mid, cutdim;
+      float cutval;
+      kdt_mean_split(D, rng, F.leaf[a.first].data() + start, count, mid, cutdim, cutval);
+      nodes[a.second].div_dim = (int)cutdim;
+      nodes[a.second].div_val = cutval;
+      const int l = kdt_new_node(nodes, start, start + mid);
+      const int r = kdt_new_node(nodes, start + mid, start + count);
+      nodes[a.second].left = l;
+      nodes[a.second].right = r;
+      if (mid > K) next.emplace_back(a.first, l);
+      if (count - mid > K) next.emplace_back(a.first, r);
+    }
+    active.swap(next);
+  }
+  for (auto &a : active) {
+    std::mt19937 rng(1998);
+    kdt_dfs_build(D, F.nodes[a.first], F.leaf[a.first], a.second, rng);
+  }
+  return F;
+}
+
+// SearchToLeaf (component_init.cpp:828-838)
+int kdt_search_to_leaf(const Data &D, const std::vector<KdtNode> &nodes, int nd, size_t id) {
+  while (nodes[nd].left >= 0 && nodes[nd].right >= 0)
+    nd = D.base[id * D.d + nodes[nd].div_dim] < nodes[nd].div_val ? nodes[nd].left : nodes[nd].right;
+  return nd;
+}
+
+struct KdtCand {  // Index::Candidate (index.h:234-253)
+  size_t row_id;
+  float distance;
+  bool operator>(const KdtCand &o) const {
+    return distance == o.distance ? row_id > o.row_id : distance > o.distance;
+  }
+};
+typedef std::set<KdtCand, std::greater<KdtCand>> KdtHeap;
+
+void kdt_offer(KdtHeap &h, unsigned K, size_t id, float dist) {
+  if (h.size() < K || dist < h.begin()->distance) {
+    h.insert(KdtCand{id, dist});
+    if (h.size() > K) h.erase(h.begin());
+  }
+}
+
+// mergeSubGraphs (component_init.cpp:840-912)
+void kdt_merge(const Data &D, const KdtForest &F, unsigned t, int nd, unsigned K, std::vector<KdtHeap> &knn) {
+  const std::vector<KdtNode> &nodes = F.nodes[t];
+  const KdtNode &x = nodes[nd];
+  if (x.left < 0 || x.right < 0) return;
+  kdt_merge(D, F, t, x.left, K, knn);
+  kdt_merge(D, F, t, x.right, K, knn);
+  const size_t numL = nodes[x.left].end - nodes[x.left].start, numR = nodes[x.right].end - nodes[x.right].start;
+  int root;
+  size_t start, end;
+  if (numL < numR) {
+    root = x.right;
+    start = nodes[x.left].start;
+    end = nodes[x.left].end;
+  } else {
+    root = x.left;
+    start = nodes[x.right].start;
+    end = nodes[x.right].end;
+  }
+  for (; start < end; start++) {
+    const size_t feature_id = F.leaf[t][start];
+    const int lf = kdt_search_to_leaf(D, nodes, root, feature_id);
+    for (size_t i = nodes[lf].start; i < nodes[lf].end; i++) {
+      const size_t tmpfea = F.leaf[t][i];
+      const float dist = l2(D.base + tmpfea * D.d, D.base + feature_id * D.d, D.d);
+      kdt_offer(knn[tmpfea], K, feature_id, dist);
+      kdt_offer(knn[feature_id], K, tmpfea, dist);
+    }
+  }
+}
+
+// getMergeLevelNodeList (component_init.cpp:814-826)
+void kdt_merge_level(const KdtForest &F, unsigned t, int nd, unsigned depth, unsigned ml,
+                     std::vector<std::pair<int, unsigned>> &out) {
+  const KdtNode &x = F.nodes[t][nd];
+  if (x.left >= 0 && x.right >= 0 && depth < ml) {
+    kdt_merge_level(F, t, x.left, depth + 1, ml, out);
+    kdt_merge_level(F, t, x.right, depth + 1, ml, out);
+  } else if (depth == ml) {
+    out.emplace_back(nd, t);
+  }
+}
+
+// InitInner's merge and final graph (component_init.cpp:582-640): rows in
+// ascending (distance, id); a row of fewer than K gets rng() % n fills into a
+// set ordered by distance alone (equal distances kept once).  Returns false
+// when a row cannot reach K distinct distances (the reference loops forever).
+bool kdt_graph(const Data &D, const KdtForest &F, unsigned K, unsigned ml, FinalGraph &g) {
+  std::vector<std::pair<int, unsigned>> mlist;
+  for (unsigned t = 0; t < F.T; t++) kdt_merge_level(F, t, 0, 0, ml, mlist);
+  std::vector<KdtHeap> knn(D.n);
+  for (auto &m : mlist) kdt_merge(D, F, m.second, m.first, K, knn);
+  g.assign(D.n, {});
+  std::mt19937 rng(1998);
+  for (unsigned i = 0; i < D.n; i++) {
+    std::vector<SimpleNeighbor> tmp;
+    for (auto it = knn[i].rbegin(); it != knn[i].rend(); it++)
+      tmp.push_back(SimpleNeighbor((unsigned)it->row_id,
+                                   l2(D.base + (size_t)i * D.d, D.base + it->row_id * D.d, D.d)));
+    if (tmp.size() < K) {
+      auto by_dist = [](const SimpleNeighbor &a, const SimpleNeighbor &b) { return a.distance < b.distance; };
+      std::set<SimpleNeighbor, decltype(by_dist)> result(by_dist);
+      for (auto &x : tmp) result.insert(x);
+      size_t tries = 0;
+      while (result.size() < K) {
+        if (++tries > 64ull * D.n + 1000000ull) return false;
+        const unsigned id = (unsigned)(rng() % D.n);
+        result.insert(SimpleNeighbor(id, l2(D.base + (size_t)i * D.d, D.base + (size_t)id * D.d, D.d)));
+      }
+      tmp.assign(result.begin(), result.end());
+    }
+    g[i] = tmp;
+  }
+  return true;
+}
+
+// ComponentSearchEntryKDT::getSearchNodeList (component_search_entry.cpp:156-170)
+void kdt_leaf_list(const std::vector<KdtNode> &nodes, int nd, const float *q, unsigned lsize, std::vector<int> &vn) {
+  if (vn.size() >= lsize) return;
+  const KdtNode &x = nodes[nd];
+  if (x.left >= 0 && x.right >= 0) {
+    const bool lt = q[x.div_dim] < x.div_val;
+    kdt_leaf_list(nodes, lt ? x.left : x.right, q, lsize, vn);
+    kdt_leaf_list(nodes, lt ? x.right : x.left, q, lsize, vn);
+  } else {
+    vn.push_back(nd);
+  }
+}
+
+// ComponentSearchEntryKDT::SearchEntryInner's seeds (component_search_entry.cpp:102-141):
+// the ids of lsize = L / (nTrees * TNS) + 1 leaves per tree, taken leaf-major
+// across the trees (the base id equal to the query's index is skipped, as the
+// reference flags it), then rand() % n fills without repeats.  A tree with
+// fewer leaves than lsize contributes the leaves it has (the reference reads
+// past its list there).
+void kdt_seeds(const KdtForest &F, const float *q, unsigned qidx, unsigned L, GlibcRand &rnd, unsigned *s) {
+  const unsigned lsize = L / (F.T * KDT_TNS) + 1;
+  std::vector<std::vector<int>> vnl(F.T);
+  for (unsigned t = 0; t < F.T; t++) kdt_leaf_list(F.nodes[t], 0, q, lsize, vnl[t]);
+  std::vector<char> flags(F.n, 0);
+  if (qidx < F.n) flags[qidx] = 1;
+  unsigned p = 0;
+  for (unsigned ni = 0; ni < lsize && p < L; ni++) {
+    for (unsigned t = 0; t < F.T && p < L; t++) {
+      if (ni >= vnl[t].size()) continue;
+      const KdtNode &lf = F.nodes[t][vnl[t][ni]];
+      for (unsigned j = lf.start; j < lf.end && p < L; j++) {
+        const unsigned nn = F.leaf[t][j];
+        if (flags[nn]) continue;
+        flags[nn] = 1;
+        s[p++] = nn;
+      }
+    }
+  }
+  while (p < L) {
+    const unsigned nn = (unsigned)rnd.next() % F.n;
+    if (flags[nn]) continue;
+    flags[nn] = 1;
+    s[p++] = nn;
+  }
+}
+
+// the pool and route of IndexBuilder::search on given seeds (builder.cpp:445-454,
+// component_route.cpp:9-53)
+void route_seeded(const Data &D, const unsigned *g_ids, const unsigned *g_deg, unsigned g_w, const float *qv,
+                  const unsigned *seeds, unsigned L, unsigned K, unsigned *res, unsigned long long &dc,
+                  unsigned long long &hc) {
+  std::vector<char> flags(D.n, 0);
+  std::vector<Neighbor> pool(L + 1);
+  for (unsigned i = 0; i < L; i++) {
+    pool[i] = Neighbor(seeds[i], l2(qv, D.base + (size_t)seeds[i] * D.d, D.d), true);
+    dc++;
+  }
+  std::sort(pool.begin(), pool.begin() + L);
+  int k = 0;
+  while (k < (int)L) {
+    int nk = (int)L;
+    if (pool[k].flag) {
+      pool[k].flag = false;
+      const unsigned nd = pool[k].id;
+      hc++;
+      for (unsigned m = 0; m < g_deg[nd]; ++m) {
+        const unsigned id = g_ids[(size_t)nd * g_w + m];
+        if (flags[id]) continue;
+        flags[id] = 1;
+        const float dist = l2(qv, D.base + (size_t)id * D.d, D.d);
+        dc++;
+        if (dist >= pool[L - 1].distance) continue;
+        const int rr = insert_into_pool(pool.data(), L, Neighbor(id, dist, true));
+        if (rr < nk) nk = rr;
+      }
+    }
+    if (nk <= k) k = nk;
+    else ++k;
+  }
+  for (unsigned i = 0; i < K; i++) res[i] = pool[i].id;
+}
+
+// flat forest arrays: per tree nodes[t * ncap + j] = (div_dim, div_val bits,
+// start, end, left, right), node counts cnt[t]; leaf lists T x n
+void kdt_export(const KdtForest &F, unsigned ncap, int *nodes, unsigned *cnt, unsigned *leaf) {
+  for (unsigned t = 0; t < F.T; t++) {
+    cnt[t] = (unsigned)F.nodes[t].size();
+    for (size_t j = 0; j < F.nodes[t].size() && j < ncap; j++) {
+      const KdtNode &x = F.nodes[t][j];
+      int *o = nodes + ((size_t)t * ncap + j) * 6;
+      o[0] = x.div_dim;
+      std::memcpy(&o[1], &x.div_val, 4);
+      o[2] = (int)x.start;
+      o[3] = (int)x.end;
+      o[4] = x.left;
+      o[5] = x.right;
+    }
+    std::memcpy(leaf + (size_t)t * F.n, F.leaf[t].data(), (size_t)F.n * 4);
+  }
+}
+KdtForest kdt_import(unsigned n, unsigned T, unsigned ncap, const int *nodes, const unsigned *cnt,
+                     const unsigned *leaf) {
+  KdtForest F;
+  F.n = n;
+  F.T = T;
+  F.leaf.assign(T, std::vector<unsigned>(n));
+  F.nodes.assign(T, std::vector<KdtNode>());
+  for (unsigned t = 0; t < T; t++) {
+    for (unsigned j = 0; j < cnt[t]; j++) {
+      const int *o = nodes + ((size_t)t * ncap + j) * 6;
+      KdtNode x;
+      x.div_dim = o[0];
+      std::memcpy(&x.div_val, &o[1], 4);
+      x.start = (unsigned)o[2];
+      x.end = (unsigned)o[3];
+      x.left = o[4];
+      x.right = o[5];
+      F.nodes[t].push_back(x);
+    }
+    std::memcpy(F.leaf[t].data(), leaf + (size_t)t * n, (size_t)n * 4);
+  }
+  return F;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1396,6 +1793,47 @@ int orc_search_seeds(unsigned n, unsigned nq, const unsigned *g_ids, const unsig
   GlibcRand &r = *(GlibcRand *)rnd;
   for (unsigned q = 0; q < nq; q++)
     draw_entry(n, g_ids, g_deg, g_w, ep, entry, L, eps, n_eps, r, seeds + (size_t)q * L);
+  return 0;
+}
+
+
+// INIT_KDT (component_init.cpp:500-640): the final graph (rows of width K,
+// ascending) and the forest (nodes: T x ncap x 6 words, node counts, leaf
+// lists T x n).  -1: ncap too small; -2: a row cannot reach K distinct
+// distances.
+int orc_init_kdt(const float *base, unsigned n, unsigned d, unsigned T, unsigned K, unsigned mlevel, void *rnd,
+                 unsigned *ids, float *dist, unsigned *deg, unsigned ncap, int *nodes, unsigned *cnt, unsigned *leaf) {
+  Data D{base, n, d};
+  KdtForest F = kdt_build(D, T, K, *(GlibcRand *)rnd);
+  for (unsigned t = 0; t < T; t++)
+    if (F.nodes[t].size() > ncap) return -1;
+  FinalGraph g;
+  if (!kdt_graph(D, F, K, mlevel, g)) return -2;
+  kdt_export(F, ncap, nodes, cnt, leaf);
+  return graph_to_arrays(g, ids, dist, deg, K);
+}
+
+// SEARCH_ENTRY_KDT + ROUTER_GREEDY (component_search_entry.cpp:102-154,
+// component_route.cpp:9-53) over a forest in the orc_init_kdt layout; queries
+// in order (their seed draws share the rand() stream)
+int orc_search_kdt(const float *base, unsigned n, unsigned d, const float *query, unsigned nq, const unsigned *g_ids,
+                   const unsigned *g_deg, unsigned g_w, unsigned T, unsigned ncap, const int *nodes,
+                   const unsigned *cnt, const unsigned *leaf, unsigned L, unsigned K, void *rnd, unsigned *res,
+                   unsigned long long *counters, unsigned *seeds_out) {
+  if (L < K || L >= n) return -1;
+  Data D{base, n, d};
+  KdtForest F = kdt_import(n, T, ncap, nodes, cnt, leaf);
+  GlibcRand &r = *(GlibcRand *)rnd;
+  std::vector<unsigned> s(L);
+  unsigned long long dc = 0, hc = 0;
+  for (unsigned q = 0; q < nq; q++) {
+    const float *qv = query + (size_t)q * d;
+    kdt_seeds(F, qv, q, L, r, s.data());
+    if (seeds_out) std::memcpy(seeds_out + (size_t)q * L, s.data(), (size_t)L * 4);
+    route_seeded(D, g_ids, g_deg, g_w, qv, s.data(), L, K, res + (size_t)q * K, dc, hc);
+  }
+  counters[0] = dc;
+  counters[1] = hc;
   return 0;
 }
 

@@ -42,7 +42,7 @@ CASES = {
     "int_n2000": dict(data=lambda: ds.int_mixture(2000, 128, 8, seed=1, n_query=50),
                       params=dict(S=10, K=20, L=40, ITER=8, R=100, L_refine=40, R_refine=16, C_refine=200,
                                   alpha=1.2, A=60, n_try=5, max_m=8, max_m0=16, ef_construction=40, mult=0,
-                                  n_threads=1, NN=10),
+                                  n_threads=1, NN=10, nTrees=4, mLevel=2),
                       pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:20", "search_rand:50",
                                   "vamana", "load:vamana", "search_centroid:30", "search_rand:17",
                                   "policy:rand_set_recall"],
@@ -53,21 +53,23 @@ CASES = {
                                  ["hnsw", "search_hnsw:20", "search_hnsw:50", "search_nsw:30"],
                                  ["init_rand", "vamana", "vamana", "load:vamana", "search_centroid:30",
                                   "policy:centroid_set_recall"],
-                                 ["nsw", "search_nswidx:20", "search_nswidx:50"]]),
+                                 ["nsw", "search_nswidx:20", "search_nswidx:50"],
+                                 ["init_kdt", "efanna", "load:efanna", "search_kdt:30", "search_kdt:64"]]),
     # S > 16 and L_refine > K: introsort on ties, rand() seed fill in the
     # candidate search, heavy reverse-list overflow (R=12)
     "int_n1500_s20": dict(data=lambda: ds.int_mixture(1500, 128, 4, seed=3, n_query=40),
                           params=dict(S=20, K=24, L=48, ITER=6, R=12, L_refine=64, R_refine=20, C_refine=100,
-                                      alpha=1.2, A=30, n_try=8),
+                                      alpha=1.2, A=30, n_try=8, nTrees=8, mLevel=4),
                           pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:33",
                                       "vamana", "load:vamana", "search_centroid:64", "vamana", "load:vamana",
                                       "search_rand:25"],
-                                     ["init_random", "nndescent", "ssg", "load:ssg", "search_sub:40"]]),
+                                     ["init_random", "nndescent", "ssg", "load:ssg", "search_sub:40"],
+                                     ["init_kdt", "efanna", "load:efanna", "search_kdt:40"]]),
     # massive distance ties (values in {0,1,2}, d=16)
     "ties_n1000": dict(data=lambda: tie_heavy(1000, 16, 3, seed=5, nq=40),
                        params=dict(S=12, K=16, L=30, ITER=5, R=20, L_refine=30, R_refine=12, C_refine=60,
                                    alpha=1.2, A=60, n_try=4, max_m=6, max_m0=12, ef_construction=30, mult=0,
-                                   n_threads=1),
+                                   n_threads=1, nTrees=2, mLevel=3),
                        pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:20", "search_rand:40",
                                    "vamana", "load:vamana", "search_centroid:24"],
                                   ["init_random", "nndescent", "nsg", "load:nsg", "search_centroid:20",
@@ -75,29 +77,33 @@ CASES = {
                                   ["init_random", "nndescent", "ssg", "load:ssg", "search_sub:20"],
                                   ["init_random", "efanna"],
                                   ["hnsw", "search_hnsw:16", "search_nsw:24"],
-                                  ["init_rand", "vamana", "load:vamana", "search_centroid:20"]]),
+                                  ["init_rand", "vamana", "load:vamana", "search_centroid:20"],
+                                  ["init_kdt", "efanna", "load:efanna", "search_kdt:24"]]),
     # real-valued unit vectors (FP32 summation order matters), d=32
     "unit_n1200": dict(data=lambda: ds.unit_mixture(1200, 32, 20, seed=2, n_query=40),
                        params=dict(S=10, K=20, L=40, ITER=6, R=50, L_refine=40, R_refine=16, C_refine=120,
                                    alpha=1.2, A=60, n_try=10, max_m=8, max_m0=16, ef_construction=40, mult=0,
-                                   n_threads=1),
+                                   n_threads=1, nTrees=3, mLevel=1),
                        pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:30",
                                    "vamana", "load:vamana", "search_centroid:30"],
                                   ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:24", "search_sub:24"],
                                   ["init_random", "efanna", "load:efanna", "search_rand:20"],
                                   ["hnsw", "search_hnsw:24", "search_nsw:24"],
-                                  ["init_rand", "vamana", "vamana", "load:vamana", "search_centroid:24"]]),
+                                  ["init_rand", "vamana", "vamana", "load:vamana", "search_centroid:24"],
+                                  ["init_kdt", "efanna", "load:efanna", "search_kdt:24"]]),
     # tiny graph: GenRandom wrap-around, self hits, L = N-1 style edges
     "tiny_n60": dict(data=lambda: ds.int_mixture(60, 8, 3, seed=9, n_query=10),
                      params=dict(S=10, K=8, L=16, ITER=4, R=6, L_refine=12, R_refine=6, C_refine=30, alpha=1.2,
-                                 A=60, n_try=3, max_m=4, max_m0=8, ef_construction=16, mult=0, n_threads=1, NN=5),
+                                 A=60, n_try=3, max_m=4, max_m0=8, ef_construction=16, mult=0, n_threads=1, NN=5,
+                                 nTrees=1, mLevel=3),
                      pipelines=[["init_random", "nndescent", "load:kgraph", "search_rand:10", "search_rand:20",
                                  "vamana", "load:vamana", "search_centroid:12"],
                                 ["init_random", "nndescent", "ssg", "load:ssg", "search_rand:10", "search_sub:10"],
                                 ["init_random", "efanna"],
                                 ["hnsw", "search_hnsw:10", "search_hnsw:30", "search_nsw:12"],
                                 ["init_rand", "vamana", "vamana", "load:vamana", "search_centroid:12"],
-                                ["nsw", "search_nswidx:10", "search_nswidx:30"]]),
+                                ["nsw", "search_nswidx:10", "search_nswidx:30"],
+                                ["init_kdt", "efanna", "load:efanna", "search_kdt:12"]]),
 }
 
 
@@ -146,6 +152,9 @@ def run_case(name, spec):
                     out[f"p{pi}.hnsw.words"] = np.fromfile(os.path.join(tmp, f), np.uint32)
                 elif key.endswith(".nswgraph"):
                     out[f"p{pi}.nsw.words"] = np.fromfile(os.path.join(tmp, f), np.uint32)
+                elif key.endswith(".kdtleaf"):
+                    raw = np.fromfile(os.path.join(tmp, f), np.uint32)
+                    out[key] = raw[2:].reshape(int(raw[0]), int(raw[1]))
                 elif key.endswith(".ssgeps"):
                     out[key[: -len("eps")] + ".eps"] = np.fromfile(os.path.join(tmp, f), np.uint32)[1:]
                 elif "search" in key:

@@ -69,6 +69,9 @@ def replay_oracle(f, pi, on_search=None, on_graph=None):
         elif kind == "init_rand":
             g = O.init_rand(base, p["L"], rnd)
             exp = key + "initrand"
+        elif kind == "init_kdt":
+            g, forest = O.init_kdt(base, p["nTrees"], p["K"], p["mLevel"], rnd)
+            exp = key + "initkdt"
         elif kind == "nndescent":
             g = O.nndescent(base, g, p["S"], p["K"], p["L"], p["ITER"], p["R"], rnd)
             exp = key + "nnd"
@@ -109,6 +112,11 @@ def replay_oracle(f, pi, on_search=None, on_graph=None):
             router, L = ("hnsw" if kind == "search_hnsw" else "nsw"), int(arg)
             got = (on_search(router, L, hwords, rnd) if on_search
                    else O.search_hnsw(base, query, hwords, L, router=router))
+            yield s, f"{key}{kind}_{arg}", got
+            continue
+        elif kind == "search_kdt":
+            L = int(arg)
+            got = on_search("kdt", L, loaded, rnd) if on_search else O.search_kdt(base, query, loaded, forest, L, rnd)
             yield s, f"{key}{kind}_{arg}", got
             continue
         else:

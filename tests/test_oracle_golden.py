@@ -51,6 +51,10 @@ def test_oracle_replays_reference(name):
             elif kind == "init_rand":
                 g = O.init_rand(base, p["L"], rnd)
                 exp = graph_of(f, key + "initrand")
+            elif kind == "init_kdt":
+                g, forest = O.init_kdt(base, p["nTrees"], p["K"], p["mLevel"], rnd)
+                assert np.array_equal(forest.leaf, f[key + "kdtleaf"]), (name, s)
+                exp = graph_of(f, key + "initkdt")
             elif kind == "nndescent":
                 g = O.nndescent(base, g, p["S"], p["K"], p["L"], p["ITER"], p["R"], rnd)
                 exp = graph_of(f, key + "nnd")
@@ -93,6 +97,12 @@ def test_oracle_replays_reference(name):
                 fn = lambda L: O.search(base, query, loaded, L, rnd, entry=entry)  # noqa: E731
                 steps = P.set_recall(fn, f["gt"])[0] if pol == "set_recall" else P.ascend(fn, f["gt"])
                 check_policy(steps, f, f"{key}policy_{arg}", (name, s))
+                continue
+            elif kind == "search_kdt":
+                res, dc, hc = O.search_kdt(base, query, loaded, forest, int(arg), rnd)
+                k = f"{key}{kind}_{arg}"
+                assert np.array_equal(res, f[k + ".res"]), (name, s)
+                assert [dc, hc] == f[k + ".counts"].tolist(), (name, s)
                 continue
             elif kind.startswith("search"):
                 entry = {"search_rand": "rand", "search_centroid": "centroid", "search_sub": "sub_centroid"}[kind]
