@@ -42,7 +42,14 @@ typedef enum {
    * search graph's SSG roots, seed distances taken -- as the reference
    * takes them -- to each row shifted by one float (a zero follows the last
    * row) */
-  WV_ENTRY_SUB_CENTROID = 3
+  WV_ENTRY_SUB_CENTROID = 3,
+  /* ComponentSearchEntryKDT (component_search_entry.cpp:102-170), the EFANNA
+   * search entry: the ids of L / (nTrees * 10) + 1 leaves per tree of the
+   * last wv_init_kdt, found depth first on the query's side of each cut,
+   * then rand() % n fills; the base id equal to the query's number in the
+   * batch is skipped, as the reference flags it.  wv_search only (the seeds
+   * are drawn on the host, in query order, from the host queries). */
+  WV_ENTRY_KDT = 4
 } wv_entry;
 
 typedef struct wv_ctx wv_ctx;
@@ -117,6 +124,16 @@ int wv_init_random(wv_ctx *ctx, uint32_t S, wv_build_stats *stats);
  * skipped), each pool make_heap'd then sorted by distance as the reference
  * does.  Result: the current graph (width L, 1 <= L <= 1024). */
 int wv_init_rand(wv_ctx *ctx, uint32_t L, wv_build_stats *stats);
+
+/* INIT_KDT: replaces ComponentInitKDT::InitInner (component_init.cpp:500-640).
+ * nTrees randomised KD-trees (ids shuffled with rand(), cuts at the mean of
+ * one of the 5 highest-variance dimensions of 101 sampled ids, leaves of at
+ * most 10 ids), leaves merged below depth mLevel into per-point sets of K
+ * nearest candidates; the current graph becomes those rows (K each,
+ * ascending; rows short of K filled from mt19937(1998) % n).  The trees are
+ * kept for WV_ENTRY_KDT.  Identical to the reference run on one thread.
+ * K <= 1024. */
+int wv_init_kdt(wv_ctx *ctx, uint32_t nTrees, uint32_t K, uint32_t mLevel, wv_build_stats *stats);
 
 /* ComponentRefineNNDescent::RefineInner (component_refine.cpp:12-239) on the
  * current graph: ITER rounds of join + update with pool size L, sample S,

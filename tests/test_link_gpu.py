@@ -93,6 +93,8 @@ def test_full_pipelines_match_reference_golden(ctx, name):
     for pi, steps in enumerate(f["pipelines"]):
         if steps[0] in ("hnsw", "nsw"):
             continue  # HNSW / NSW routing over the reference's graphs: tests/test_hnsw_gpu.py
+        if steps[0] == "init_kdt":
+            continue  # INIT_KDT -> EFANNA -> KD-tree entry: tests/test_kdt_gpu.py
         assert _replay(ctx, f, pi)
 
 

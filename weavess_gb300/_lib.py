@@ -119,6 +119,7 @@ def load(build_if_needed: bool = True):
     L.wv_load_built_graph.argtypes = [vp]
     L.wv_init_random.argtypes = [vp, C.c_uint32, C.POINTER(BuildStats)]
     L.wv_init_rand.argtypes = [vp, C.c_uint32, C.POINTER(BuildStats)]
+    L.wv_init_kdt.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(BuildStats)]
     L.wv_nnd_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                 C.POINTER(BuildStats)]
     L.wv_vamana_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, C.POINTER(BuildStats)]

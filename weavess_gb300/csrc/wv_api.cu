@@ -182,6 +182,8 @@ int draw(wv_ctx *c, uint32_t nq, int entry, uint32_t L, uint32_t *seeds, uint32_
   } else if (entry == WV_ENTRY_CENTROID) {
     WV_CHECK(c, c->gn == c->n, WV_ERR_STATE, "centroid entry needs the search graph");
     draw_seeds_centroid(c->rnd, nq, L, c->n, c->ep_row.data(), (uint32_t)c->ep_row.size(), seeds, stride);
+  } else if (entry == WV_ENTRY_KDT) {
+    return fail(c, WV_ERR_ARG, "the KD-tree entry takes the host queries of wv_search");
   } else if (entry == WV_ENTRY_SUB_CENTROID) {
     int rc = check_roots(c, L);
     if (rc) return rc;
@@ -278,6 +280,7 @@ int wv_upload_base(wv_ctx *c, const float *base, uint32_t n, uint32_t d) {
   c->generation++;
   if (c->n != n) c->gn = 0;  // the old graph no longer matches
   c->storage = 0;            // a low-precision copy no longer matches
+  c->kdt = wv::KdtForest{};  // nor do KD-trees of the old base
   c->n = n;
   c->d = d;
   int *ok = c->d_status() + 4;
@@ -383,6 +386,11 @@ int wv_search(wv_ctx *c, const float *queries, uint32_t nq, int entry, uint32_t 
       rc = put_roots_device(c, nq, nullptr, c->seed_buf.as<uint32_t>(), L);
       if (rc) return rc;
     }
+  } else if (entry == WV_ENTRY_KDT) {
+    hs.resize((size_t)nq * L);
+    rc = draw_seeds_kdt(c, queries, nq, L, hs.data(), L);
+    if (rc) return rc;
+    seeds = hs.data();
   } else {
     hs.resize((size_t)nq * L);
     rc = draw(c, nq, entry, L, hs.data(), L);

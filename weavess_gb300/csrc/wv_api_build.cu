@@ -112,6 +112,20 @@ int wv_init_rand(wv_ctx *c, uint32_t L, wv_build_stats *stats) {
   return rc;
 }
 
+int wv_init_kdt(wv_ctx *c, uint32_t nTrees, uint32_t K, uint32_t mLevel, wv_build_stats *stats) {
+  if (!c) return WV_ERR_ARG;
+  WV_CUDA(c, cudaSetDevice(c->device));
+  auto t0 = std::chrono::steady_clock::now();
+  const unsigned long long d0 = c->rnd.drawn;
+  int rc = init_kdt_gpu(c, nTrees, K, mLevel);
+  if (stats) {
+    *stats = wv_build_stats{};
+    stats->rand_draws = c->rnd.drawn - d0;
+    stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return rc;
+}
+
 int wv_nnd_refine(wv_ctx *c, uint32_t S, uint32_t K, uint32_t L, uint32_t ITER, uint32_t R, wv_build_stats *stats) {
   if (!c) return WV_ERR_ARG;
   WV_CUDA(c, cudaSetDevice(c->device));

@@ -12,6 +12,7 @@
 
 #include "../../include/weavess_gpu.h"
 #include "wv_host.h"
+#include "wv_kdt.h"
 
 namespace wv {
 
@@ -85,6 +86,10 @@ struct wv_ctx {
   struct {
     uint32_t n = 0, w0 = 0, wu = 0, ep = 0, max_level = 0, ep_layers = 0;
   } hnsw;
+
+  // KD-trees of the last INIT_KDT on this base (wv_kdt.cu), for the KD-tree
+  // search entry; T = 0 while none is built
+  wv::KdtForest kdt;
 
   // learned entry / beam model (wv_learn.cu), or null
   void *learn = nullptr;

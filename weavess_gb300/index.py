@@ -11,7 +11,7 @@ import numpy as np
 
 from . import _lib
 
-ENTRY = {"rand": 0, "centroid": 1, "seeds": 2, "sub_centroid": 3}
+ENTRY = {"rand": 0, "centroid": 1, "seeds": 2, "sub_centroid": 3, "kdt": 4}
 RAND_FN = C.CFUNCTYPE(C.c_int)
 
 
@@ -160,6 +160,14 @@ class Context:
         """INIT_RAND (the Vamana pipeline's init): L random neighbours per node."""
         st = _lib.BuildStats()
         self._check(self.L.wv_init_rand(self.h, L, C.byref(st)))
+        return st.as_dict()
+
+    def init_kdt(self, nTrees: int, K: int, mLevel: int):
+        """INIT_KDT (the EFANNA pipeline's init): nTrees randomised KD-trees,
+        leaves merged below depth mLevel into rows of K; the trees are kept
+        for the "kdt" search entry."""
+        st = _lib.BuildStats()
+        self._check(self.L.wv_init_kdt(self.h, nTrees, K, mLevel, C.byref(st)))
         return st.as_dict()
 
     def nnd_refine(self, S: int, K: int, L: int, ITER: int, R: int):
