@@ -939,6 +939,31 @@ def run_graphs1m(args):
                      f"ITER={cfg['ITER']} R={cfg['R']} from INIT_RANDOM", "graph_recall@10_1000_nodes": round(grec, 4),
                      "pairs": est["pairs"], "rand_draws": est["rand_draws"], "nndescent_s_same_params": round(knn_s, 2)}
     log(f"efanna {out['efanna']}")
+    # ---- the reference's EFANNA pipeline: INIT_KDT -> REFINE_EFANNA ->
+    # SEARCH_ENTRY_KDT (parameters of its sift1M row, exp_data.h:320)
+    kp = dict(nTrees=8, mLevel=8, K=60, L=70, ITER=10, S=15, R=150)
+    ctx.srand(1)
+    t = time.time()
+    kst = ctx.init_kdt(kp["nTrees"], kp["K"], kp["mLevel"])
+    torch.cuda.synchronize()
+    kdt_s = time.time() - t
+    kids2, _, _, _ = ctx.get_graph()
+    krec = float(np.mean([len(set(kids2[v, :10].tolist()) & set(ex[i].tolist())) / 10 for i, v in enumerate(sample)]))
+    t = time.time()
+    ctx.efanna_refine(kp["S"], kp["K"], kp["L"], kp["ITER"], kp["R"])
+    torch.cuda.synchronize()
+    ef2_s = time.time() - t
+    eids2, _, _, _ = ctx.get_graph()
+    erec = float(np.mean([len(set(eids2[v, :10].tolist()) & set(ex[i].tolist())) / 10 for i, v in enumerate(sample)]))
+    ctx.load_built_graph()
+    Lk, rk = sweep(lambda L: ctx.search(query, L, K, entry="kdt"))
+    qps_k, _ = timed_search(lambda: ctx.search(query, Lk, K, entry="kdt"))
+    out["efanna_kdt"] = {"init_kdt_s": round(kdt_s, 2), "efanna_refine_s": round(ef2_s, 2),
+                         "params": " ".join(f"{k}={v}" for k, v in kp.items()),
+                         "kdt_graph_recall@10_1000_nodes": round(krec, 4),
+                         "efanna_graph_recall@10_1000_nodes": round(erec, 4), "L_search": Lk,
+                         "recall@10": round(rk, 4), "qps_e2e": round(qps_k, 1), "rand_draws": kst["rand_draws"]}
+    log(f"efanna_kdt {out['efanna_kdt']}")
     line = {"metric": "HNSW routing QPS at recall@10>=0.90, with the SSG and EFANNA rows (1M x 128)",
             "value": out["hnsw"]["qps_e2e"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

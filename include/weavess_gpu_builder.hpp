@@ -16,9 +16,9 @@
 //    ->refine(weavess_gpu::REFINE_NN_DESCENT, false)->refine(weavess_gpu::REFINE_NSG, false)
 //    ->save_graph(weavess_gpu::INDEX_NSG, file);
 //
-// Supported: INIT_RANDOM, INIT_RAND; REFINE_NN_DESCENT, REFINE_NSG,
+// Supported: INIT_RANDOM, INIT_RAND, INIT_KDT; REFINE_NN_DESCENT, REFINE_NSG,
 // REFINE_VAMANA, REFINE_SSG, REFINE_EFANNA; search entries RAND, CENTROID,
-// SUB_CENTROID (ROUTER_GREEDY) and NONE (ROUTER_HNSW, ROUTER_NSW); the three
+// SUB_CENTROID, KDT (ROUTER_GREEDY) and NONE (ROUTER_HNSW, ROUTER_NSW); the three
 // L policies; graph files KGRAPH / EFANNA (no header), NSG / VAMANA (entry
 // point), SSG (roots), HNSW and NSW (load only).  The rand() values the components
 // draw come from the process's own rand(), as in the reference.
@@ -184,6 +184,11 @@ class IndexBuilder {
     } else if (type == INIT_RAND) {
       std::cout << "__INIT : RAND__" << std::endl;
       check(wv_init_rand(ctx_, params_.get<unsigned>("L"), nullptr), "INIT_RAND");
+    } else if (type == INIT_KDT) {
+      std::cout << "__INIT : KDT__" << std::endl;
+      check(wv_init_kdt(ctx_, params_.get<unsigned>("nTrees"), params_.get<unsigned>("K"),
+                        params_.get<unsigned>("mLevel"), nullptr),
+            "INIT_KDT");
     } else {
       detail::die("__INIT : WRONG TYPE__");
     }
@@ -272,6 +277,7 @@ class IndexBuilder {
       if (entry_type == SEARCH_ENTRY_RAND) entry = WV_ENTRY_RAND;
       else if (entry_type == SEARCH_ENTRY_CENTROID) entry = WV_ENTRY_CENTROID;
       else if (entry_type == SEARCH_ENTRY_SUB_CENTROID) entry = WV_ENTRY_SUB_CENTROID;
+      else if (entry_type == SEARCH_ENTRY_KDT) entry = WV_ENTRY_KDT;
       else detail::die("__SEARCH ENTRY : WRONG TYPE__");
     } else if (route_type == ROUTER_HNSW || route_type == ROUTER_NSW) {
       if (entry_type != SEARCH_ENTRY_NONE) detail::die("__SEARCH ENTRY : WRONG TYPE__");

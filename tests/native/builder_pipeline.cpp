@@ -2,9 +2,9 @@
 // builder, against weavess_gpu::IndexBuilder (include/weavess_gpu_builder.hpp).
 //
 // usage: builder_pipeline base.fvecs query.fvecs gt.ivecs outprefix key=value ... -- step ...
-//   steps: init_random | init_rand | nndescent | nsg | vamana | ssg | efanna
+//   steps: init_random | init_rand | init_kdt | nndescent | nsg | vamana | ssg | efanna
 //          | save:<kgraph|nsg|vamana|ssg> | load:<kgraph|nsg|vamana|ssg|hnsw>
-//          | search:<rand|centroid|sub|hnsw|nsw>:<L>   (L_SEARCH_ASSIGN; ids to outprefix.sN.bin)
+//          | search:<rand|centroid|sub|kdt|hnsw|nsw>:<L>   (L_SEARCH_ASSIGN; ids to outprefix.sN.bin)
 //          | policy:<rand|centroid>:<set_recall|ascend> | info:<nsg|...>
 // The parameter alpha (if given) sets the builder's Vamana alpha before the
 // first step, as a harness sets the reference's index member.
@@ -20,6 +20,7 @@ static TYPE index_type(const std::string &s) {
   if (s == "nsg") return INDEX_NSG;
   if (s == "vamana") return INDEX_VAMANA;
   if (s == "ssg") return INDEX_SSG;
+  if (s == "efanna") return INDEX_EFANNA;
   if (s == "hnsw") return INDEX_HNSW;
   return INDEX_KGRAPH;
 }
@@ -60,6 +61,7 @@ int main(int argc, char **argv) {
     std::string file = prefix + "." + arg + ".graph";
     if (step == "init_random") builder.init(INIT_RANDOM);
     else if (step == "init_rand") builder.init(INIT_RAND);
+    else if (step == "init_kdt") builder.init(INIT_KDT);
     else if (step == "nndescent") builder.refine(REFINE_NN_DESCENT, false);
     else if (step == "nsg") builder.refine(REFINE_NSG, false);
     else if (step == "vamana") builder.refine(REFINE_VAMANA, false);
@@ -72,6 +74,7 @@ int main(int argc, char **argv) {
       TYPE entry = SEARCH_ENTRY_RAND, route = ROUTER_GREEDY;
       if (arg == "centroid") entry = SEARCH_ENTRY_CENTROID;
       else if (arg == "sub") entry = SEARCH_ENTRY_SUB_CENTROID;
+      else if (arg == "kdt") entry = SEARCH_ENTRY_KDT;
       else if (arg == "hnsw" || arg == "nsw") {
         entry = SEARCH_ENTRY_NONE;
         route = arg == "hnsw" ? ROUTER_HNSW : ROUTER_NSW;

@@ -102,3 +102,18 @@ def test_ssg_pipeline_and_index_info(program, tmp_path):
     m = re.search(r"Max out degree = (\d+), Min out degree= (\d+), Avg out degree = ([0-9.]+)", out)
     assert m and int(m.group(1)) == deg.max() and int(m.group(2)) == deg.min()
     assert "Conn Statistics: conn = 1" in out
+
+
+def test_efanna_pipeline_kdt(program, tmp_path):
+    """INIT_KDT -> REFINE_EFANNA -> save / load -> SEARCH_ENTRY_KDT, as the
+    reference's EFANNA test (test/main.cpp:190-210) drives it."""
+    f = load("int_n2000")
+    pi = [i for i, s in enumerate(f["pipelines"]) if s[0] == "init_kdt"][0]
+    key = f"p{pi}."
+    prefix, counts, _ = run(program, f, tmp_path, ["init_kdt", "efanna", "save:efanna", "load:efanna",
+                                                   "search:kdt:30", "search:kdt:64"])
+    assert open(prefix + ".efanna.graph", "rb").read() == graph_bytes(f[key + "efanna.ids"], f[key + "efanna.deg"])
+    for i, L in enumerate((30, 64)):
+        res = np.fromfile(prefix + f".s{i}.bin", np.uint32).reshape(-1, 10)
+        assert np.array_equal(res, f[f"{key}search_kdt_{L}.res"])
+        assert counts[i] == tuple(f[f"{key}search_kdt_{L}.counts"].tolist())

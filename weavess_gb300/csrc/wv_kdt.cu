@@ -726,58 +726,77 @@ int draw_seeds_kdt(wv_ctx *c, const float *queries, uint32_t nq, uint32_t L, uin
   const KdtForest &F = c->kdt;
   WV_CHECK(c, F.T > 0 && F.n == c->n, WV_ERR_STATE, "the KD-tree entry needs the trees of wv_init_kdt on this base");
   const uint32_t n = F.n, d = c->d, lsize = L / (F.T * KDT_TNS) + 1;
+  std::vector<uint32_t> taken(nq);
+  // the leaf ids of every query (independent across queries: host threads)
+#pragma omp parallel
+  {
+    std::vector<char> flags(n, 0);
+    std::vector<uint32_t> touched;
+    std::vector<std::vector<int>> vnl(F.T);
+    std::vector<int> stack;
+#pragma omp for schedule(dynamic, 64)
+    for (long long qq = 0; qq < (long long)nq; qq++) {
+      const uint32_t q = (uint32_t)qq;
+      const float *qv = queries + (size_t)q * d;
+      // getSearchNodeList (component_search_entry.cpp:156-170), depth first,
+      // the query's side of each cut first
+      for (uint32_t t = 0; t < F.T; t++) {
+        std::vector<int> &vn = vnl[t];
+        vn.clear();
+        stack.assign(1, (int)t);
+        while (!stack.empty() && vn.size() < lsize) {
+          const int nd = stack.back();
+          const KNode &x = F.nodes[nd];
+          stack.pop_back();
+          if (x.left >= 0 && x.right >= 0) {
+            const bool lt = qv[x.dim] < x.val;
+            stack.push_back(lt ? x.right : x.left);
+            stack.push_back(lt ? x.left : x.right);
+          } else {
+            vn.push_back(nd);
+          }
+        }
+      }
+      uint32_t *s = seeds + (size_t)q * stride;
+      uint32_t p = 0;
+      touched.clear();
+      if (q < n) {  // the reference flags the base id equal to the query's number
+        flags[q] = 1;
+        touched.push_back(q);
+      }
+      for (uint32_t ni = 0; ni < lsize && p < L; ni++) {
+        for (uint32_t t = 0; t < F.T && p < L; t++) {
+          if (ni >= vnl[t].size()) continue;
+          const KNode &lf = F.nodes[vnl[t][ni]];
+          for (uint32_t j = lf.start; j < lf.end && p < L; j++) {
+            const uint32_t id = F.leaf[(size_t)t * n + j];
+            if (flags[id]) continue;
+            flags[id] = 1;
+            touched.push_back(id);
+            s[p++] = id;
+          }
+        }
+      }
+      taken[q] = p;
+      for (uint32_t id : touched) flags[id] = 0;
+    }
+  }
+  // rand() % n fills, in query order (they share the rand() stream)
   std::vector<char> flags(n, 0);
-  std::vector<uint32_t> touched;
-  std::vector<std::vector<int>> vnl(F.T);
-  std::vector<int> stack;
   for (uint32_t q = 0; q < nq; q++) {
-    const float *qv = queries + (size_t)q * d;
-    // getSearchNodeList (component_search_entry.cpp:156-170), depth first,
-    // the query's side of each cut first
-    for (uint32_t t = 0; t < F.T; t++) {
-      std::vector<int> &vn = vnl[t];
-      vn.clear();
-      stack.assign(1, (int)t);
-      while (!stack.empty() && vn.size() < lsize) {
-        const KNode &x = F.nodes[stack.back()];
-        const int nd = stack.back();
-        stack.pop_back();
-        if (x.left >= 0 && x.right >= 0) {
-          const bool lt = qv[x.dim] < x.val;
-          stack.push_back(lt ? x.right : x.left);
-          stack.push_back(lt ? x.left : x.right);
-        } else {
-          vn.push_back(nd);
-        }
-      }
-    }
     uint32_t *s = seeds + (size_t)q * stride;
-    uint32_t p = 0;
-    touched.clear();
-    auto take = [&](uint32_t id) {
-      flags[id] = 1;
-      touched.push_back(id);
-    };
-    if (q < n) take(q);  // the reference flags the base id equal to the query's number
-    for (uint32_t ni = 0; ni < lsize && p < L; ni++) {
-      for (uint32_t t = 0; t < F.T && p < L; t++) {
-        if (ni >= vnl[t].size()) continue;
-        const KNode &lf = F.nodes[vnl[t][ni]];
-        for (uint32_t j = lf.start; j < lf.end && p < L; j++) {
-          const uint32_t id = F.leaf[(size_t)t * n + j];
-          if (flags[id]) continue;
-          take(id);
-          s[p++] = id;
-        }
-      }
-    }
+    uint32_t p = taken[q];
+    if (p >= L) continue;
+    for (uint32_t i = 0; i < p; i++) flags[s[i]] = 1;
+    if (q < n) flags[q] = 1;
     while (p < L) {
       const uint32_t id = (uint32_t)c->rnd.next() % n;
       if (flags[id]) continue;
-      take(id);
+      flags[id] = 1;
       s[p++] = id;
     }
-    for (uint32_t id : touched) flags[id] = 0;
+    for (uint32_t i = 0; i < L; i++) flags[s[i]] = 0;
+    if (q < n) flags[q] = 0;
   }
   return WV_OK;
 }
