@@ -53,6 +53,7 @@ def test_kdt_efanna_pipeline_matches_reference_golden(ctx, name):
     ("int", 20000, 128, 8, 30, 4, 64),
     ("int", 12000, 64, 3, 17, 0, 40),
     ("unit", 10000, 96, 4, 20, 2, 48),
+    ("int", 60000, 16, 2, 12, 6, 30),  # id lists beyond shared memory: shuffled in global memory
 ])
 def test_init_kdt_matches_oracle(ctx, kind, n, d, T, K, ml, L):
     if kind == "int":

@@ -58,22 +58,60 @@ constexpr int KW = 4;                     // warps per block
 constexpr uint32_t KDT_MAX_K = 1024;
 
 // ---------------------------------------------------------------- shuffle
+// std::random_shuffle of 0..n-1 (libstdc++: step i swaps positions i and
+// j = rand() % (i + 1)); before step i position i still holds i, so a step is
+// a[i] = a[j]; a[j] = i.  The steps run in blocks of SH_W: the SH_W reads of
+// a block are issued together (they see every store of earlier blocks), and
+// a read of a position an earlier step of the same block wrote takes that
+// step's value from registers instead.
+constexpr int SH_W = 16;
+
+__device__ __forceinline__ void shuffle_steps(uint32_t *a, const int *rt, uint32_t n) {
+  a[0] = 0;
+  uint32_t i0 = 1;
+  for (; i0 + SH_W <= n; i0 += SH_W) {
+    uint32_t j[SH_W], v[SH_W];
+#pragma unroll
+    for (int k = 0; k < SH_W; k++) {
+      j[k] = (uint32_t)((long long)rt[i0 + k - 1] % (long long)(i0 + k + 1));
+      v[k] = a[j[k]];
+    }
+#pragma unroll
+    for (int k = 0; k < SH_W; k++) {
+#pragma unroll
+      for (int m = 0; m < k; m++) {
+        if (j[k] == i0 + m) v[k] = v[m];  // step m wrote a[i_m] = (its read)
+        if (j[k] == j[m]) v[k] = i0 + m;  // ... then a[j_m] = i_m (a[i_m] when j_m == i_m)
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < SH_W; k++) {
+      const uint32_t i = i0 + k;
+      if (j[k] == i) {
+        a[i] = i;
+      } else {
+        a[i] = v[k];
+        a[j[k]] = i;
+      }
+    }
+  }
+  for (uint32_t i = i0; i < n; i++) {
+    const uint32_t jj = (uint32_t)((long long)rt[i - 1] % (long long)(i + 1));
+    if (jj == i) {
+      a[i] = i;
+    } else {
+      a[i] = a[jj];
+      a[jj] = i;
+    }
+  }
+}
+
 __global__ void k_kdt_shuffle(uint32_t n, const int *r, uint32_t *leaf, int in_smem) {
   extern __shared__ uint32_t sh[];
   if (threadIdx.x != 0) return;
   const uint32_t t = blockIdx.x;
   uint32_t *a = in_smem ? sh : leaf + (size_t)t * n;
-  const int *rt = r + (size_t)t * (n - 1);
-  a[0] = 0;
-  for (uint32_t i = 1; i < n; i++) {
-    const uint32_t j = (uint32_t)((long long)rt[i - 1] % (long long)(i + 1));
-    if (j == i) {
-      a[i] = i;
-    } else {
-      a[i] = a[j];
-      a[j] = i;
-    }
-  }
+  shuffle_steps(a, r + (size_t)t * (n - 1), n);
   if (in_smem)
     for (uint32_t i = 0; i < n; i++) leaf[(size_t)t * n + i] = a[i];
 }
