@@ -52,3 +52,29 @@ def test_kgraph_nsg_ssg_and_searches_at_10k(tmp_path):
             res, dc, hc = O.search(base, query, g, L, r, entry=entry)
             wres, wdc, whc = O.read_search_dump(f"{prefix}.search_{entry}_{L}.bin")
             assert np.array_equal(res, wres) and (dc, hc) == (wdc, whc), (tag, entry, L)
+
+
+def test_init_kdt_and_kdt_search_at_10k(tmp_path):
+    base, query = ds.int_mixture(10000, 64, 24, seed=17, n_query=100)
+    gt = ds.groundtruth_fp64(base, query, 20)
+    bf, qf, gf = (str(tmp_path / x) for x in ("b.fvecs", "q.fvecs", "g.ivecs"))
+    ds.write_vecs(bf, base)
+    ds.write_vecs(qf, query)
+    ds.write_vecs(gf, gt)
+    p = dict(nTrees=6, mLevel=5, K=25, S=10, L=40, ITER=4, R=60)
+    prefix = str(tmp_path / "k")
+    subprocess.run([O.REF_DRIVER, bf, qf, gf, prefix] + [f"{k}={v}" for k, v in p.items()] +
+                   ["--", "init_kdt", "efanna", "load:efanna", "search_kdt:48"], check=True, capture_output=True,
+                   timeout=900)
+    r = O.Rand(1)
+    g, forest = O.init_kdt(base, p["nTrees"], p["K"], p["mLevel"], r)
+    lf = np.fromfile(prefix + ".kdtleaf.bin", np.uint32)[2:].reshape(p["nTrees"], -1)
+    assert np.array_equal(lf, forest.leaf)
+    want = O.read_graph_dump(prefix + ".initkdt.bin")
+    assert rows_equal(g.ids, g.dist, g.deg, want.ids, want.dist, want.deg) == 0
+    g = O.efanna(base, g, p["S"], p["K"], p["L"], p["ITER"], p["R"], r)
+    want = O.read_graph_dump(prefix + ".efanna.bin")
+    assert rows_equal(g.ids, g.dist, g.deg, want.ids, want.dist, want.deg) == 0
+    res, dc, hc = O.search_kdt(base, query, g, forest, 48, r)
+    wres, wdc, whc = O.read_search_dump(prefix + ".search_kdt_48.bin")
+    assert np.array_equal(res, wres) and (dc, hc) == (wdc, whc)
