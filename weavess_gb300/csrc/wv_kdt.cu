@@ -690,6 +690,15 @@ int init_kdt_gpu(wv_ctx *c, uint32_t T, uint32_t K, uint32_t mlevel) {
   k_kdt_records<<<nblocks(total, 256, gb), 256, 0, c->stream>>>(c->base.as<float>(), d, n, total, leaf, nodes,
                                                                   leaf_of, (int)mlevel, rcnt, nullptr, nullptr);
   WV_CUDA(c, cudaGetLastError());
+  {
+    // the offsets are 32-bit: refuse forests whose records would not fit
+    std::vector<uint32_t> hc((size_t)count + 1);
+    WV_CUDA(c, cudaMemcpyAsync(hc.data(), rcnt, hc.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    unsigned long long sum = 0;
+    for (uint32_t v : hc) sum += v;
+    WV_CHECK(c, sum < 0xffffffffull, WV_ERR_LIMIT, "INIT_KDT: %llu merge records exceed 32-bit offsets", sum);
+  }
   WV_CUDA(c, exclusive_scan_u32(rcnt, roff, (size_t)count + 1, scan_tmp, c->stream));
   uint32_t nrec = 0;
   WV_CUDA(c, cudaMemcpyAsync(&nrec, roff + count, 4, cudaMemcpyDeviceToHost, c->stream));
