@@ -277,7 +277,9 @@ class IndexBuilder {
       if (entry_type == SEARCH_ENTRY_RAND) entry = WV_ENTRY_RAND;
       else if (entry_type == SEARCH_ENTRY_CENTROID) entry = WV_ENTRY_CENTROID;
       else if (entry_type == SEARCH_ENTRY_SUB_CENTROID) entry = WV_ENTRY_SUB_CENTROID;
-      else if (entry_type == SEARCH_ENTRY_KDT) entry = WV_ENTRY_KDT;
+      // ComponentSearchEntryKDTSingle (component_search_entry.cpp:173-240) is
+      // the same entry, line for line
+      else if (entry_type == SEARCH_ENTRY_KDT || entry_type == SEARCH_ENTRY_KDT_SINGLE) entry = WV_ENTRY_KDT;
       else detail::die("__SEARCH ENTRY : WRONG TYPE__");
     } else if (route_type == ROUTER_HNSW || route_type == ROUTER_NSW) {
       if (entry_type != SEARCH_ENTRY_NONE) detail::die("__SEARCH ENTRY : WRONG TYPE__");
