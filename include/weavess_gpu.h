@@ -47,8 +47,9 @@ typedef enum {
    * search entry: the ids of L / (nTrees * 10) + 1 leaves per tree of the
    * last wv_init_kdt, found depth first on the query's side of each cut,
    * then rand() % n fills; the base id equal to the query's number in the
-   * batch is skipped, as the reference flags it.  wv_search only (the seeds
-   * are drawn on the host, in query order, from the host queries). */
+   * batch is skipped, as the reference flags it.  wv_search only (the
+   * leaves are walked on the device; the rand() fills follow on the host in
+   * query order). */
   WV_ENTRY_KDT = 4
 } wv_entry;
 

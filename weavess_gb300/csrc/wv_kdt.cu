@@ -580,6 +580,67 @@ __global__ void k_kdt_fill(const float *__restrict__ base, uint32_t d, uint32_t 
   more[0] = 0;
 }
 
+// SEARCH_ENTRY_KDT's leaf part (component_search_entry.cpp:115-134), one
+// query per warp: lane 0 walks each tree for its first lsize leaves in
+// getSearchNodeList's order (the query's side of a cut first), then the
+// warp takes their ids leaf-major across the trees without repeats (the base
+// id equal to the query's number excluded); taken[q] = how many
+__global__ void k_kdt_entry(const KNode *nodes, const uint32_t *leaf, uint32_t n, uint32_t T, const float *queries,
+                            uint32_t nq, uint32_t d, uint32_t L, uint32_t lsize, int *vn, uint32_t *seeds,
+                            uint32_t stride, uint32_t *taken, int *status) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nq; q += nw) {
+    const float *qv = queries + (size_t)q * d;
+    int *vq = vn + (size_t)q * T * lsize;
+    if (lane == 0) {
+      int stack[KDT_MAX_DEPTH + 2];
+      for (uint32_t t = 0; t < T; t++) {
+        uint32_t cnt = 0;
+        int sp = 0;
+        stack[sp++] = (int)t;
+        while (sp > 0 && cnt < lsize) {
+          const int nd = stack[--sp];
+          const KNode x = nodes[nd];
+          if (x.left >= 0 && x.right >= 0) {
+            if (sp + 2 > KDT_MAX_DEPTH + 2) {
+              set_err(status, DEV_OVERFLOW);
+              break;
+            }
+            const bool lt = qv[x.dim] < x.val;
+            stack[sp++] = lt ? x.right : x.left;
+            stack[sp++] = lt ? x.left : x.right;
+          } else {
+            vq[t * lsize + cnt++] = nd;
+          }
+        }
+        for (; cnt < lsize; cnt++) vq[t * lsize + cnt] = -1;
+      }
+    }
+    __syncwarp();
+    uint32_t *s = seeds + (size_t)q * stride;
+    uint32_t p = 0;
+    for (uint32_t ni = 0; ni < lsize && p < L; ni++) {
+      for (uint32_t t = 0; t < T && p < L; t++) {
+        const int nd = vq[t * lsize + ni];
+        if (nd < 0) continue;
+        const KNode lf = nodes[nd];
+        for (uint32_t j = lf.start; j < lf.end && p < L; j++) {
+          const uint32_t id = leaf[(size_t)t * n + j];
+          bool hit = false;
+          for (uint32_t u = lane; u < p; u += 32) hit |= s[u] == id;
+          if (id == q || __any_sync(FULL, hit)) continue;
+          if (lane == 0) s[p] = id;
+          p++;
+          __syncwarp();
+        }
+      }
+    }
+    if (lane == 0) taken[q] = p;
+    __syncwarp();
+  }
+}
+
 int nblocks(size_t items, int per_block, int cap) {
   return (int)std::max<size_t>(1, std::min<size_t>((items + per_block - 1) / per_block, (size_t)cap));
 }
@@ -758,81 +819,41 @@ int init_kdt_gpu(wv_ctx *c, uint32_t T, uint32_t K, uint32_t mlevel) {
   c->fg_w = K;
   c->fg_has_ep = false;
   c->fg_eps.clear();
-  // host copy of the forest for SEARCH_ENTRY_KDT
+  // the forest stays in the work buffers for SEARCH_ENTRY_KDT
   c->kdt.n = n;
   c->kdt.T = T;
-  c->kdt.nodes.resize(count);
-  c->kdt.leaf.resize(total);
-  WV_CUDA(c, cudaMemcpyAsync(c->kdt.nodes.data(), nodes, (size_t)count * sizeof(KNode), cudaMemcpyDeviceToHost,
-                             c->stream));
-  WV_CUDA(c, cudaMemcpyAsync(c->kdt.leaf.data(), leaf, total * 4, cudaMemcpyDeviceToHost, c->stream));
   return check_device_status(c, "INIT_KDT");
 }
 
 int draw_seeds_kdt(wv_ctx *c, const float *queries, uint32_t nq, uint32_t L, uint32_t *seeds, uint32_t stride) {
   const KdtForest &F = c->kdt;
   WV_CHECK(c, F.T > 0 && F.n == c->n, WV_ERR_STATE, "the KD-tree entry needs the trees of wv_init_kdt on this base");
+  if (nq == 0) return WV_OK;
   const uint32_t n = F.n, d = c->d, lsize = L / (F.T * KDT_TNS) + 1;
-  std::vector<uint32_t> taken(nq);
-  // the leaf ids of every query (independent across queries: host threads)
-#pragma omp parallel
-  {
-    std::vector<char> flags(n, 0);
-    std::vector<uint32_t> touched;
-    std::vector<std::vector<int>> vnl(F.T);
-    std::vector<int> stack;
-#pragma omp for schedule(dynamic, 64)
-    for (long long qq = 0; qq < (long long)nq; qq++) {
-      const uint32_t q = (uint32_t)qq;
-      const float *qv = queries + (size_t)q * d;
-      // getSearchNodeList (component_search_entry.cpp:156-170), depth first,
-      // the query's side of each cut first
-      for (uint32_t t = 0; t < F.T; t++) {
-        std::vector<int> &vn = vnl[t];
-        vn.clear();
-        stack.assign(1, (int)t);
-        while (!stack.empty() && vn.size() < lsize) {
-          const int nd = stack.back();
-          const KNode &x = F.nodes[nd];
-          stack.pop_back();
-          if (x.left >= 0 && x.right >= 0) {
-            const bool lt = qv[x.dim] < x.val;
-            stack.push_back(lt ? x.right : x.left);
-            stack.push_back(lt ? x.left : x.right);
-          } else {
-            vn.push_back(nd);
-          }
-        }
-      }
-      uint32_t *s = seeds + (size_t)q * stride;
-      uint32_t p = 0;
-      touched.clear();
-      if (q < n) {  // the reference flags the base id equal to the query's number
-        flags[q] = 1;
-        touched.push_back(q);
-      }
-      for (uint32_t ni = 0; ni < lsize && p < L; ni++) {
-        for (uint32_t t = 0; t < F.T && p < L; t++) {
-          if (ni >= vnl[t].size()) continue;
-          const KNode &lf = F.nodes[vnl[t][ni]];
-          for (uint32_t j = lf.start; j < lf.end && p < L; j++) {
-            const uint32_t id = F.leaf[(size_t)t * n + j];
-            if (flags[id]) continue;
-            flags[id] = 1;
-            touched.push_back(id);
-            s[p++] = id;
-          }
-        }
-      }
-      taken[q] = p;
-      for (uint32_t id : touched) flags[id] = 0;
-    }
-  }
+  cudaError_t e = cudaSuccess;
+  const KNode *nodes = c->buf<KNode>("kd_nodes", 1, &e);
+  const uint32_t *leaf = c->buf<uint32_t>("kd_leaf", 1, &e);
+  float *dq = c->buf<float>("kd_q", (size_t)nq * d, &e);
+  int *vn = c->buf<int>("kd_vn", (size_t)nq * F.T * lsize, &e);
+  uint32_t *ds = c->buf<uint32_t>("kd_seeds", (size_t)nq * L, &e);
+  uint32_t *dt = c->buf<uint32_t>("kd_taken", nq, &e);
+  WV_CUDA(c, e);
+  WV_CUDA(c, cudaMemcpyAsync(dq, queries, (size_t)nq * d * 4, cudaMemcpyHostToDevice, c->stream));
+  k_kdt_entry<<<nblocks(nq, 8, c->sms * 16), 256, 0, c->stream>>>(nodes, leaf, n, F.T, dq, nq, d, L, lsize, vn, ds, L,
+                                                                   dt, c->d_status());
+  WV_CUDA(c, cudaGetLastError());
+  std::vector<uint32_t> taken(nq), hs((size_t)nq * L);
+  WV_CUDA(c, cudaMemcpyAsync(hs.data(), ds, hs.size() * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaMemcpyAsync(taken.data(), dt, (size_t)nq * 4, cudaMemcpyDeviceToHost, c->stream));
+  int rc = check_device_status(c, "KD-tree entry");
+  if (rc) return rc;
   // rand() % n fills, in query order (they share the rand() stream)
   std::vector<char> flags(n, 0);
   for (uint32_t q = 0; q < nq; q++) {
+    const uint32_t *g = hs.data() + (size_t)q * L;
     uint32_t *s = seeds + (size_t)q * stride;
     uint32_t p = taken[q];
+    std::copy(g, g + p, s);
     if (p >= L) continue;
     for (uint32_t i = 0; i < p; i++) flags[s[i]] = 1;
     if (q < n) flags[q] = 1;

@@ -17,12 +17,11 @@ struct KNode {
   int depth, tree;
 };
 
-// the forest of the last wv_init_kdt on the current base (host copy, for the
-// search entry): node t is the root of tree t; leaf = T x n id lists
+// the forest of the last wv_init_kdt on the current base (n, T; 0 while
+// none): its nodes and T x n id lists stay in the context's work buffers
+// "kd_nodes" / "kd_leaf" (node t is the root of tree t) for the search entry
 struct KdtForest {
   uint32_t n = 0, T = 0;
-  std::vector<KNode> nodes;
-  std::vector<uint32_t> leaf;
 };
 
 // INIT_KDT on the uploaded base: the current graph becomes the KD-tree graph
