@@ -34,6 +34,9 @@
 //  * final rows in ascending (distance, id); a row of fewer than K is filled
 //    by one thread, row by row, from mt19937(1998) outputs % n into a set
 //    keyed by distance alone (equal distances kept once), as the reference.
+// SEARCH_ENTRY_KDT (component_search_entry.cpp:102-170) walks the kept trees
+// on the device, one warp per query; only its rand() % n fills, which share
+// the rand() stream across queries, are drawn on the host in query order.
 #include <algorithm>
 #include <cstring>
 #include <random>
