@@ -396,9 +396,13 @@ int wv_plan_destroy(wv_plan *plan);
  * It needs no context and allocates nothing: its working memory is a fixed
  * 64 MiB device array inside this library, shared by every call, so calls
  * that overlap on the GPU race on it.  The first call on a device looks that
- * array up (make it before any stream capture).  Returns WV_ERR_LIMIT when n
- * is too large for the fixed array (about 130 million nodes) or L / width
- * exceed the search limits, WV_ERR_DEVICE if the kernel saw an id >= n. */
+ * array's address up and keeps it for later calls; make that first call
+ * before any stream capture, and after a cudaDeviceReset the kept address is
+ * stale (the library must then be reloaded).  The call returns once the
+ * search has finished on `stream` (it reads the kernel's status back).
+ * Returns WV_ERR_LIMIT when n is too large for the fixed array (n / 16
+ * words per warp slot, four slots at least: about 67 million nodes) or L /
+ * width exceed the search limits, WV_ERR_DEVICE if the kernel saw an id >= n. */
 int wv_search_noalloc(const float *d_base, uint32_t n, uint32_t d, const uint32_t *d_graph_ids,
                       const uint32_t *d_graph_deg, uint32_t width, const float *d_queries, uint32_t nq,
                       const uint32_t *d_seeds, uint32_t L, uint32_t K, uint32_t *d_out_ids, float *d_out_dist,

@@ -10,10 +10,20 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("WEAVESS_REF", "/root/reference")
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include", "weavess")) or not shutil.which("g++"),
+def _reference_tree() -> str:
+    """WEAVESS_REF, else the tree the oracle's reference build recorded."""
+    if os.environ.get("WEAVESS_REF"):
+        return os.environ["WEAVESS_REF"]
+    rec = os.path.join(ROOT, "oracle", "_ref", "REF_PATH")
+    return open(rec).read().strip() if os.path.exists(rec) else ""
+
+
+REF = _reference_tree()
+
+
+@pytest.mark.skipif(not REF or not os.path.isdir(os.path.join(REF, "include", "weavess")) or not shutil.which("g++"),
                     reason="reference headers not present")
 def test_component_subclasses_compile_against_reference_headers(tmp_path):
     text = open(os.path.join(ROOT, "INTEGRATION.md")).read()

@@ -93,3 +93,23 @@ def test_init_kdt_short_rows_and_errors(ctx):
     ctx.load_built_graph()
     with pytest.raises(RuntimeError):
         ctx.search_batch(query, np.full(20, 20, np.uint32), np.full(20, 10, np.uint32), entry="kdt")
+
+
+def test_failed_init_kdt_clears_the_forest(ctx):
+    """An INIT_KDT that is refused part way through rewrites the forest's work
+    buffers, so the trees of the earlier init on the same base are gone: the
+    KD-tree entry must refuse instead of walking a partial forest."""
+    rng = np.random.default_rng(9)
+    # five distinct rows repeated: every point sees at most five distinct
+    # distances, so K = 3 fills its rows and K = 8 cannot
+    base = np.repeat(rng.integers(0, 256, (5, 16)).astype(np.float32), 40, axis=0)
+    query = base[::37].copy()
+    ctx.upload_base(base)
+    ctx.srand(1)
+    ctx.init_kdt(2, 3, 30)
+    ctx.load_built_graph()
+    ctx.search(query, 8, 3, entry="kdt")  # the forest of the completed init
+    with pytest.raises(RuntimeError):
+        ctx.init_kdt(2, 8, 30)  # refused by the K fill
+    with pytest.raises(RuntimeError):
+        ctx.search(query, 8, 3, entry="kdt")

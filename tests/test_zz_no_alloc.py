@@ -13,11 +13,17 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_noalloc_search_matches_search_device():
+@pytest.mark.parametrize("kind", ["int", "unit"])
+def test_noalloc_search_matches_search_device(kind):
+    """Integer data (any summation order exact) and real-valued unit
+    vectors (distances folded in the reference's order)."""
     import torch
     from weavess_gb300 import Context, datasets as ds
 
-    base, query = ds.int_mixture(6000, 64, 8, seed=17, n_query=300)
+    if kind == "int":
+        base, query = ds.int_mixture(6000, 64, 8, seed=17, n_query=300)
+    else:
+        base, query = ds.unit_mixture(6000, 96, 12, seed=17, n_query=300)
     ctx = Context(0)
     ctx.upload_base(base)
     ctx.srand(1)
@@ -57,3 +63,11 @@ def test_noalloc_search_matches_search_device():
                                    C.c_void_p(d_ids.data_ptr()), C.c_void_p(d_deg.data_ptr()), ids.shape[1],
                                    C.c_void_p(d_q.data_ptr()), nq, C.c_void_p(d_seeds.data_ptr()), 5000, K,
                                    C.c_void_p(out_ids.data_ptr()), None, C.c_void_p(stream)) != 0
+    # a base too large for the fixed scratch (n / 16 words per warp slot,
+    # four slots at least) is refused before anything is launched: n is
+    # only compared, the buffers are never read
+    n_big = 67_200_000
+    assert ctx.L.wv_search_noalloc(C.c_void_p(d_base.data_ptr()), n_big, base.shape[1],
+                                   C.c_void_p(d_ids.data_ptr()), C.c_void_p(d_deg.data_ptr()), ids.shape[1],
+                                   C.c_void_p(d_q.data_ptr()), nq, C.c_void_p(d_seeds.data_ptr()), L, K,
+                                   C.c_void_p(out_ids.data_ptr()), None, C.c_void_p(stream)) == 5  # WV_ERR_LIMIT

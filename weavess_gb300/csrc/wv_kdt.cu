@@ -588,9 +588,9 @@ __global__ void k_kdt_fill(const float *__restrict__ base, uint32_t d, uint32_t 
 // getSearchNodeList's order (the query's side of a cut first), then the
 // warp takes their ids leaf-major across the trees without repeats (the base
 // id equal to the query's number excluded); taken[q] = how many
-__global__ void k_kdt_entry(const KNode *nodes, const uint32_t *leaf, uint32_t n, uint32_t T, const float *queries,
-                            uint32_t nq, uint32_t d, uint32_t L, uint32_t lsize, int *vn, uint32_t *seeds,
-                            uint32_t stride, uint32_t *taken, int *status) {
+__global__ void k_kdt_entry(const KNode *nodes, uint32_t nnodes, const uint32_t *leaf, uint32_t n, uint32_t T,
+                            const float *queries, uint32_t nq, uint32_t d, uint32_t L, uint32_t lsize, int *vn,
+                            uint32_t *seeds, uint32_t stride, uint32_t *taken, int *status) {
   const int lane = threadIdx.x & 31;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < nq; q += nw) {
@@ -604,7 +604,17 @@ __global__ void k_kdt_entry(const KNode *nodes, const uint32_t *leaf, uint32_t n
         stack[sp++] = (int)t;
         while (sp > 0 && cnt < lsize) {
           const int nd = stack[--sp];
+          // a forest is walked only as the init left it; a node or a split
+          // dimension out of range is reported, never followed
+          if (nd < 0 || (uint32_t)nd >= nnodes) {
+            set_err(status, DEV_BAD_ID);
+            break;
+          }
           const KNode x = nodes[nd];
+          if (x.left >= 0 && x.right >= 0 && (x.dim < 0 || (uint32_t)x.dim >= d)) {
+            set_err(status, DEV_BAD_ID);
+            break;
+          }
           if (x.left >= 0 && x.right >= 0) {
             if (sp + 2 > KDT_MAX_DEPTH + 2) {
               set_err(status, DEV_OVERFLOW);
@@ -628,6 +638,10 @@ __global__ void k_kdt_entry(const KNode *nodes, const uint32_t *leaf, uint32_t n
         const int nd = vq[t * lsize + ni];
         if (nd < 0) continue;
         const KNode lf = nodes[nd];
+        if (lf.start > lf.end || lf.end > n) {
+          if (lane == 0) set_err(status, DEV_BAD_ID);
+          continue;
+        }
         for (uint32_t j = lf.start; j < lf.end && p < L; j++) {
           const uint32_t id = leaf[(size_t)t * n + j];
           bool hit = false;
@@ -656,6 +670,9 @@ int init_kdt_gpu(wv_ctx *c, uint32_t T, uint32_t K, uint32_t mlevel) {
   WV_CHECK(c, T >= 1 && T <= 4096, WV_ERR_ARG, "nTrees=%u (1..4096)", T);
   WV_CHECK(c, K >= 1 && K <= KDT_MAX_K, WV_ERR_ARG, "K=%u (1..%u)", K, KDT_MAX_K);
   WV_CHECK(c, mlevel < (uint32_t)KDT_MAX_DEPTH, WV_ERR_ARG, "mLevel=%u", mlevel);
+  // the work buffers are rewritten from here on: the old forest is gone
+  // whether or not this init completes
+  c->kdt = KdtForest{};
   const uint32_t n = c->n, d = c->d;
   const size_t total = (size_t)T * n;
   const uint32_t ncap = (uint32_t)std::min<size_t>(2 * total, 0x7fffffffu);
@@ -822,15 +839,19 @@ int init_kdt_gpu(wv_ctx *c, uint32_t T, uint32_t K, uint32_t mlevel) {
   c->fg_w = K;
   c->fg_has_ep = false;
   c->fg_eps.clear();
+  rc = check_device_status(c, "INIT_KDT");
+  if (rc) return rc;
   // the forest stays in the work buffers for SEARCH_ENTRY_KDT
   c->kdt.n = n;
   c->kdt.T = T;
-  return check_device_status(c, "INIT_KDT");
+  c->kdt.nodes = count;
+  return WV_OK;
 }
 
 int draw_seeds_kdt(wv_ctx *c, const float *queries, uint32_t nq, uint32_t L, uint32_t *seeds, uint32_t stride) {
   const KdtForest &F = c->kdt;
-  WV_CHECK(c, F.T > 0 && F.n == c->n, WV_ERR_STATE, "the KD-tree entry needs the trees of wv_init_kdt on this base");
+  WV_CHECK(c, F.T > 0 && F.n == c->n && F.nodes >= F.T, WV_ERR_STATE,
+           "the KD-tree entry needs the trees of a completed wv_init_kdt on this base");
   if (nq == 0) return WV_OK;
   const uint32_t n = F.n, d = c->d, lsize = L / (F.T * KDT_TNS) + 1;
   cudaError_t e = cudaSuccess;
@@ -842,8 +863,8 @@ int draw_seeds_kdt(wv_ctx *c, const float *queries, uint32_t nq, uint32_t L, uin
   uint32_t *dt = c->buf<uint32_t>("kd_taken", nq, &e);
   WV_CUDA(c, e);
   WV_CUDA(c, cudaMemcpyAsync(dq, queries, (size_t)nq * d * 4, cudaMemcpyHostToDevice, c->stream));
-  k_kdt_entry<<<nblocks(nq, 8, c->sms * 16), 256, 0, c->stream>>>(nodes, leaf, n, F.T, dq, nq, d, L, lsize, vn, ds, L,
-                                                                   dt, c->d_status());
+  k_kdt_entry<<<nblocks(nq, 8, c->sms * 16), 256, 0, c->stream>>>(nodes, F.nodes, leaf, n, F.T, dq, nq, d, L, lsize,
+                                                                   vn, ds, L, dt, c->d_status());
   WV_CUDA(c, cudaGetLastError());
   std::vector<uint32_t> taken(nq), hs((size_t)nq * L);
   WV_CUDA(c, cudaMemcpyAsync(hs.data(), ds, hs.size() * 4, cudaMemcpyDeviceToHost, c->stream));

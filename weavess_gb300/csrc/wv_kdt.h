@@ -17,11 +17,13 @@ struct KNode {
   int depth, tree;
 };
 
-// the forest of the last wv_init_kdt on the current base (n, T; 0 while
-// none): its nodes and T x n id lists stay in the context's work buffers
-// "kd_nodes" / "kd_leaf" (node t is the root of tree t) for the search entry
+// the forest of the last wv_init_kdt on the current base (n, T, node count;
+// all 0 while none): its nodes and T x n id lists stay in the context's work
+// buffers "kd_nodes" / "kd_leaf" (node t is the root of tree t) for the
+// search entry.  Set only when an init completed: an init that fails part
+// way (the buffers then hold a partial forest) leaves it cleared.
 struct KdtForest {
-  uint32_t n = 0, T = 0;
+  uint32_t n = 0, T = 0, nodes = 0;
 };
 
 // INIT_KDT on the uploaded base: the current graph becomes the KD-tree graph

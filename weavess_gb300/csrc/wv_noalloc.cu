@@ -16,10 +16,19 @@
 // part that must start at zero; two calls whose work overlaps on the GPU
 // (different streams, or different host threads) race on it.
 //
+// Each warp slot of the launch takes a visited bitset and a touched-word
+// list of n / 32 words each from the array, and a launch has at least one
+// block of search_warps_per_block() = 4 slots, so n is limited to about 67
+// million nodes ((16M - 64) / 8 words per bitset).
+//
 // Host code cannot use the array's name as a device address (it names a
 // host-side stand-in), so the first call on each device looks the address up
 // with cudaGetSymbolAddress while that device is current, and later calls on
 // that device reuse it.  Make that first call before any stream capture.
+// The kept address does not survive a cudaDeviceReset (the module is
+// unloaded with the context); a process that resets a device must not call
+// this entry point on it again.  Each call waits for its stream (the
+// kernel's status word is read back before it returns).
 #include <mutex>
 
 #include "wv_common.cuh"
