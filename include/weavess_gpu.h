@@ -212,6 +212,18 @@ int wv_search_device(wv_ctx *ctx, const float *d_queries, uint32_t nq, uint32_t 
  * the top K are returned.  WV_STORE_FP32 restores the plain form. */
 typedef enum { WV_STORE_FP32 = 0, WV_STORE_BF16 = 1, WV_STORE_FP8 = 2 } wv_storage;
 int wv_set_search_precision(wv_ctx *ctx, int storage, uint32_t rerank);
+/* Traversal of the route searches (wv_search*, plans, the learned search).
+ * No counterpart in the reference, whose RouteInner
+ * (src/component_route.cpp:9-53) expands one pool entry at a time.
+ * parents = 0 (the default): the exact traversal, the reference's expansion
+ * order, ids and DistCount/HopCount equal to RouteInner's.  parents = E in
+ * 1..4: the throughput form -- each step expands the E best unexpanded pool
+ * entries together, seeds are marked visited when pooled, and candidate
+ * distances of bf16 rows (d = 96, 128) and of FP32 rows of integer data
+ * (d = 128) run on the tensor cores; results are a best-first beam search of
+ * the same graph but not the reference's traversal order.  Build-time
+ * candidate searches and the sub-centroid entry always use the exact form. */
+int wv_set_search_expansion(wv_ctx *ctx, uint32_t parents);
 /* Candidate distances of the current precision for nq host queries against
  * m base ids each (ids nq x m): out nq x m (to measure the error). */
 int wv_candidate_distances(wv_ctx *ctx, const float *queries, uint32_t nq, const uint32_t *ids, uint32_t m,

@@ -128,6 +128,7 @@ def load(build_if_needed: bool = True):
     L.wv_nsg_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(BuildStats)]
     L.wv_ssg_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, vp, C.POINTER(BuildStats)]
     L.wv_set_search_precision.argtypes = [vp, C.c_int, C.c_uint32]
+    L.wv_set_search_expansion.argtypes = [vp, C.c_uint32]
     L.wv_candidate_distances.argtypes = [vp, f32p, C.c_uint32, u32p, C.c_uint32, f32p]
     L.wv_learn_default_params.argtypes = [C.POINTER(LearnParams)]
     L.wv_learn_default_params.restype = None

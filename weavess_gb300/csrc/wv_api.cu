@@ -53,8 +53,7 @@ __global__ void k_row_norms(const float *x, uint32_t n, uint32_t d, float *out) 
 }
 
 int ensure_search_scratch(wv_ctx *c, uint32_t Lmax, SearchShape sh, int *out_blocks) {
-  const uint32_t cap = c->gw + 32;
-  int blocks = search_grid(c->d, Lmax, cap, c->device, sh);
+  int blocks = route_grid(c, Lmax, sh);
   WV_CHECK(c, blocks > 0, WV_ERR_LIMIT, "search kernel cannot run with d=%u L=%u width=%u (shared memory)", c->d,
            Lmax, c->gw);
   size_t slots = (size_t)blocks * sh.wpb;
@@ -115,7 +114,13 @@ SearchArgs wv::search_args(wv_ctx *c, const float *d_q, uint32_t nq, const uint3
   a.qscale = c->qscale.as<float>();
   a.qnorm = c->qnorm.as<float>();
   a.rerank = c->rerank == 0 ? Lmax : c->rerank;
+  a.parents = c->parents;
   return a;
+}
+
+int wv::route_grid(wv_ctx *c, uint32_t Lmax, SearchShape sh) {
+  return c->parents > 0 ? beam_grid(c->d, Lmax, c->gw, c->parents, c->device, sh)
+                        : search_grid(c->d, Lmax, c->gw + 32, c->device, sh);
 }
 
 int wv::search_enqueue(wv_ctx *c, const SearchArgs &a, SearchShape shape, int blocks) {

@@ -58,6 +58,9 @@ struct wv_ctx {
   // low-precision copy of the base for candidate distances
   int storage = 0;
   uint32_t rerank = 0;
+  // route searches: 0 the exact traversal; E >= 1 the throughput form with
+  // E parents expanded per step (wv_set_search_expansion)
+  uint32_t parents = 0;
   wv::DevBuf qbase, qscale, qnorm;  // qnorm: squared norms of the low-precision rows
 
   // search graph (load_graph_)
@@ -160,6 +163,10 @@ SearchArgs search_args(wv_ctx *c, const float *d_q, uint32_t nq, const uint32_t 
                        uint32_t Lmax, uint32_t *d_out, float *d_dist, uint32_t out_stride);
 // clears the query counter and the counters, launches; nothing synchronizes
 // (capturable once search_prepare ran)
+// persistent grid of a route search at beams up to Lmax in shape sh: the
+// exact kernel's, or the throughput form's when the context expands E > 0
+// parents per step
+int route_grid(wv_ctx *c, uint32_t Lmax, SearchShape sh);
 int search_enqueue(wv_ctx *c, const SearchArgs &a, SearchShape shape, int blocks);
 
 // records `ev` on `s`; inside a stream capture as an event node of the graph

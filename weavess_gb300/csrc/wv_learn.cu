@@ -449,6 +449,14 @@ int learn_fit(wv_ctx *c, const float *train_q, uint32_t nt, const LearnParams &p
   LearnState &S = state(c);
   S.ready = false;
   S.layout(c->d, p.clusters);
+  // the traces and labels come from the plain search in the exact traversal
+  // (the judge), whatever expansion width later searches use
+  struct KeepParents {
+    wv_ctx *c;
+    uint32_t p;
+    ~KeepParents() { c->parents = p; }
+  } keep_parents{c, c->parents};
+  c->parents = 0;
   const uint32_t C = p.clusters, d = c->d, n = c->n;
   cudaError_t e = cudaSuccess;
   cudaEvent_t e0, e1;

@@ -149,7 +149,7 @@ int prepare(wv_plan *p) {
   } else {
     p->Lcap = p->p.L_max;
   }
-  const int grid = search_grid(c->d, p->Lcap, c->gw + 32, c->device, p->shape);
+  const int grid = route_grid(c, p->Lcap, p->shape);
   WV_CHECK(c, grid > 0, WV_ERR_LIMIT, "search kernel cannot run with d=%u L=%u width=%u", c->d, p->Lcap, c->gw);
   p->blocks = std::min<int>(grid, (int)((p->p.nq_max + p->shape.wpb - 1) / p->shape.wpb));
   return ensure_scratch(p, (size_t)p->blocks * p->shape.wpb);
@@ -215,7 +215,7 @@ int stage(wv_plan *p, uint32_t nq) {
 // times the search of the staged batch with one shape (best of 3)
 int time_shape(wv_plan *p, uint32_t nq, SearchShape sh, cudaEvent_t e0, cudaEvent_t e1, float *ms, int *blocks) {
   wv_ctx *c = p->c;
-  const int grid = search_grid(c->d, p->Lcap, c->gw + 32, c->device, sh);
+  const int grid = route_grid(c, p->Lcap, sh);
   if (grid <= 0) return WV_ERR_LIMIT;
   *blocks = std::min<int>(grid, (int)((nq + sh.wpb - 1) / sh.wpb));
   int rc = ensure_scratch(p, (size_t)*blocks * sh.wpb);

@@ -126,6 +126,15 @@ int wv_set_search_precision(wv_ctx *c, int storage, uint32_t rerank) {
   return WV_OK;
 }
 
+int wv_set_search_expansion(wv_ctx *c, uint32_t parents) {
+  if (!c) return WV_ERR_ARG;
+  WV_CHECK(c, parents <= BEAM_MAX_PARENTS, WV_ERR_ARG, "parents=%u (0 for the exact traversal, 1..%u)", parents,
+           BEAM_MAX_PARENTS);
+  c->generation++;
+  c->parents = parents;
+  return WV_OK;
+}
+
 int wv_candidate_distances(wv_ctx *c, const float *queries, uint32_t nq, const uint32_t *ids, uint32_t m,
                            float *out) {
   if (!c || !queries || !ids || !out) return WV_ERR_ARG;

@@ -61,6 +61,10 @@ struct SearchArgs {
   const float *qscale;
   const float *qnorm;  // squared norms of the low-precision rows
   uint32_t rerank;
+  // 0: the exact traversal (k_search, the reference's expansion order);
+  // E >= 1: the throughput form (k_beam, wv_beam.cu), E pool entries
+  // expanded per step, tensor-core row distances where the layout allows
+  uint32_t parents;
 };
 
 constexpr uint32_t SEARCH_MAX_WIDTH = 256;  // graph row width the kernel accepts
@@ -91,6 +95,15 @@ uint32_t search_hash_min(uint32_t Lmax, uint32_t n);
 int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device, SearchShape sh);
 int search_grid(uint32_t d, uint32_t Lmax, uint32_t cap, int device);
 cudaError_t launch_search(const SearchArgs &a, SearchShape sh, int blocks, cudaStream_t stream);
+
+// the throughput form (wv_beam.cu): candidate entries per warp for graph
+// width gw and E parents per step, the persistent grid of a shape, and the
+// launch (launch_search dispatches to it when a.parents > 0 and the search
+// is a route search without shifted seeds)
+constexpr uint32_t BEAM_MAX_PARENTS = 4;  // pool entries expanded per step, at most
+uint32_t beam_cap(uint32_t gw, uint32_t parents);
+int beam_grid(uint32_t d, uint32_t Lmax, uint32_t gw, uint32_t parents, int device, SearchShape sh);
+cudaError_t launch_beam(const SearchArgs &a, SearchShape sh, int blocks, cudaStream_t stream);
 cudaError_t launch_search_exact(const SearchArgs &a, int blocks, cudaStream_t stream);
 
 }  // namespace wv

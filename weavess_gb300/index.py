@@ -235,6 +235,11 @@ class Context:
         rerank of the first `rerank` pool entries (0 = whole pool)."""
         self._check(self.L.wv_set_search_precision(self.h, self.STORAGE[storage], rerank))
 
+    def set_expansion(self, parents: int = 0):
+        """Route-search traversal: 0 the exact form (the reference's order);
+        E in 1..4 the throughput form, E pool entries expanded per step."""
+        self._check(self.L.wv_set_search_expansion(self.h, int(parents)))
+
     def candidate_distances(self, queries, ids):
         q = _f32(queries)
         ids = _u32(ids)
