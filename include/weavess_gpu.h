@@ -270,6 +270,11 @@ int wv_learn_predict(wv_ctx *ctx, const float *queries, uint32_t nq, uint32_t *c
 int wv_learn_assign(wv_ctx *ctx, const uint32_t *ids, uint32_t n, uint32_t *cluster);
 /* Overrides the calibrated beam margin (beam = margin * 2^regressor). */
 int wv_learn_set_margin(wv_ctx *ctx, float margin);
+/* The fallback: queries whose top entry-cluster probability is below p take
+ * the plain search instead (SearchEntryRand seeds, beam L_plain, drawn in
+ * query order as the plain search draws them); L_plain also sizes the plain
+ * seeds that fill short entry lists.  p = 0 turns the fallback off. */
+int wv_learn_set_fallback(wv_ctx *ctx, float p, uint32_t L_plain);
 /* Plain (SearchEntryRand) seeds per query that wv_search_learned draws on the
  * host and copies to the device: the trace beam, or 0 when no query can read
  * one (no fallback and every entry list covers the largest beam). */

@@ -135,3 +135,45 @@ def test_learned_search_beats_plain_at_equal_recall():
             break
     assert r_l >= 0.9, (r_l, rep)
     assert dc_p is None or dc_p > 1.5 * dc_l, (dc_p, dc_l, r_l, rep, float(Ls.mean()))
+
+
+@pytest.mark.parametrize("E,storage", [(0, "fp32"), (2, "bf16")])
+def test_learned_fallback_returns_the_plain_search(E, storage):
+    """Queries below the confidence threshold take the plain search (rand
+    seeds drawn in query order, beam L_plain): their ids equal the plain
+    search's with the same seeds under the same traversal and precision, the
+    other queries keep their learned beams."""
+    from weavess_gb300 import Context
+    base, query = ds.int_mixture(100_000, 128, 64, seed=11, n_query=400)
+    _, train = ds.int_mixture(0, 128, 64, seed=11, n_query=20_000, query_stream=3)
+    ctx = Context(0)
+    ctx.upload_base(base)
+    ctx.srand(1)
+    ctx.init_random(10)
+    ctx.nnd_refine(10, 32, 40, 6, 60)
+    ctx.load_built_graph()
+    ctx.learn_fit(train, clusters=16, L_trace=256, L_max=128, list_len=128, epochs=2, batch=1024)
+    _, prob, _ = ctx.learn_predict(query)
+    # a threshold in a clear gap of the probabilities near their 30% quantile
+    # (the host and the device round the softmax differently)
+    ps = np.sort(prob)
+    gaps = [(ps[i + 1] - ps[i], i) for i in range(len(ps) // 5, len(ps) // 2)]
+    _, i = max(gaps)
+    p = float((ps[i] + ps[i + 1]) / 2)
+    Lp = 200
+    ctx.learn_set_fallback(p, Lp)
+    ctx.set_precision(storage)
+    ctx.set_expansion(E)
+    try:
+        ctx.srand(5)
+        res, _, _, Ls = ctx.search_learned(query, 10, return_L=True)
+        fb = prob < p
+        assert fb.sum() > 20
+        assert np.all(Ls[fb] == Lp) and np.all(Ls[~fb] <= 128)
+        ctx.srand(5)
+        seeds = ctx.draw_seeds(query.shape[0], Lp, "rand")
+        plain, _, _ = ctx.search(query, Lp, 10, entry=seeds)
+        assert np.array_equal(res[fb], plain[fb])
+    finally:
+        ctx.set_expansion(0)
+        ctx.set_precision("fp32")

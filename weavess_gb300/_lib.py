@@ -137,6 +137,7 @@ def load(build_if_needed: bool = True):
     L.wv_search_learned_device.argtypes = [vp, vp, C.c_uint32, C.c_uint32, vp, vp, vp, C.POINTER(Counters)]
     L.wv_learn_set_margin.argtypes = [vp, C.c_float]
     L.wv_learn_plain_beam.argtypes = [vp, C.POINTER(C.c_uint32)]
+    L.wv_learn_set_fallback.argtypes = [vp, C.c_float, C.c_uint32]
     L.wv_learn_predict.argtypes = [vp, f32p, C.c_uint32, u32p, f32p, f32p]
     L.wv_learn_assign.argtypes = [vp, u32p, C.c_uint32, u32p]
     L.wv_learn_param_count.argtypes = [C.c_uint32, C.c_uint32, C.POINTER(C.c_ulonglong)]

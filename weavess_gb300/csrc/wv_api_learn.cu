@@ -100,6 +100,15 @@ int wv_learn_set_margin(wv_ctx *c, float margin) {
   return learn_set_margin(c, margin);
 }
 
+int wv_learn_set_fallback(wv_ctx *c, float p, uint32_t L_plain) {
+  if (!c || !(p >= 0.f && p <= 1.f)) return WV_ERR_ARG;
+  WV_CHECK(c, c->learn, WV_ERR_STATE, "no trained model");
+  WV_CHECK(c, L_plain >= 1 && L_plain < c->n && L_plain <= SEARCH_MAX_L, WV_ERR_ARG,
+           "fallback beam %u (1..min(n - 1, %u))", L_plain, SEARCH_MAX_L);
+  c->generation++;
+  return learn_set_fallback(c, p, L_plain);
+}
+
 int wv_learn_plain_beam(wv_ctx *c, uint32_t *L) {
   if (!c || !L) return WV_ERR_ARG;
   WV_CHECK(c, c->learn, WV_ERR_STATE, "no trained model");

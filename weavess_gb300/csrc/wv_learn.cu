@@ -860,6 +860,13 @@ int learn_set_margin(wv_ctx *c, float margin) {
   return WV_OK;
 }
 
+int learn_set_fallback(wv_ctx *c, float p, uint32_t L_plain) {
+  LearnState &S = *static_cast<LearnState *>(c->learn);
+  S.fallback_p = p;
+  S.L_plain = L_plain;
+  return WV_OK;
+}
+
 uint32_t learn_plain_beam(wv_ctx *c) {
   if (!c->learn) return 0u;
   const LearnState &S = *static_cast<LearnState *>(c->learn);

@@ -45,6 +45,7 @@ int learn_grad(wv_ctx *c, const float *x, const uint32_t *yc, const float *yr, u
                const float *params, float lam, float *grad, float *loss);
 size_t learn_param_count(uint32_t d, uint32_t C);
 int learn_set_margin(wv_ctx *c, float margin);
+int learn_set_fallback(wv_ctx *c, float p, uint32_t L_plain);
 int learn_predict(wv_ctx *c, const float *q, uint32_t nq, uint32_t *cluster, float *prob, float *log2L);
 int learn_assign(wv_ctx *c, const uint32_t *ids, uint32_t n, uint32_t *cluster);
 // plain seeds per query the learned search may read (the trace beam), or 0

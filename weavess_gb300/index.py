@@ -275,6 +275,11 @@ class Context:
     def learn_set_margin(self, margin: float):
         self._check(self.L.wv_learn_set_margin(self.h, margin))
 
+    def learn_set_fallback(self, p: float, L_plain: int):
+        """Queries whose top entry-cluster probability is below p take the
+        plain search at beam L_plain (p = 0: no fallback)."""
+        self._check(self.L.wv_learn_set_fallback(self.h, float(p), int(L_plain)))
+
     def learn_plain_beam(self) -> int:
         v = C.c_uint32()
         self._check(self.L.wv_learn_plain_beam(self.h, C.byref(v)))
