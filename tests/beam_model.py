@@ -20,7 +20,9 @@ entries per step.  Its rules:
 * the next step restarts at min(the smallest final position of a merged
   candidate, the last parent's position + 1);
 * low-precision candidates: the finite head of the final pool (up to
-  `rerank` entries) is re-scored by `exact` and stably re-sorted.
+  `rerank` entries) is re-scored by `exact` and stably re-sorted -- except
+  bf16 candidates of integer data at d <= 128, which are exact and are not
+  re-scored (pass rerank=0).
 
 On integer data in [0, 255] (d <= 128) every distance path of the kernel is
 exact, so this statement and the kernel agree id for id, distance for

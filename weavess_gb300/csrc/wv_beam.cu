@@ -32,7 +32,8 @@
 //
 // Other row layouts (fp8, other d) use the warp-cooperative row distances of
 // the exact form.  The final pool of low-precision candidates is re-ranked in
-// FP32 as in the exact form.  DistCount counts every distance taken (seeds
+// FP32 as in the exact form, except bf16 candidates of integer data at
+// d <= 128, which are exact already.  DistCount counts every distance taken (seeds
 // included), HopCount every expanded node.
 #include <cuda_bf16.h>
 
@@ -262,10 +263,9 @@ __device__ void beam_sort_seeds(const BeamSmem &s, int L, int lane) {
   __syncwarp();
 }
 
-// merges the ncand accepted candidates (cd, ci; visit order) into the sorted
-// pool of L entries, stably; returns the smallest final position of a
-// candidate (L if none stays)
-__device__ int beam_merge(const BeamSmem &s, int L, int ncand, int lane) {
+// the ncand accepted candidates (cd, ci; visit order) sorted stably by
+// distance into (sd, si)
+__device__ void beam_sort_cands(const BeamSmem &s, int ncand, int lane) {
   for (int c = lane; c < ncand; c += 32) {
     const float dc = s.cd[c];
     int r = 0;
@@ -277,6 +277,12 @@ __device__ int beam_merge(const BeamSmem &s, int L, int ncand, int lane) {
     s.si[r] = s.ci[c];
   }
   __syncwarp();
+}
+
+// merges the ncand sorted candidates (sd, si) into the sorted pool of L
+// entries, stably (pool entries before equal candidates); returns the
+// smallest final position of a candidate (L if none stays)
+__device__ int beam_merge(const BeamSmem &s, int L, int ncand, int lane) {
   uint32_t *ub = s.ci;
   int mink = L;
   for (int c = lane; c < ncand; c += 32) {
@@ -409,11 +415,21 @@ __global__ void __maxnreg__(128) k_beam(SearchArgs a) {
     }
     __syncwarp();
 
-    // ---- steps of E expansions
+    // ---- steps of E expansions.  The rows of the next step's parents are
+    // read before the merge that settles them: the next parents are the
+    // first E unexpanded entries of the merged pool, i.e. the E closest of
+    // the pool's next unexpanded entries and the sorted candidates, so their
+    // row reads overlap the merge; a step takes the rows read for its
+    // parents and reads only those of parents that were not foreseen.
+    uint32_t pnode = INVALID, pdeg = 0;  // lane t < npred: foreseen parent t, its degree
+    uint32_t phead[BEAM_MAX_PARENTS];    // the first 32 slots of their rows
+    int npred = 0;
+#pragma unroll
+    for (int c = 0; c < BEAM_MAX_PARENTS; c++) phead[c] = INVALID;
     int k = first_flag(pi, 0, L, lane);
     while (k < L) {
       // the first E unexpanded entries from k (lane p < got holds the p-th
-      // position), and the next E after them, whose rows go toward L2
+      // position), and the next E after them (lane p < pf)
       int got = 0, pf = 0, mypos = -1, pfpos = -1;
       for (int b = k; b < L && pf < E; b += 32) {
         unsigned fm = __ballot_sync(FULL, b + lane < L && (pi[b + lane] & FLAG));
@@ -434,25 +450,31 @@ __global__ void __maxnreg__(128) k_beam(SearchArgs a) {
       if (lane < got) node = pi[mypos] & ID_MASK;
       __syncwarp();
       if (lane < got) pi[mypos] = node;  // expanded
-      if (lane < pf) {
-        const uint32_t nx = pi[pfpos] & ID_MASK;
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(a.gids + (size_t)nx * a.gw));
-      }
       __syncwarp();
       hcount += got;
-      uint32_t deg = lane < got ? __ldg(a.gdeg + node) : 0u;
-      if (deg > a.gw) {
-        set_err(a.status, DEV_BAD_ID);
-        deg = a.gw;
-      }
       const float thr = pd[L - 1];
-      // the first 32 slots of every parent's row, loaded together
-      uint32_t head[BEAM_MAX_PARENTS];
+      // each parent's degree and the first 32 slots of its row (slots past
+      // the degree are read and ignored: rows are gw wide), from the rows
+      // read ahead when the parent was foreseen
+      uint32_t head[BEAM_MAX_PARENTS], dgs[BEAM_MAX_PARENTS];
 #pragma unroll
       for (int c = 0; c < BEAM_MAX_PARENTS; c++) {
-        const uint32_t nd = __shfl_sync(FULL, node, c);
-        const uint32_t dg = __shfl_sync(FULL, deg, c);
-        head[c] = (c < got && (uint32_t)lane < dg) ? __ldg(a.gids + (size_t)nd * a.gw + lane) : INVALID;
+        head[c] = INVALID;
+        dgs[c] = 0;
+        if (c < got) {
+          const uint32_t nd = __shfl_sync(FULL, node, c);
+          const unsigned hit = __ballot_sync(FULL, lane < npred && pnode == nd);
+          if (hit) {
+            const int m = __ffs(hit) - 1;
+            dgs[c] = __shfl_sync(FULL, pdeg, m);
+#pragma unroll
+            for (int t = 0; t < BEAM_MAX_PARENTS; t++)
+              if (t == m) head[c] = phead[t];
+          } else {
+            dgs[c] = __ldg(a.gdeg + nd);
+            head[c] = (uint32_t)lane < a.gw ? __ldg(a.gids + (size_t)nd * a.gw + lane) : INVALID;
+          }
+        }
       }
       // fresh neighbours, parent by parent in adjacency order
       uint32_t nfresh = 0;
@@ -460,7 +482,11 @@ __global__ void __maxnreg__(128) k_beam(SearchArgs a) {
       for (int c = 0; c < BEAM_MAX_PARENTS; c++) {
         if (c >= got) break;
         const uint32_t nd = __shfl_sync(FULL, node, c);
-        const uint32_t dg = __shfl_sync(FULL, deg, c);
+        uint32_t dg = dgs[c];
+        if (dg > a.gw) {
+          if (lane == 0) set_err(a.status, DEV_BAD_ID);
+          dg = a.gw;
+        }
         for (uint32_t m0 = 0; m0 < dg; m0 += 32) {
           const uint32_t mm = m0 + lane;
           uint32_t id = mm < dg ? (m0 == 0 ? head[c] : __ldg(a.gids + (size_t)nd * a.gw + mm)) : INVALID;
@@ -495,12 +521,47 @@ __global__ void __maxnreg__(128) k_beam(SearchArgs a) {
       }
       dcount += nfresh;
       __syncwarp();
+      if (ncand > 0) beam_sort_cands(s, ncand, lane);
+      // foresee the next parents and read their rows
+      {
+        int i = 0, j = 0;
+        npred = 0;
+        pnode = INVALID;
+#pragma unroll
+        for (int t = 0; t < BEAM_MAX_PARENTS; t++) {
+          phead[t] = INVALID;
+          if (t < E) {
+            const int pp = __shfl_sync(FULL, pfpos, i & 31);
+            const float dp = i < pf ? pd[pp] : __int_as_float(0x7f800000);
+            const float dc = j < ncand ? s.sd[j] : __int_as_float(0x7f800000);
+            uint32_t nd = INVALID;
+            if (i < pf && (j >= ncand || dp <= dc)) {
+              nd = pi[pp] & ID_MASK;
+              i++;
+            } else if (j < ncand) {
+              nd = s.si[j];
+              j++;
+            }
+            if (nd != INVALID) {
+              if (lane == t) {
+                pnode = nd;
+                pdeg = __ldg(a.gdeg + nd);
+              }
+              phead[t] = (uint32_t)lane < a.gw ? __ldg(a.gids + (size_t)nd * a.gw + lane) : INVALID;
+              npred = t + 1;
+            }
+          }
+        }
+      }
+      __syncwarp();
       int nk = L;
       if (ncand > 0) nk = beam_merge(s, L, ncand, lane);
       k = first_flag(pi, min(nk, last + 1), L, lane);
     }
-    // ---- exact FP32 rerank of the final pool (low-precision storage)
-    if (a.storage != 0 && a.rerank > 0) {
+    // ---- exact FP32 rerank of the final pool (low-precision storage); bf16
+    // candidates of integer data at d <= 128 are already exact (integer
+    // values, products and partial sums below 2^24), so they keep their order
+    if (a.storage != 0 && a.rerank > 0 && !(a.storage == 1 && ints && a.d <= 128)) {
       // (empty slots, +inf, sit at the tail when seeds repeated)
       const int R = min((int)a.rerank, lower_bound_of(pd, L, __int_as_float(0x7f800000)));
       float *xd = reinterpret_cast<float *>(s.hash);

@@ -346,6 +346,11 @@ int wv_plan_tune(wv_plan *p, uint32_t nq, wv_tune_report *rep) {
   std::vector<SearchShape> cand;
   for (int w : {1, 2, 4, 8})
     for (uint32_t h : areas) cand.push_back(SearchShape{w, h});
+  // the throughput form also tries 32-bit visited-hash entries (half the
+  // slots in the same bytes, but a native compare-and-swap per probe)
+  if (c->parents > 0)
+    for (int w : {1, 2, 4, 8})
+      for (uint32_t h : {0u, 2 * h0}) cand.push_back(SearchShape{w, h, true});
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   WV_CUDA(c, cudaEventCreate(&e0));
   WV_CUDA(c, cudaEventCreate(&e1));
