@@ -44,7 +44,8 @@ METRIC = "QPS at recall@10>=0.95 (learned+BF16 vs plain FP32, 1 GB300); build se
 # DRAM bytes (read + write) of one learned-plan search launch on the 1M x 128
 # workload, by expansion width (0: the exact traversal), from ncu captures of
 # this command (profiles/)
-TRAFFIC_LEARNED_1M = {0: 3251252992 + 4440064}
+TRAFFIC_LEARNED_1M = {0: 2781244672 + 781312, 1: 2289462016 + 993536, 2: 2276730112 + 1079296,
+                      3: 2273065216 + 1006080, 4: 2284729600 + 1025280}
 
 
 def log(*a):
@@ -539,7 +540,8 @@ def run_ours(args):
         roof = {"bound": "hbm", "achieved": round(l_achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(l_achieved / hbm, 4),
                 "traffic": TRAFFIC_LEARNED_1M.get(learned["expansion"]) if cfg["n"] == 1_000_000 else None,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this launch (profiles/)",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of this search launch, "
+                                  "profiles/launches_search_1M.md",
                 "peak_kind": peak_kind, "alg_bytes_per_launch": int(alg), "dist_count": ldc, "hop_count": lhc,
                 "mean_graph_degree": round(avg_deg, 2), "kernel": kname + ", learned seeds, per-query L",
                 "kernel_ms": round(learned["search_kernel_ms"], 4),
