@@ -91,3 +91,29 @@ def test_efanna_matches_oracle_20k(ctx, mix20k, S, L, R):
     assert rows_equal(ids, dist, deg, ge.ids, ge.dist, ge.deg) == 0, st
     assert st["rand_draws"] == 1 + ge.overflow_events
     assert ctx.rand() == ro.next()
+
+
+@pytest.mark.parametrize("d,S,R", [(128, 10, 60), (64, 20, 100), (16, 8, 30)])
+def test_tensor_core_join_equals_fp32_join(ctx, d, S, R, monkeypatch):
+    """The local join's Gram tiles on the tensor cores (integer data, d a
+    multiple of 16, new lists of at most 128 ids) give the offers of the FP32
+    pair kernel: the graphs, the pair and offer counts and the rand() stream
+    are identical, and both equal the single-threaded oracle."""
+    base, _ = ds.int_mixture(12000, d, 24, seed=50 + d)
+    out = {}
+    for path in ("tc", "fp32"):
+        if path == "fp32":
+            monkeypatch.setenv("WV_NND_JOIN", "fp32")
+        else:
+            monkeypatch.delenv("WV_NND_JOIN", raising=False)
+        ctx.upload_base(base)
+        ctx.srand(1)
+        ctx.init_random(S)
+        st = ctx.nnd_refine(S, 24, 40, 6, R)
+        out[path] = (ctx.get_graph(), st, ctx.rand())
+    (g1, st1, r1), (g2, st2, r2) = out["tc"], out["fp32"]
+    assert rows_equal(g1[0], g1[1], g1[2], g2[0], g2[1], g2[2]) == 0
+    assert (st1["pairs"], st1["offers"], st1["rand_draws"], r1) == (st2["pairs"], st2["offers"], st2["rand_draws"], r2)
+    ro = O.Rand(1)
+    g = O.nndescent(base, O.init_random(base, S, ro), S, 24, 40, 6, R, ro)
+    assert rows_equal(g1[0], g1[1], g1[2], g.ids, g.dist, g.deg) == 0

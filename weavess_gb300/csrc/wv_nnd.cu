@@ -31,14 +31,18 @@
 //    context's stream.
 //  * the first join is skipped: nhood(L, S) leaves nn_new as 2S zeros
 //    (index.h:98-103), which join pairs with nothing.
+#include <cuda_bf16.h>
+
 #include <algorithm>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "wv_common.cuh"
 #include "wv_mt.cuh"
 #include "wv_nnd.h"
 #include "wv_scan.h"
+#include "wv_umma.cuh"
 
 namespace wv {
 namespace {
@@ -229,6 +233,7 @@ __global__ void __launch_bounds__(IR_WARPS * 32)
 struct Nnd {
   uint32_t n, d, S, K, L, R, capn, capo;
   const float *base;
+  const float *xnorm;  // squared row norms (integer data; the tensor-core join)
   Ent *pool;
   uint32_t *psz, *M;
   uint32_t *nnew, *nold, *lnew, *lold, *pnew, *pold;
@@ -574,6 +579,176 @@ __global__ void __launch_bounds__(J_THREADS) k_join(Nnd s, uint32_t n0, Offers o
   }
 }
 
+// ---------------------------------------------------------------- join on the tensor cores
+// The same local join for integer data in [0, 255] with d a multiple of 16,
+// d <= 128 and new lists of at most 128 ids: every pair distance is the
+// norm form |x|^2 + |y|^2 - 2 x.y with the dot products of a Gram tile
+// computed by tcgen05.mma, BF16 operands (the integer values are exact in
+// BF16, their products in FP32) and FP32 accumulation in tensor memory --
+// every partial sum an integer below 2^24, so the distances are the exact
+// FP32 values the reference's sequential sum gives, and the offers (targets,
+// keys, candidates, distances) are those of k_join.
+//
+// One CTA of 4 warps per node.  The node's rows (new ++ old) are converted to
+// BF16 into the canonical no-swizzle K-major layout (8 x 8 core matrices of
+// 16-byte rows, K-adjacent core matrices 128 bytes apart, 8-row groups d * 16
+// bytes apart): the first 128 rows (the new rows, then old ones) are the A
+// operand (M = 128) and also the first B chunk; later B chunks of 128 rows
+// take the second buffer.  Per chunk one thread issues d / 16 MMAs (M = 128,
+// N = the chunk's rows rounded up to 16, K = 16) into 128 columns of tensor
+// memory and commits to an mbarrier; warp w reads accumulator lanes
+// 32w..32w+31 (new rows 32w..) 16 columns at a time with tcgen05.ld and
+// emits the two offers of each valid pair.  The targets' pool maxima are read
+// once per node into shared memory (pools do not change during a join
+// chunk).  The wait on the MMAs is bounded: on time-out the CTA reports
+// DEV_TIMEOUT, waits (bounded) once more for its MMAs and frees its tensor
+// memory.
+constexpr int JT_THREADS = 128;
+constexpr uint32_t JT_ROWS = 128;  // rows per operand buffer (M of A, the N chunk of B)
+constexpr uint32_t JT_LBO = 128;
+constexpr uint32_t JT_TMEM_COLS = 128;
+
+__device__ __forceinline__ uint32_t jt_pack(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+// rows [r0, r0 + 128) of the node's list as BF16 in the K-major core layout
+// (zeros past tot)
+__device__ void jt_stage(uint8_t *dst, const float *__restrict__ base, uint32_t d, const uint32_t *ids, uint32_t tot,
+                         uint32_t r0, uint32_t sbo, int tid) {
+  const uint32_t kc = d / 8;
+  for (uint32_t e = tid; e < JT_ROWS * kc; e += JT_THREADS) {
+    const uint32_t r = e / kc, k = (e % kc) * 8;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (r0 + r < tot) {
+      const float4 *src = reinterpret_cast<const float4 *>(base + (size_t)ids[r0 + r] * d + k);
+      const float4 x0 = __ldg(src), x1 = __ldg(src + 1);
+      v = make_uint4(jt_pack(x0.x, x0.y), jt_pack(x0.z, x0.w), jt_pack(x1.x, x1.y), jt_pack(x1.z, x1.w));
+    }
+    *reinterpret_cast<uint4 *>(dst + (r >> 3) * sbo + (k >> 3) * JT_LBO + (r & 7) * 16) = v;
+  }
+}
+
+size_t join_tc_smem(uint32_t d, uint32_t capn, uint32_t capo) {
+  return 2 * (size_t)JT_ROWS * d * 2 + 3 * (size_t)(capn + capo) * 4 + 16;
+}
+
+__global__ void __launch_bounds__(JT_THREADS) k_join_tc(Nnd s, uint32_t n0, Offers of, unsigned long long *pairs,
+                                                        int *status) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_base;
+  const uint32_t n = n0 + blockIdx.x;
+  const uint32_t a = s.lnew[n], b = s.lold[n];
+  if (a == 0) return;  // (block-uniform, before any tensor memory is taken)
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t tot = a + b, d = s.d;
+  const uint32_t sbo = (d / 8) * 128;
+  uint8_t *tA = smem, *tB = smem + (size_t)JT_ROWS * d * 2;
+  uint32_t *ids = reinterpret_cast<uint32_t *>(tB + (size_t)JT_ROWS * d * 2);
+  float *nrm = reinterpret_cast<float *>(ids + s.capn + s.capo);
+  float *mx = nrm + s.capn + s.capo;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(umma::smem_u32(&tmem_base)),
+                 "r"(JT_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    umma::mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  for (uint32_t t = tid; t < tot; t += JT_THREADS) {
+    const uint32_t id = t < a ? s.nnew[(size_t)n * s.capn + t] : s.nold[(size_t)n * s.capo + (t - a)];
+    ids[t] = id;
+    nrm[t] = s.xnorm[id];
+    // nhood::insert's first test against the pool's current maximum (an
+    // empty pool takes nothing here, as k_join's psz test)
+    mx[t] = s.psz[id] > 0 ? s.pool[(size_t)id * s.L].d : __int_as_float(0xff800000);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_base;
+  jt_stage(tA, s.base, d, ids, tot, 0, sbo, tid);
+  unsigned long long npairs = 0;
+  uint32_t phase = 0;
+  bool ok = true;
+  for (uint32_t j0 = 0; j0 < tot && ok; j0 += JT_ROWS) {
+    const uint32_t nc = min(JT_ROWS, tot - j0), ncp = (nc + 15) & ~15u;
+    const uint8_t *bt = j0 == 0 ? tA : tB;
+    if (j0 > 0) jt_stage(tB, s.base, d, ids, tot, j0, sbo, tid);
+    asm volatile("fence.proxy.async.shared::cta;");  // generic stores -> tensor core reads
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t a0 = umma::smem_u32(tA), b0 = umma::smem_u32(bt);
+      const uint32_t idesc = umma::idesc(128, (int)ncp);
+      for (uint32_t kk = 0; kk < d / 16; kk++) {
+        const uint64_t ad = umma::desc(a0 + kk * 2 * JT_LBO, JT_LBO, sbo);
+        const uint64_t bd = umma::desc(b0 + kk * 2 * JT_LBO, JT_LBO, sbo);
+        const uint32_t acc = kk > 0 ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          umma::smem_u32(&bar)));
+    }
+    ok = __syncthreads_and(umma::mbar_wait(&bar, phase)) != 0;
+    phase ^= 1;
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (!ok) break;
+    if ((uint32_t)warp * 32 < a) {
+      const uint32_t gi = warp * 32 + lane;
+      const bool rowok = gi < a;
+      const uint32_t iid = rowok ? ids[gi] : 0u;
+      const float ni = rowok ? nrm[gi] : 0.f, mi = rowok ? mx[gi] : __int_as_float(0xff800000);
+      for (uint32_t c0 = 0; c0 < ncp && j0 + c0 < tot; c0 += 16) {
+        uint32_t v[16];
+        const uint32_t addr = tmem + ((uint32_t)(warp * 32) << 16) + c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(addr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++) {
+          const uint32_t gj = j0 + c0 + jj;
+          if (gj >= tot) break;  // (warp-uniform)
+          const uint32_t jid = ids[gj];
+          const bool valid = rowok && (gj < a ? (iid < jid) : (iid != jid));
+          // integers below 2^24 throughout: the exact FP32 distance
+          const float dist = (ni + nrm[gj]) - 2.f * __uint_as_float(v[jj]);
+          npairs += valid;
+          const unsigned long long kbase = ((unsigned long long)n << 32) | ((gi * tot + gj) << 1);
+          emit(of, valid && dist <= mi, iid, kbase, jid, dist, lane, status);
+          emit(of, valid && dist <= mx[gj], jid, kbase | 1ull, iid, dist, lane, status);
+        }
+      }
+    }
+    // the accumulator is read and the B buffer free before the next chunk
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+  }
+  if (!ok) {
+    if (tid == 0) set_err(status, DEV_TIMEOUT);
+    // the MMAs of the chunk that timed out may still run: wait for them
+    // (bounded) before the tensor memory is freed
+    umma::mbar_wait(&bar, phase ^ 1);
+  }
+  if (pairs) {
+    for (int o = 16; o > 0; o >>= 1) npairs += __shfl_xor_sync(FULL, npairs, o);
+    if (lane == 0 && npairs) atomicAdd(pairs, npairs);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(JT_TMEM_COLS));
+}
+
 // targets with offers, and the largest segment
 __global__ void k_active(uint32_t n, const uint32_t *tcnt, uint32_t *act, uint32_t *nact, uint32_t *big,
                          uint32_t *nbig, uint32_t warp_cap, uint32_t *maxseg) {
@@ -824,6 +999,7 @@ int nndescent_gpu(wv_ctx *c, const NndParams &p, NndStats *st) {
   s.capn = std::max(p.S + p.R, 2 * p.S);  // EFANNA's first nn_new holds 2S ids
   s.capo = std::min(p.L + p.R, 2 * p.R);
   s.base = c->base.as<float>();
+  s.xnorm = c->base_int ? c->xnorm.as<float>() : nullptr;
   s.pool = c->buf<Ent>("pool", (size_t)n * p.L, &e);
   s.psz = c->buf<uint32_t>("psz", n, &e);
   s.M = c->buf<uint32_t>("M", n, &e);
@@ -905,6 +1081,15 @@ int nndescent_gpu(wv_ctx *c, const NndParams &p, NndStats *st) {
                                                           c->fg_deg.as<uint32_t>(), c->fg_w, p.efanna ? 1 : 0);
   WV_CUDA(c, cudaGetLastError());
 
+  // the local join's pair distances: on the tensor cores where they are exact
+  // (integer data, d a multiple of 16 up to 128, new lists of at most 128
+  // ids; WV_NND_JOIN=fp32 keeps the FP32 pair kernel), else in FP32 in the
+  // reference's order.  Both give the same offers.
+  const char *join_env = getenv("WV_NND_JOIN");
+  const bool join_tc = c->base_int && c->d % 16 == 0 && c->d <= 128 && s.capn <= JT_ROWS &&
+                       !(join_env && std::string(join_env) == "fp32");
+  const size_t jtc_smem = join_tc_smem(c->d, s.capn, s.capo);
+  if (join_tc) WV_CUDA(c, cudaFuncSetAttribute(k_join_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jtc_smem));
   const uint32_t stride = ((c->d + 3) & ~3u) + 4;
   uint32_t tjc = J_TJ;
   while (tjc > 32 && (size_t)(J_TI + tjc) * stride * 4 > 200 * 1024) tjc -= 32;
@@ -943,7 +1128,10 @@ int nndescent_gpu(wv_ctx *c, const NndParams &p, NndStats *st) {
         while (true) {
           WV_CUDA(c, cudaMemsetAsync(tcnt, 0, (size_t)n * 4, c->stream));
           WV_CUDA(c, cudaMemsetAsync(small, 0, 16, c->stream));
-          k_join<<<n1 - n0, J_THREADS, join_smem, c->stream>>>(s, n0, of, pairs, c->d_status(), tjc);
+          if (join_tc)
+            k_join_tc<<<n1 - n0, JT_THREADS, jtc_smem, c->stream>>>(s, n0, of, pairs, c->d_status());
+          else
+            k_join<<<n1 - n0, J_THREADS, join_smem, c->stream>>>(s, n0, of, pairs, c->d_status(), tjc);
           WV_CUDA(c, cudaGetLastError());
           k_active<<<nb, NODE_THREADS, 0, c->stream>>>(n, tcnt, act, small, big, small + 1, AP_WARP_CAP, small + 2);
           uint32_t hs[4];

@@ -28,6 +28,7 @@
 
 #include "wv_common.cuh"
 #include "wv_mlp.cuh"
+#include "wv_umma.cuh"
 
 namespace wv {
 namespace {
@@ -37,49 +38,13 @@ constexpr int STAGE_A = TM * TK * 2, STAGE_B = TN * TK * 2;  // bytes per stage
 constexpr uint32_t LBO = 128;                        // K-adjacent core matrices
 constexpr uint32_t SBO = (TK / 8) * 128;             // 8-row groups
 constexpr uint32_t TMEM_COLS = 128;
-constexpr long long WAIT_LIMIT = 1ll << 26;          // polls before giving up
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
+using umma::mbar_init;
+using umma::mbar_wait;
+using umma::smem_u32;
 
-// shared-memory matrix descriptor (no swizzle): start, leading and stride
-// byte offsets in 16-byte units, the descriptor version bit (46), layout 0
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
-  d |= (uint64_t)((LBO >> 4) & 0x3FFF) << 16;
-  d |= (uint64_t)((SBO >> 4) & 0x3FFF) << 32;
-  d |= (uint64_t)1 << 46;
-  return d;
-}
-
-// instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major,
-// N >> 3 and M >> 4
-__host__ __device__ constexpr uint32_t umma_idesc(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.u32 %0, 1, 0, P;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// bounded wait: false on time-out
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (long long i = 0; i < WAIT_LIMIT; i++)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) { return umma::desc(saddr, LBO, SBO); }
+__host__ __device__ constexpr uint32_t umma_idesc(int M, int N) { return umma::idesc(M, N); }
 
 // the byte offset of element (row, k) of a staged operand
 __device__ __forceinline__ uint32_t core_off(int row, int k) {
