@@ -592,17 +592,18 @@ __global__ void __launch_bounds__(J_THREADS) k_join(Nnd s, uint32_t n0, Offers o
 // One CTA of 4 warps per node.  The node's rows (new ++ old) are converted to
 // BF16 into the canonical no-swizzle K-major layout (8 x 8 core matrices of
 // 16-byte rows, K-adjacent core matrices 128 bytes apart, 8-row groups d * 16
-// bytes apart): the first 128 rows (the new rows, then old ones) are the A
-// operand (M = 128) and also the first B chunk; later B chunks of 128 rows
-// take the second buffer.  Per chunk one thread issues d / 16 MMAs (M = 128,
-// N = the chunk's rows rounded up to 16, K = 16) into 128 columns of tensor
+// bytes apart).  The first 128 rows (the new rows, then old ones) are the B
+// operand (N = the new rows rounded up to 16) and also the first A tile;
+// later A tiles of 128 rows take the second buffer.  Per tile one thread
+// issues d / 16 MMAs (M = 128, N, K = 16) into up to 128 columns of tensor
 // memory and commits to an mbarrier; warp w reads accumulator lanes
-// 32w..32w+31 (new rows 32w..) 16 columns at a time with tcgen05.ld and
-// emits the two offers of each valid pair.  The targets' pool maxima are read
-// once per node into shared memory (pools do not change during a join
-// chunk).  The wait on the MMAs is bounded: on time-out the CTA reports
-// DEV_TIMEOUT, waits (bounded) once more for its MMAs and frees its tensor
-// memory.
+// 32w..32w+31 (rows j of new ++ old) 16 columns (new rows i) at a time with
+// tcgen05.ld and emits the two offers of each valid pair (i, j) -- all four
+// warps hold rows, the columns run over the short new list.  The targets'
+// pool maxima are read once per node into shared memory (pools do not change
+// during a join chunk).  The wait on the MMAs is bounded: on time-out the CTA
+// reports DEV_TIMEOUT, waits (bounded) once more for its MMAs and frees its
+// tensor memory.
 constexpr int JT_THREADS = 128;
 constexpr uint32_t JT_ROWS = 128;  // rows per operand buffer (M of A, the N chunk of B)
 constexpr uint32_t JT_LBO = 128;
@@ -674,16 +675,16 @@ __global__ void __launch_bounds__(JT_THREADS) k_join_tc(Nnd s, uint32_t n0, Offe
   unsigned long long npairs = 0;
   uint32_t phase = 0;
   bool ok = true;
-  for (uint32_t j0 = 0; j0 < tot && ok; j0 += JT_ROWS) {
-    const uint32_t nc = min(JT_ROWS, tot - j0), ncp = (nc + 15) & ~15u;
-    const uint8_t *bt = j0 == 0 ? tA : tB;
-    if (j0 > 0) jt_stage(tB, s.base, d, ids, tot, j0, sbo, tid);
+  const uint32_t acols = (a + 15) & ~15u;  // N: the new rows, rounded up to 16
+  for (uint32_t m0 = 0; m0 < tot && ok; m0 += JT_ROWS) {
+    const uint8_t *at = m0 == 0 ? tA : tB;
+    if (m0 > 0) jt_stage(tB, s.base, d, ids, tot, m0, sbo, tid);
     asm volatile("fence.proxy.async.shared::cta;");  // generic stores -> tensor core reads
     __syncthreads();
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t a0 = umma::smem_u32(tA), b0 = umma::smem_u32(bt);
-      const uint32_t idesc = umma::idesc(128, (int)ncp);
+      const uint32_t a0 = umma::smem_u32(at), b0 = umma::smem_u32(tA);
+      const uint32_t idesc = umma::idesc(128, (int)acols);
       for (uint32_t kk = 0; kk < d / 16; kk++) {
         const uint64_t ad = umma::desc(a0 + kk * 2 * JT_LBO, JT_LBO, sbo);
         const uint64_t bd = umma::desc(b0 + kk * 2 * JT_LBO, JT_LBO, sbo);
@@ -700,12 +701,12 @@ __global__ void __launch_bounds__(JT_THREADS) k_join_tc(Nnd s, uint32_t n0, Offe
     phase ^= 1;
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (!ok) break;
-    if ((uint32_t)warp * 32 < a) {
-      const uint32_t gi = warp * 32 + lane;
-      const bool rowok = gi < a;
-      const uint32_t iid = rowok ? ids[gi] : 0u;
-      const float ni = rowok ? nrm[gi] : 0.f, mi = rowok ? mx[gi] : __int_as_float(0xff800000);
-      for (uint32_t c0 = 0; c0 < ncp && j0 + c0 < tot; c0 += 16) {
+    if (m0 + (uint32_t)warp * 32 < tot) {
+      const uint32_t gj = m0 + warp * 32 + lane;  // this lane's row of new ++ old
+      const bool rowok = gj < tot;
+      const uint32_t jid = rowok ? ids[gj] : 0u;
+      const float nj = rowok ? nrm[gj] : 0.f, mj = rowok ? mx[gj] : __int_as_float(0xff800000);
+      for (uint32_t c0 = 0; c0 < a; c0 += 16) {
         uint32_t v[16];
         const uint32_t addr = tmem + ((uint32_t)(warp * 32) << 16) + c0;
         asm volatile(
@@ -715,21 +716,21 @@ __global__ void __launch_bounds__(JT_THREADS) k_join_tc(Nnd s, uint32_t n0, Offe
             : "r"(addr));
         asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-        for (int jj = 0; jj < 16; jj++) {
-          const uint32_t gj = j0 + c0 + jj;
-          if (gj >= tot) break;  // (warp-uniform)
-          const uint32_t jid = ids[gj];
+        for (int ii = 0; ii < 16; ii++) {
+          const uint32_t gi = c0 + ii;  // a new row (warp-uniform)
+          if (gi >= a) continue;
+          const uint32_t iid = ids[gi];
           const bool valid = rowok && (gj < a ? (iid < jid) : (iid != jid));
           // integers below 2^24 throughout: the exact FP32 distance
-          const float dist = (ni + nrm[gj]) - 2.f * __uint_as_float(v[jj]);
+          const float dist = (nrm[gi] + nj) - 2.f * __uint_as_float(v[ii]);
           npairs += valid;
           const unsigned long long kbase = ((unsigned long long)n << 32) | ((gi * tot + gj) << 1);
-          emit(of, valid && dist <= mi, iid, kbase, jid, dist, lane, status);
-          emit(of, valid && dist <= mx[gj], jid, kbase | 1ull, iid, dist, lane, status);
+          emit(of, valid && dist <= mx[gi], iid, kbase, jid, dist, lane, status);
+          emit(of, valid && dist <= mj, jid, kbase | 1ull, iid, dist, lane, status);
         }
       }
     }
-    // the accumulator is read and the B buffer free before the next chunk
+    // the accumulator is read and the A buffer free before the next tile
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
