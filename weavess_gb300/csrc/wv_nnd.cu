@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(J_THREADS) k_join(Nnd s, uint32_t n0, Offers o
 // FP32 values the reference's sequential sum gives, and the offers (targets,
 // keys, candidates, distances) are those of k_join.
 //
-// One CTA of 4 warps per node.  The node's rows (new ++ old) are converted to
+// One CTA of 8 warps per node.  The node's rows (new ++ old) are converted to
 // BF16 into the canonical no-swizzle K-major layout (8 x 8 core matrices of
 // 16-byte rows, K-adjacent core matrices 128 bytes apart, 8-row groups d * 16
 // bytes apart).  The first 128 rows (the new rows, then old ones) are the B
@@ -597,14 +597,15 @@ __global__ void __launch_bounds__(J_THREADS) k_join(Nnd s, uint32_t n0, Offers o
 // later A tiles of 128 rows take the second buffer.  Per tile one thread
 // issues d / 16 MMAs (M = 128, N, K = 16) into up to 128 columns of tensor
 // memory and commits to an mbarrier; warp w reads accumulator lanes
-// 32w..32w+31 (rows j of new ++ old) 16 columns (new rows i) at a time with
-// tcgen05.ld and emits the two offers of each valid pair (i, j) -- all four
-// warps hold rows, the columns run over the short new list.  The targets'
+// 32(w % 4).. (rows j of new ++ old) 16 columns (new rows i) at a time with
+// tcgen05.ld and emits the two offers of each valid pair (i, j) -- warps w
+// and w + 4 share lanes 32w.. and split the columns; all warps hold rows,
+// the columns run over the short new list.  The targets'
 // pool maxima are read once per node into shared memory (pools do not change
 // during a join chunk).  The wait on the MMAs is bounded: on time-out the CTA
 // reports DEV_TIMEOUT, waits (bounded) once more for its MMAs and frees its
 // tensor memory.
-constexpr int JT_THREADS = 128;
+constexpr int JT_THREADS = 256;  // 8 warps: warps w and w + 4 share TMEM lanes 32w.. (column halves)
 constexpr uint32_t JT_ROWS = 128;  // rows per operand buffer (M of A, the N chunk of B)
 constexpr uint32_t JT_LBO = 128;
 constexpr uint32_t JT_TMEM_COLS = 128;
@@ -615,19 +616,22 @@ __device__ __forceinline__ uint32_t jt_pack(float lo, float hi) {
 }
 
 // rows [r0, r0 + 128) of the node's list as BF16 in the K-major core layout
-// (zeros past tot)
+// (zeros past tot).  Item e is the 16-byte core row at byte offset 16 e of
+// the layout (8-row group e / (8 kc), core matrix (e / 8) % kc, row e % 8):
+// consecutive threads store consecutive 16 bytes (no bank conflicts) and
+// each loads 32 bytes of one row.
 __device__ void jt_stage(uint8_t *dst, const float *__restrict__ base, uint32_t d, const uint32_t *ids, uint32_t tot,
-                         uint32_t r0, uint32_t sbo, int tid) {
+                         uint32_t r0, int tid) {
   const uint32_t kc = d / 8;
   for (uint32_t e = tid; e < JT_ROWS * kc; e += JT_THREADS) {
-    const uint32_t r = e / kc, k = (e % kc) * 8;
+    const uint32_t r = (e / (8 * kc)) * 8 + (e & 7), k = ((e >> 3) % kc) * 8;
     uint4 v = make_uint4(0, 0, 0, 0);
     if (r0 + r < tot) {
       const float4 *src = reinterpret_cast<const float4 *>(base + (size_t)ids[r0 + r] * d + k);
       const float4 x0 = __ldg(src), x1 = __ldg(src + 1);
       v = make_uint4(jt_pack(x0.x, x0.y), jt_pack(x0.z, x0.w), jt_pack(x1.x, x1.y), jt_pack(x1.z, x1.w));
     }
-    *reinterpret_cast<uint4 *>(dst + (r >> 3) * sbo + (k >> 3) * JT_LBO + (r & 7) * 16) = v;
+    reinterpret_cast<uint4 *>(dst)[e] = v;
   }
 }
 
@@ -637,7 +641,7 @@ size_t join_tc_smem(uint32_t d, uint32_t capn, uint32_t capo) {
 
 __global__ void __launch_bounds__(JT_THREADS) k_join_tc(Nnd s, uint32_t n0, Offers of, unsigned long long *pairs,
                                                         int *status) {
-  extern __shared__ __align__(1024) uint8_t smem[];
+  extern __shared__ __align__(16) uint8_t smem[];  // (the no-swizzle layout needs 16-byte alignment)
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmem_base;
   const uint32_t n = n0 + blockIdx.x;
@@ -671,14 +675,14 @@ __global__ void __launch_bounds__(JT_THREADS) k_join_tc(Nnd s, uint32_t n0, Offe
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_base;
-  jt_stage(tA, s.base, d, ids, tot, 0, sbo, tid);
+  jt_stage(tA, s.base, d, ids, tot, 0, tid);
   unsigned long long npairs = 0;
   uint32_t phase = 0;
   bool ok = true;
   const uint32_t acols = (a + 15) & ~15u;  // N: the new rows, rounded up to 16
   for (uint32_t m0 = 0; m0 < tot && ok; m0 += JT_ROWS) {
     const uint8_t *at = m0 == 0 ? tA : tB;
-    if (m0 > 0) jt_stage(tB, s.base, d, ids, tot, m0, sbo, tid);
+    if (m0 > 0) jt_stage(tB, s.base, d, ids, tot, m0, tid);
     asm volatile("fence.proxy.async.shared::cta;");  // generic stores -> tensor core reads
     __syncthreads();
     if (tid == 0) {
@@ -701,14 +705,17 @@ __global__ void __launch_bounds__(JT_THREADS) k_join_tc(Nnd s, uint32_t n0, Offe
     phase ^= 1;
     asm volatile("tcgen05.fence::after_thread_sync;");
     if (!ok) break;
-    if (m0 + (uint32_t)warp * 32 < tot) {
-      const uint32_t gj = m0 + warp * 32 + lane;  // this lane's row of new ++ old
+    // warp w: TMEM lanes 32 (w % 4).. (rows of new ++ old), columns (new
+    // rows) of half w / 4
+    const uint32_t quad = warp & 3, chalf = (uint32_t)(warp >> 2) * 64;
+    if (m0 + quad * 32 < tot) {
+      const uint32_t gj = m0 + quad * 32 + lane;  // this lane's row of new ++ old
       const bool rowok = gj < tot;
       const uint32_t jid = rowok ? ids[gj] : 0u;
       const float nj = rowok ? nrm[gj] : 0.f, mj = rowok ? mx[gj] : __int_as_float(0xff800000);
-      for (uint32_t c0 = 0; c0 < a; c0 += 16) {
+      for (uint32_t c0 = chalf; c0 < a && c0 < chalf + 64; c0 += 16) {
         uint32_t v[16];
-        const uint32_t addr = tmem + ((uint32_t)(warp * 32) << 16) + c0;
+        const uint32_t addr = tmem + ((quad * 32) << 16) + c0;
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
