@@ -225,7 +225,15 @@ def build_index(ctx, base, cfg):
     st0 = ctx.init_random(cfg["S"])
     st1 = ctx.nnd_refine(cfg["S"], cfg["K"], cfg["L"], cfg["ITER"], cfg["R"])
     stages = {"init_random": st0, "nndescent": st1}
-    stages["nsg"] = ctx.nsg_refine(cfg["L_refine"], cfg["R_refine"], cfg["C_refine"])
+    if cfg.get("link") == "vamana":
+        # the RNG/alpha prune as the 1M configuration states it: alpha 1.2,
+        # R 32, in the clean build mode (the reference's Vamana link defects
+        # fixed; compat mode reproduces them bit for bit)
+        ctx.set_build_mode("clean")
+        stages["vamana"] = ctx.vamana_refine(cfg["L_refine"], cfg["R_refine"], cfg["alpha"], 0)
+        ctx.set_build_mode("compat")
+    else:
+        stages["nsg"] = ctx.nsg_refine(cfg["L_refine"], cfg["R_refine"], cfg["C_refine"])
     ctx.load_built_graph()
     torch.cuda.synchronize()
     dt = time.time() - t0
@@ -469,6 +477,8 @@ def run_ours(args):
         cfg["nq"] = args.nq
     if args.n:
         cfg["n"] = args.n
+    if args.link == "vamana":
+        cfg.update(link="vamana", alpha=1.2, L_refine=args.vamana_L)
     dev = torch.device("cuda", local_device())
     torch.cuda.set_device(dev)
     base, query = make_data(cfg)
@@ -568,12 +578,16 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": round(head_qps, 1), "unit": "queries/s", "n_gpus": world(), "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(head_ms, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "bf16 candidates, f32 rerank" if learned else "f32",
+        "vs_baseline": None,
+        "dtype": ("bf16 candidates (f32 accumulate; exact on this integer data, so no f32 rerank)" if learned
+                  else "f32"),
         "data": "synthetic (seeded integer Gaussian mixture)",
         "config": {"workload": f"{cfg['n']}x{cfg['d']} int-mixture({cfg['centers']}), {nq} queries, top-{K}, "
                                f"KGraph NN-Descent S={cfg['S']} K={cfg['K']} L={cfg['L']} ITER={cfg['ITER']} "
-                               f"R={cfg['R']} -> NSG R={cfg['R_refine']} L_refine={cfg['L_refine']} "
-                               f"C_refine={cfg['C_refine']}",
+                               f"R={cfg['R']} -> " + (
+                                   f"Vamana (clean build mode) alpha={cfg['alpha']} R={cfg['R_refine']} "
+                                   f"L_refine={cfg['L_refine']}" if cfg.get("link") == "vamana" else
+                                   f"NSG R={cfg['R_refine']} L_refine={cfg['L_refine']} C_refine={cfg['C_refine']}"),
                    "headline": "learned entry + beam, bf16 candidates" if learned else "plain FP32",
                    "learned": ({k: (round(v, 4) if isinstance(v, float) else v) for k, v in learned.items()}
                                if learned else None),
@@ -1065,6 +1079,9 @@ def main():
     ap.add_argument("--nq", type=int, default=0, help="override the number of queries")
     ap.add_argument("--n", type=int, default=0, help="override the number of base vectors")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned + bf16 leg")
+    ap.add_argument("--link", choices=["nsg", "vamana"], default="nsg",
+                    help="the graph: NSG (RNG prune, the default) or Vamana alpha=1.2 in the clean build mode")
+    ap.add_argument("--vamana-L", type=int, default=64, help="L_refine of the Vamana link")
     ap.add_argument("--workload", default="int128",
                     choices=["int128", "precision96", "batch960", "learned10m", "graphs1m"],
                     help="int128: the 1M x 128 measurement (default); the others print informational lines")

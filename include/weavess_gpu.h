@@ -165,6 +165,18 @@ int wv_efanna_refine(wv_ctx *ctx, uint32_t S, uint32_t K, uint32_t L, uint32_t I
  * call.  Result: the current graph (width R_refine) with its entry point. */
 int wv_vamana_refine(wv_ctx *ctx, uint32_t L_refine, uint32_t R_refine, float alpha, uint32_t entry_L,
                      wv_build_stats *stats);
+/* Build behaviour.  No counterpart in the reference.  WV_BUILD_COMPAT (the
+ * default) reproduces the reference bit for bit, defects included.
+ * WV_BUILD_CLEAN fixes the Vamana link's three: the entry point is the
+ * centroid search with L_refine (entry_L = 0 reads as L_refine; the
+ * reference's entry is node 0, component_refine.cpp:831-833 never sets the
+ * L_refine that component_entry.cpp:32 reads); PruneVAMANA sorts short pools
+ * too (component_prune.cpp:281-285 copies them unsorted); and the overflow
+ * re-prune of InterInsert walks the sorted row closest first, testing each
+ * candidate against its own distance (component_refine.cpp:905-907 walks
+ * farthest first against temp_pool[i], the outer index). */
+typedef enum { WV_BUILD_COMPAT = 0, WV_BUILD_CLEAN = 1 } wv_build_mode;
+int wv_set_build_mode(wv_ctx *ctx, int mode);
 
 /* ComponentRefineNSG::RefineInner (component_refine.cpp:393-541) on the
  * current graph: centroid entry point with L_refine, candidate search, the

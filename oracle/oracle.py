@@ -54,7 +54,7 @@ def lib():
         L.orc_nndescent_pools.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint,
                                           C.c_uint, C.c_uint, C.c_uint, C.c_void_p, u32p, f32p, u8p, u32p, u32p]
         L.orc_vamana.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint, C.c_uint,
-                                 C.c_float, C.c_uint, C.c_void_p, C.c_int, u32p, f32p, u32p, u32p]
+                                 C.c_float, C.c_uint, C.c_void_p, C.c_int, u32p, f32p, u32p, u32p, C.c_int]
         L.orc_nsg.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint, C.c_uint, C.c_uint,
                               C.c_void_p, C.c_int, u32p, f32p, u32p, C.c_uint, u32p, u32p]
         L.orc_ssg.argtypes = [f32p, C.c_uint, C.c_uint, u32p, f32p, u32p, C.c_uint, C.c_uint, C.c_uint, C.c_float,
@@ -229,7 +229,9 @@ def nndescent_pools(base, init: Graph, S, L, iters, R, rnd: Rand):
     return ids, dist, flag, deg, M
 
 
-def vamana(base, g: Graph, L_refine, R_refine, alpha, rnd: Rand, entry_L=0, threads=1) -> Graph:
+def vamana(base, g: Graph, L_refine, R_refine, alpha, rnd: Rand, entry_L=0, threads=1, clean=False) -> Graph:
+    """REFINE_VAMANA; clean=True: this library's clean build mode (the
+    link's defects fixed), not the reference."""
     base = _c(base, np.float32)
     n, d = base.shape
     ids = np.zeros((n, R_refine), np.uint32)
@@ -237,7 +239,8 @@ def vamana(base, g: Graph, L_refine, R_refine, alpha, rnd: Rand, entry_L=0, thre
     deg = np.zeros(n, np.uint32)
     ep = np.zeros(1, np.uint32)
     assert lib().orc_vamana(base, n, d, _c(g.ids, np.uint32), _c(g.dist, np.float32), _c(g.deg, np.uint32),
-                            g.width, L_refine, R_refine, alpha, entry_L, rnd.h, threads, ids, dist, deg, ep) == 0
+                            g.width, L_refine, R_refine, alpha, entry_L, rnd.h, threads, ids, dist, deg, ep,
+                            1 if clean else 0) == 0
     return Graph(ids, dist, deg, int(ep[0]))
 
 

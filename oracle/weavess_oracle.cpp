@@ -554,8 +554,11 @@ void prune_nsg(const Data &D, const FinalGraph &g, unsigned query, unsigned rang
 
 // ComponentPruneVAMANA::PruneInner (component_prune.cpp:245-300)
 void prune_vamana(const Data &D, unsigned query, unsigned range, float alpha, std::vector<SimpleNeighbor> &pool,
-                  SimpleNeighbor *cut_graph) {
+                  SimpleNeighbor *cut_graph, bool clean = false) {
   std::vector<SimpleNeighbor> picked;
+  // clean mode (this library's WV_BUILD_CLEAN, not the reference): a short
+  // pool is sorted as well
+  if (clean && pool.size() <= range) std::sort(pool.begin(), pool.end());
   if (pool.size() > range) {
     std::sort(pool.begin(), pool.end());
     MinHeap skipped;
@@ -590,7 +593,7 @@ void prune_vamana(const Data &D, unsigned query, unsigned range, float alpha, st
 // Vamana re-prune reads temp_pool[i] (the outer index) as the distance to
 // beat, as the reference does at component_refine.cpp:907.
 void inter_insert(const Data &D, unsigned n, unsigned range, bool vamana, float alpha, std::vector<std::mutex> &locks,
-                  SimpleNeighbor *cut_graph) {
+                  SimpleNeighbor *cut_graph, bool clean = false) {
   SimpleNeighbor *src_pool = cut_graph + (size_t)n * range;
   for (size_t i = 0; i < range; i++) {
     if (src_pool[i].distance == -1) break;
@@ -636,9 +639,12 @@ void inter_insert(const Data &D, unsigned n, unsigned range, bool vamana, float 
         }
       } else {
         MinHeap skipped;
-        for (int k = (int)temp_pool.size() - 1; k >= 0; --k) {
+        // clean mode (WV_BUILD_CLEAN): closest first, each candidate against
+        // its own distance -- the rule of PruneVAMANA
+        for (int kk = 0; kk < (int)temp_pool.size(); ++kk) {
+          const int k = clean ? kk : (int)temp_pool.size() - 1 - kk;
           bool skip = false;
-          float cur_dist = temp_pool[i].distance;
+          float cur_dist = clean ? temp_pool[k].distance : temp_pool[i].distance;
           for (size_t j = 0; j < result.size(); j++) {
             float dist = l2(D.row(result[j].id), D.row(temp_pool[k].id), D.d);
             if (alpha * dist < cur_dist) {
@@ -689,7 +695,7 @@ FinalGraph cut_to_final(const std::vector<SimpleNeighbor> &cut, unsigned n, unsi
 
 // Link for both refines (component_refine.cpp:438-472, 835-872)
 FinalGraph link(const Data &D, const FinalGraph &g, unsigned ep, unsigned Lr, unsigned Rr, unsigned Cr, bool vamana,
-                float alpha, GlibcRand &rnd, int threads) {
+                float alpha, GlibcRand &rnd, int threads, bool clean = false) {
   std::vector<SimpleNeighbor> cut((size_t)D.n * Rr);
   std::vector<std::mutex> locks(D.n);
 #pragma omp parallel num_threads(threads)
@@ -701,11 +707,11 @@ FinalGraph link(const Data &D, const FinalGraph &g, unsigned ep, unsigned Lr, un
       pool.clear();
       std::fill(flags.begin(), flags.end(), 0);
       candidate_nsg(D, g, n, ep, Lr, rnd, pool, flags);
-      if (vamana) prune_vamana(D, n, Rr, alpha, pool, cut.data());
+      if (vamana) prune_vamana(D, n, Rr, alpha, pool, cut.data(), clean);
       else prune_nsg(D, g, n, Rr, Cr, pool, cut.data());
     }
 #pragma omp for schedule(dynamic, 100)
-    for (unsigned n = 0; n < D.n; ++n) inter_insert(D, n, Rr, vamana, alpha, locks, cut.data());
+    for (unsigned n = 0; n < D.n; ++n) inter_insert(D, n, Rr, vamana, alpha, locks, cut.data(), clean);
   }
   return cut_to_final(cut, D.n, Rr);
 }
@@ -1643,12 +1649,14 @@ int orc_nndescent_pools(const float *base, unsigned n, unsigned d, const unsigne
 // index's L_refine member (0 unless an NSG refine ran before).  Out width R.
 int orc_vamana(const float *base, unsigned n, unsigned d, const unsigned *in_ids, const float *in_dist,
                const unsigned *in_deg, unsigned in_w, unsigned L_refine, unsigned R_refine, float alpha,
-               unsigned entry_L, void *rnd, int threads, unsigned *ids, float *dist, unsigned *deg, unsigned *ep) {
+               unsigned entry_L, void *rnd, int threads, unsigned *ids, float *dist, unsigned *deg, unsigned *ep,
+               int clean) {
   Data D{base, n, d};
   GlibcRand &r = *(GlibcRand *)rnd;
   FinalGraph g = graph_from_arrays(in_ids, in_dist, in_deg, n, in_w);
-  unsigned e = entry_centroid(D, g, entry_L, r);
-  FinalGraph out = link(D, g, e, L_refine, R_refine, 0, true, alpha, r, threads < 1 ? 1 : threads);
+  // clean mode: the entry search the link intends (L_refine when unset)
+  unsigned e = entry_centroid(D, g, (clean && entry_L == 0) ? L_refine : entry_L, r);
+  FinalGraph out = link(D, g, e, L_refine, R_refine, 0, true, alpha, r, threads < 1 ? 1 : threads, clean != 0);
   *ep = e;
   return graph_to_arrays(out, ids, dist, deg, R_refine);
 }

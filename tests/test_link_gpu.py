@@ -121,6 +121,29 @@ def test_vamana_matches_oracle_20k(ctx, mix20k, alpha, L_refine):
     assert rows_equal(ids, dist, deg, gv.ids, gv.dist, gv.deg) == 0, st
 
 
+@pytest.mark.parametrize("alpha,L_refine", [(1.2, 24), (1.2, 48), (2.0, 32)])
+def test_vamana_clean_mode_matches_oracle_20k(ctx, mix20k, alpha, L_refine):
+    """The clean build mode (the Vamana link's defects fixed: centroid entry
+    search, sorted short pools, closest-first re-prune) against the oracle's
+    clean mode, row for row and entry point; compat stays the default."""
+    base, query, g = mix20k
+    ctx.upload_base(base)
+    ctx.srand(1)
+    ctx.init_random(10)
+    ctx.nnd_refine(10, 24, 40, 6, 50)
+    ro = O.Rand(1)
+    go = O.nndescent(base, O.init_random(base, 10, ro), 10, 24, 40, 6, 50, ro)
+    gv = O.vamana(base, go, L_refine, 32, alpha, ro, clean=True)
+    ctx.set_build_mode("clean")
+    try:
+        st = ctx.vamana_refine(L_refine, 32, alpha, 0)
+    finally:
+        ctx.set_build_mode("compat")
+    ids, dist, deg, ep = ctx.get_graph()
+    assert ep == gv.ep and ep != 0  # the centroid search, not node 0
+    assert rows_equal(ids, dist, deg, gv.ids, gv.dist, gv.deg) == 0, st
+
+
 def test_nsg_matches_oracle_20k(ctx, mix20k):
     base, query, g = mix20k
     ctx.upload_base(base)

@@ -123,6 +123,7 @@ def load(build_if_needed: bool = True):
     L.wv_nnd_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                 C.POINTER(BuildStats)]
     L.wv_vamana_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, C.POINTER(BuildStats)]
+    L.wv_set_build_mode.argtypes = [vp, C.c_int]
     L.wv_efanna_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                    C.POINTER(BuildStats)]
     L.wv_nsg_refine.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(BuildStats)]

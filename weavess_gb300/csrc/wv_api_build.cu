@@ -175,7 +175,12 @@ int wv_vamana_refine(wv_ctx *c, uint32_t L_refine, uint32_t R_refine, float alph
   auto t0 = std::chrono::steady_clock::now();
   const unsigned long long d0 = c->rnd.drawn;
   LinkStats st;
-  int rc = link_gpu(c, LinkParams{L_refine, R_refine, 0, alpha, entry_L, LinkMode::VAMANA}, &st);
+  LinkParams lp{L_refine, R_refine, 0, alpha, entry_L, LinkMode::VAMANA};
+  lp.clean = c->build_clean != 0;
+  // clean mode: the entry point is the centroid search the link intends
+  // (the reference's Vamana refine never sets the L_refine it reads)
+  if (lp.clean && lp.entry_L == 0) lp.entry_L = L_refine;
+  int rc = link_gpu(c, lp, &st);
   if (stats) {
     *stats = wv_build_stats{};
     stats->rand_draws = c->rnd.drawn - d0;
@@ -184,6 +189,13 @@ int wv_vamana_refine(wv_ctx *c, uint32_t L_refine, uint32_t R_refine, float alph
     stats->ms_total = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
   return rc;
+}
+
+int wv_set_build_mode(wv_ctx *c, int mode) {
+  if (!c) return WV_ERR_ARG;
+  WV_CHECK(c, mode == WV_BUILD_COMPAT || mode == WV_BUILD_CLEAN, WV_ERR_ARG, "unknown build mode %d", mode);
+  c->build_clean = mode == WV_BUILD_CLEAN ? 1 : 0;
+  return WV_OK;
 }
 
 int wv_nsg_refine(wv_ctx *c, uint32_t L_refine, uint32_t R_refine, uint32_t C_refine, wv_build_stats *stats) {

@@ -61,6 +61,9 @@ struct wv_ctx {
   // route searches: 0 the exact traversal; E >= 1 the throughput form with
   // E parents expanded per step (wv_set_search_expansion)
   uint32_t parents = 0;
+  // builds: 0 the reference's behaviour (compat); 1 clean -- the Vamana
+  // link's defects fixed (wv_set_build_mode)
+  int build_clean = 0;
   wv::DevBuf qbase, qscale, qnorm;  // qnorm: squared norms of the low-precision rows
 
   // search graph (load_graph_)

@@ -85,6 +85,7 @@ struct PruneArgs {
   const uint32_t *g_ids;  // NSG: the candidate graph (final_graph_)
   const uint32_t *g_deg;
   uint32_t gw;
+  int clean;            // Vamana: a short pool is sorted too (clean mode)
   int *gscr;            // per warp: 2 * vcap + 256 ints
   HeapItem *hscr;       // per warp: vcap items (VAMANA refill)
   uint32_t *out_ids;    // rows of width R, indexed by node
@@ -139,7 +140,7 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
       m = min(m + deg, a.vcap);
       __syncwarp();
     }
-    if (!NSG && m <= a.R) {  // PruneVAMANA keeps a short pool unsorted
+    if (!NSG && m <= a.R && !a.clean) {  // PruneVAMANA keeps a short pool unsorted
       for (uint32_t j = lane; j < m; j += 32) {
         oid[j] = pool[j].i;
         od[j] = pool[j].d;
@@ -153,6 +154,14 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
     }
     warp_std_sort(pool, (int)m, DILess(), WarpSortScratch{scr, scr + a.vcap, scr + 2 * a.vcap,
                                                           scr + 2 * a.vcap + 192}, lane);
+    if (!NSG && m <= a.R) {  // clean mode: the short pool, sorted
+      for (uint32_t j = lane; j < m; j += 32) {
+        oid[j] = pool[j].i;
+        od[j] = pool[j].d;
+      }
+      if (lane == 0) a.out_deg[node] = m;
+      continue;
+    }
     uint32_t np = 0;   // picked
     uint32_t ex = 0;   // next pool index to examine
     uint32_t end = m;  // examination bound
@@ -264,6 +273,7 @@ struct IIArgs {
   uint32_t d, n, R;
   float alpha;
   int vamana;
+  int clean;               // Vamana re-prune closest first, each candidate against its own distance
   int ssg;                 // SSG re-prune: angle test, sentinel after a short result
   float threshold;
   const uint32_t *p_ids;   // pruned rows (width R)
@@ -420,9 +430,13 @@ __device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t &rs, 
   __syncwarp();
   uint32_t nres = 0;
   if (a.vamana) {
-    const float cur = w.tmp[i].d;  // temp_pool[i]: the outer index (refine.cpp:907)
+    // compat: farthest first, every candidate against temp_pool[i].d (the
+    // outer index, refine.cpp:907); clean: closest first, each candidate
+    // against its own distance (the rule of PruneVAMANA)
     uint32_t nskip = 0;
-    for (int k = (int)T - 1; k >= 0; --k) {
+    for (int kk = 0; kk < (int)T; kk++) {
+      const int k = a.clean ? kk : (int)T - 1 - kk;
+      const float cur = a.clean ? w.tmp[k].d : w.tmp[i].d;
       const uint32_t ks = w.tmp[k].slot;
       bool hit = false;
       for (uint32_t j = lane; j < nres; j += 32) hit |= __fmul_rn(a.alpha, w.D[w.tmp[w.res[j]].slot * S + ks]) < cur;
@@ -967,6 +981,7 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
       pa.cnt = cnt;
       pa.R = R;
       pa.alpha = p.alpha;
+      pa.clean = p.clean ? 1 : 0;
       pa.maxc = p.C;
       pa.threshold = threshold;
       pa.g_ids = c->fg_ids.as<uint32_t>();
@@ -1045,6 +1060,7 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
   ia.R = R;
   ia.alpha = p.alpha;
   ia.vamana = vamana;
+  ia.clean = p.clean ? 1 : 0;
   ia.ssg = ssg;
   ia.threshold = threshold;
   ia.p_ids = p_ids;

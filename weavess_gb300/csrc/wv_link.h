@@ -17,6 +17,9 @@ struct LinkParams {
   uint32_t entry_L;  // the index's L_refine member read by the entry search (0: ep_ = 0)
   LinkMode mode;
   float A = 0.f;     // SSG: angle bound in degrees
+  // Vamana, clean mode: short prune pools sorted, the overflow re-prune of
+  // InterInsert closest first against each candidate's own distance
+  bool clean = false;
 };
 
 struct LinkStats {

@@ -185,6 +185,12 @@ class Context:
         self._check(self.L.wv_vamana_refine(self.h, L_refine, R_refine, alpha, entry_L, C.byref(st)))
         return st.as_dict()
 
+    def set_build_mode(self, mode: str = "compat"):
+        """"compat": the reference's behaviour bit for bit (the default);
+        "clean": the Vamana link's defects fixed (entry point, short-pool
+        order, InterInsert re-prune)."""
+        self._check(self.L.wv_set_build_mode(self.h, {"compat": 0, "clean": 1}[mode]))
+
     def nsg_refine(self, L_refine: int, R_refine: int, C_refine: int):
         st = _lib.BuildStats()
         self._check(self.L.wv_nsg_refine(self.h, L_refine, R_refine, C_refine, C.byref(st)))
