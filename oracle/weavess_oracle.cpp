@@ -553,13 +553,46 @@ void prune_nsg(const Data &D, const FinalGraph &g, unsigned query, unsigned rang
 }
 
 // ComponentPruneVAMANA::PruneInner (component_prune.cpp:245-300)
-void prune_vamana(const Data &D, unsigned query, unsigned range, float alpha, std::vector<SimpleNeighbor> &pool,
-                  SimpleNeighbor *cut_graph, bool clean = false) {
+void prune_vamana(const Data &D, const FinalGraph &g, unsigned query, unsigned range, float alpha,
+                  std::vector<SimpleNeighbor> &pool, SimpleNeighbor *cut_graph, bool clean = false) {
   std::vector<SimpleNeighbor> picked;
-  // clean mode (this library's WV_BUILD_CLEAN, not the reference): a short
-  // pool is sorted as well
-  if (clean && pool.size() <= range) std::sort(pool.begin(), pool.end());
-  if (pool.size() > range) {
+  if (clean) {
+    // clean mode (this library's WV_BUILD_CLEAN, not the reference): the
+    // pool is the visited set plus the node's own row (DiskANN's RobustPrune
+    // prunes V u N_out(p)), sorted whatever its size; the node itself and
+    // ids already picked are dropped, not skipped; the refill takes an id
+    // once
+    for (unsigned nn = 0; nn < g[query].size(); nn++) {
+      unsigned id = g[query][nn].id;
+      pool.push_back(SimpleNeighbor(id, l2(D.row(query), D.row(id), D.d)));
+    }
+    std::sort(pool.begin(), pool.end());
+    MinHeap skipped;
+    auto taken = [&](unsigned id) {
+      for (auto &x : picked)
+        if (x.id == id) return true;
+      return false;
+    };
+    for (size_t i = 0; i < pool.size(); i++) {
+      if (pool[i].id == query || taken(pool[i].id)) continue;
+      bool skip = false;
+      float cur_dist = pool[i].distance;
+      for (size_t j = 0; j < picked.size(); j++) {
+        float dist = l2(D.row(picked[j].id), D.row(pool[i].id), D.d);
+        if (alpha * dist < cur_dist) {
+          skip = true;
+          break;
+        }
+      }
+      if (!skip) picked.push_back(pool[i]);
+      else skipped.push(cur_dist, pool[i]);
+      if (picked.size() == range) break;
+    }
+    while (picked.size() < range && skipped.size()) {
+      if (!taken(skipped.top().data.id)) picked.push_back(skipped.top().data);
+      skipped.pop();
+    }
+  } else if (pool.size() > range) {
     std::sort(pool.begin(), pool.end());
     MinHeap skipped;
     for (size_t i = 0; i < pool.size(); i++) {
@@ -707,7 +740,7 @@ FinalGraph link(const Data &D, const FinalGraph &g, unsigned ep, unsigned Lr, un
       pool.clear();
       std::fill(flags.begin(), flags.end(), 0);
       candidate_nsg(D, g, n, ep, Lr, rnd, pool, flags);
-      if (vamana) prune_vamana(D, n, Rr, alpha, pool, cut.data(), clean);
+      if (vamana) prune_vamana(D, g, n, Rr, alpha, pool, cut.data(), clean);
       else prune_nsg(D, g, n, Rr, Cr, pool, cut.data());
     }
 #pragma omp for schedule(dynamic, 100)

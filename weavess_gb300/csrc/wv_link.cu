@@ -124,7 +124,11 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
     uint32_t m = min(a.vcnt[qi], a.vcap);
     uint32_t *oid = a.out_ids + (size_t)node * a.R;
     float *od = a.out_dist + (size_t)node * a.R;
-    if (NSG) {
+    // clean Vamana (this library's clean build mode): the pool is the visited
+    // set plus the node's own row, as DiskANN's RobustPrune prunes V u
+    // N_out(p); the node itself and repeated ids are dropped, not skipped
+    const bool cv = !NSG && a.clean;
+    if (NSG || cv) {
       // the node's own row joins the pool, distances recomputed
       // (component_prune.cpp:26-34); vcap leaves room for it
       const uint32_t deg = min(a.g_deg[node], a.gw);
@@ -154,14 +158,6 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
     }
     warp_std_sort(pool, (int)m, DILess(), WarpSortScratch{scr, scr + a.vcap, scr + 2 * a.vcap,
                                                           scr + 2 * a.vcap + 192}, lane);
-    if (!NSG && m <= a.R) {  // clean mode: the short pool, sorted
-      for (uint32_t j = lane; j < m; j += 32) {
-        oid[j] = pool[j].i;
-        od[j] = pool[j].d;
-      }
-      if (lane == 0) a.out_deg[node] = m;
-      continue;
-    }
     uint32_t np = 0;   // picked
     uint32_t ex = 0;   // next pool index to examine
     uint32_t end = m;  // examination bound
@@ -187,8 +183,13 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
       const uint32_t cnt = min(32u, end - ex);
       DI cand = lane < (int)cnt ? pool[ex + lane] : DI{0.f, 0u};
       // against the rows picked before this batch
-      bool s1 = false;
+      bool s1 = false, dup1 = false;  // dup1 (clean Vamana): the node itself or an id picked before
       if (lane < (int)cnt) {
+        if (cv) {
+          dup1 = cand.i == node;
+          for (uint32_t j = 0; j < np && !dup1; j++) dup1 = pid[j] == cand.i;
+          s1 = dup1;
+        }
         for (uint32_t j = 0; j < np && !s1; j++) {
           if (NSG && pid[j] == cand.i) s1 = true;
           else {
@@ -200,13 +201,16 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
       }
       // which earlier batch members would occlude this one
       uint32_t occl = 0;
+      uint32_t dupo = 0;  // clean Vamana: earlier batch members with the same id
       for (int b = 0; b < (int)cnt; b++) {
         const uint32_t bid = __shfl_sync(FULL, cand.i, b);
         const float bd = __shfl_sync(FULL, cand.d, b);
         if (b < lane && lane < (int)cnt) {
           bool hit;
-          if (NSG && bid == cand.i) hit = true;
-          else {
+          if ((NSG || cv) && bid == cand.i) {
+            hit = true;
+            if (cv) dupo |= 1u << b;
+          } else {
             float dd = l2g(a.base, a.d, bid, cand.i);
             hit = MODE == 2 ? ssg_occludes(cand.d, bd, dd, a.threshold)
                             : (NSG ? (dd < cand.d) : (__fmul_rn(a.alpha, dd) < cand.d));
@@ -220,6 +224,7 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
       for (int b = 0; b < (int)cnt; b++) {
         const bool sb = __shfl_sync(FULL, s1, b);
         const uint32_t ob = __shfl_sync(FULL, occl, b);
+        const bool db = __shfl_sync(FULL, dup1, b) || (__shfl_sync(FULL, dupo, b) & pm);
         const DI cb = DI{__shfl_sync(FULL, cand.d, b), __shfl_sync(FULL, cand.i, b)};
         const bool skip = sb || (ob & pm);
         if (!skip) {
@@ -234,7 +239,7 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
             done = true;
             break;
           }
-        } else if (!NSG) {
+        } else if (!NSG && !db) {
           if (lane == 0) heap[nskip] = HeapItem{cb.d, cb};
           nskip++;
         }
@@ -248,9 +253,13 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
         for (uint32_t k = 1; k <= nskip; k++) stl::push_heap(heap, (int)k, HeapItemLess());
         uint32_t hs = nskip;
         while (np < a.R && hs > 0) {
-          pid[np] = heap[0].data.i;
-          pd[np] = heap[0].data.d;
-          np++;
+          bool again = false;  // clean Vamana: an id skipped twice is taken once
+          for (uint32_t j = 0; cv && j < np && !again; j++) again = pid[j] == heap[0].data.i;
+          if (!again) {
+            pid[np] = heap[0].data.i;
+            pd[np] = heap[0].data.d;
+            np++;
+          }
           stl::pop_heap(heap, (int)hs, HeapItemLess());
           hs--;
         }
@@ -958,7 +967,7 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
                    : run_build_search(c, c->base.as<float>() + (size_t)n0 * c->d, cnt, dseeds,
                                       shared_seeds ? 0 : p.L, p.L, c->fg_ids.as<uint32_t>(),
                                       c->fg_deg.as<uint32_t>(), gw, vis, vcnt, vcap, nullptr, 1,
-                                      vcap - (vamana ? 0 : gw));
+                                      vcap - ((vamana && !p.clean) ? 0 : gw));
       if (rc) return rc;
       int st0 = 0;
       WV_CUDA(c, cudaMemcpyAsync(&st0, c->d_status(), 4, cudaMemcpyDeviceToHost, c->stream));
