@@ -482,6 +482,13 @@ def run_ours(args):
     dev = torch.device("cuda", local_device())
     torch.cuda.set_device(dev)
     base, query = make_data(cfg)
+    if world() > 1:
+        # weak scaling: every rank holds a replica and searches its own slice
+        # of a batch of nq x N queries (weavess_gb300.replicas)
+        from weavess_gb300.replicas import query_slice
+        _, allq = ds.int_mixture(0, cfg["d"], cfg["centers"], seed=cfg["seed"], n_query=cfg["nq"] * world())
+        s0, s1 = query_slice(allq.shape[0], rank(), world())
+        query = allq[s0:s1]
     ctx = Context(local_device())
     # one stream for everything timed: the L2 flush, the events and the
     # context's kernels (the legacy default stream would not order the
