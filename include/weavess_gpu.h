@@ -383,7 +383,9 @@ typedef struct {
   uint32_t hash_words; /* visited-hash area per warp (32-bit words) */
   int wide_hash;       /* 1: 32-bit entries; 0: 16-bit entries where n allows (twice the slots) */
   int blocks;
-  float ms; /* measured search time (tuning) */
+  float ms;        /* measured search time (tuning) */
+  int query_warps; /* throughput form (wv_set_search_expansion > 0): warps per query, 1, 2 or 4 (a divisor of
+                      warps_per_block); 0 reads as 1 */
 } wv_plan_shape;
 #define WV_TUNE_MAX 32
 typedef struct {

@@ -149,3 +149,54 @@ def test_expansion_setting_is_checked(ctx):
     with pytest.raises(WeavessError):
         ctx.set_expansion(5)
     ctx.set_expansion(0)
+
+
+@pytest.mark.parametrize("kind", ["int128_bf16", "unit96_bf16", "int64_fp32"])
+@pytest.mark.parametrize("wpb,qw", [(2, 2), (4, 4), (8, 2)])
+def test_query_warps_do_not_change_results(ctx, kind, wpb, qw):
+    """2 or 4 warps sharing each query's distance passes (seeds, fresh rows,
+    the FP32 rerank) return the ids, distances and counters of one warp per
+    query, mixed beams included."""
+    import torch
+    if kind == "int128_bf16":
+        base, query, ids, deg = graph_for(ctx, 128)
+        storage = "bf16"
+    elif kind == "int64_fp32":
+        base, query, ids, deg = graph_for(ctx, 64)
+        storage = "fp32"
+    else:
+        base, query = ds.unit_mixture(6000, 96, 24, seed=8, n_query=150)
+        ctx.upload_base(base)
+        ctx.set_precision("fp32")
+        ctx.srand(1)
+        ctx.init_random(12)
+        ctx.nnd_refine(12, 24, 40, 5, 40)
+        ctx.load_built_graph()
+        storage = "bf16"  # real-valued: the final pool is re-ranked in FP32
+    ctx.set_precision(storage)
+    ctx.set_expansion(2)
+    try:
+        nq = query.shape[0]
+        rng = np.random.default_rng(2)
+        L = rng.integers(10, 200, size=nq).astype(np.int32)
+        dq = torch.from_numpy(query).cuda()
+        dL = torch.from_numpy(L).cuda()
+        dout = torch.zeros((nq, 10), dtype=torch.int32, device="cuda")
+        ddist = torch.zeros((nq, 10), dtype=torch.float32, device="cuda")
+        plan = ctx.plan(nq, 10, dq.data_ptr(), dout.data_ptr(), L_max=200, mode="rand", d_L=dL.data_ptr(),
+                        d_out_dist=ddist.data_ptr())
+        res = []
+        for shape in ((wpb, 1), (wpb, qw)):
+            plan.set_shape(shape[0], 0, False, shape[1])
+            assert plan.shape()["query_warps"] == shape[1]
+            ctx.srand(33)
+            plan.run(nq)
+            counters = plan.wait()
+            res.append((dout.cpu().numpy().copy(), ddist.cpu().numpy().copy(), counters))
+        plan.close()
+        assert np.array_equal(res[0][0], res[1][0])
+        assert np.array_equal(res[0][1].view(np.uint32), res[1][1].view(np.uint32))
+        assert res[0][2] == res[1][2]
+    finally:
+        ctx.set_expansion(0)
+        ctx.set_precision("fp32")

@@ -44,7 +44,7 @@ class PlanParams(C.Structure):
 
 class PlanShape(C.Structure):
     _fields_ = [("warps_per_block", C.c_int), ("hash_words", C.c_uint32), ("wide_hash", C.c_int), ("blocks", C.c_int),
-                ("ms", C.c_float)]
+                ("ms", C.c_float), ("query_warps", C.c_int)]
 
 
 class TuneReport(C.Structure):

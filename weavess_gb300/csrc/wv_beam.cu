@@ -30,8 +30,9 @@
 //  * the seeds are marked visited when they enter the pool (a seed met again
 //    as a neighbour is not re-scored), duplicate seeds keep one entry.
 //
-// Other row layouts (fp8, other d) use the warp-cooperative row distances of
-// the exact form.  The final pool of low-precision candidates is re-ranked in
+// Other row layouts (fp8, other d) use warp-cooperative row distances (a
+// warp per row, coalesced; FP32 rows of real-valued data in an order that is
+// not the reference's).  The final pool of low-precision candidates is re-ranked in
 // FP32 as in the exact form, except bf16 candidates of integer data at
 // d <= 128, which are exact already.  DistCount counts every distance taken (seeds
 // included), HopCount every expanded node.
@@ -64,6 +65,7 @@ enum BeamDist : int {
 __host__ __device__ inline uint32_t qfrag_words(uint32_t d) { return (d % 32 == 0 && d <= 256) ? 2 * (d / 32) * 16 : 0; }
 
 struct BeamSmem {
+  uint32_t *task;  // a distance pass shared by the query's warps: kind, count, |q|^2 bits, flags
   uint32_t *hash;  // visited set; scratch of the seed sort and the rerank
   float *qv;       // the query (FP32)
   uint32_t *qf;    // query fragments
@@ -75,8 +77,9 @@ struct BeamSmem {
   uint32_t *si;    //   (before that: the step's fresh ids)
 };
 
+// shared memory of one query (one group of query_warps warps)
 __host__ __device__ inline size_t beam_warp_bytes(uint32_t d, uint32_t Lmax, uint32_t cap, uint32_t hcap) {
-  size_t b = align16((size_t)hash_slots(Lmax, hcap) * 4);
+  size_t b = 16 + align16((size_t)hash_slots(Lmax, hcap) * 4);
   b += align16(((d + 3) & ~3u) * 4);
   b += align16((size_t)qfrag_words(d) * 4);
   b += 2 * align16((size_t)pool_cap(Lmax) * 4);
@@ -86,6 +89,8 @@ __host__ __device__ inline size_t beam_warp_bytes(uint32_t d, uint32_t Lmax, uin
 
 __device__ inline BeamSmem beam_carve(uint8_t *p, uint32_t d, uint32_t Lmax, uint32_t cap, uint32_t hcap) {
   BeamSmem s;
+  s.task = (uint32_t *)p;
+  p += 16;
   s.hash = (uint32_t *)p;
   p += align16((size_t)hash_slots(Lmax, hcap) * 4);
   s.qv = (float *)p;
@@ -218,19 +223,20 @@ __device__ __forceinline__ float beam_dist(const SearchArgs &a, bool ints, bool 
   if (a.storage != 0)
     return lowp_rows_dist(LowpRows{a.qbase, a.qscale, (ints && a.d > 128) ? nullptr : a.qnorm, a.storage, a.d}, my,
                           cnt, qv, qn, lane);
-  return ints ? batch_dist<true>(a.base, a.d, my, cnt, qv, lane, qn, a.d <= 128 ? a.xnorm : nullptr)
-              : batch_dist<false>(a.base, a.d, my, cnt, qv, lane);
+  // FP32 rows: a warp per row with coalesced loads (the norm form on integer
+  // data up to d = 128, else the difference form; the summation order is not
+  // the reference's, which the throughput form does not promise)
+  return batch_dist<true>(a.base, a.d, my, cnt, qv, lane, qn, (ints && a.d <= 128) ? a.xnorm : nullptr);
 }
 
-// stable bitonic sort of the L seeds -- (dist, id) pairs in drawn order over
-// the pool region -- into (pd, pi | FLAG); the hash area is the scratch
+// stable bitonic sort of the L seeds -- distances pd[i] of ids pi[i] in
+// drawn order -- into (pd, pi | FLAG); the hash area is the scratch
 __device__ void beam_sort_seeds(const BeamSmem &s, int L, int lane) {
   const int P = (int)pow2_at_least((uint32_t)L);
-  const DI *dv = reinterpret_cast<const DI *>(s.pd);
   float *kd = reinterpret_cast<float *>(s.hash);
   uint32_t *kx = s.hash + P;
   for (int i = lane; i < P; i += 32) {
-    kd[i] = i < L ? dv[i].d : __int_as_float(0x7f800000);
+    kd[i] = i < L ? s.pd[i] : __int_as_float(0x7f800000);
     kx[i] = i;
   }
   __syncwarp();
@@ -254,13 +260,85 @@ __device__ void beam_sort_seeds(const BeamSmem &s, int L, int lane) {
       __syncwarp();
     }
   }
-  for (int i = lane; i < L; i += 32) kx[i] = dv[kx[i]].i;
+  for (int i = lane; i < L; i += 32) kx[i] = s.pi[kx[i]];
   __syncwarp();
   for (int i = lane; i < L; i += 32) {
     s.pd[i] = kd[i];
     s.pi[i] = kx[i] | FLAG;
   }
   __syncwarp();
+}
+
+// ---- the warps of one query (query_warps > 1): a leader warp runs the
+// search; at each distance pass it posts the task in shared memory and the
+// group's named barrier (id 1 + group) releases the member warps, which take
+// 32-row chunks m, m + QW, ... of the pass; a second barrier joins them.
+// Kind 0 ends the members' loop (the leader has no more queries).
+enum BeamTask : uint32_t { BT_EXIT = 0, BT_FRESH = 1, BT_SEEDS = 2, BT_RERANK = 3 };
+
+__device__ __forceinline__ void group_bar(int grp, int qw) {
+  asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "r"(qw * 32) : "memory");
+}
+
+// this warp's chunks of a distance pass
+template <int DK>
+__device__ void beam_share(const SearchArgs &a, const BeamSmem &s, uint32_t kind, int n, bool ints, bool lo,
+                           float qn, int mem, int qw, int lane) {
+  for (int c = mem * 32; c < n; c += qw * 32) {
+    const int cnt = min(32, n - c);
+    if (kind == BT_RERANK) {
+      const int R = n;
+      float *xd = reinterpret_cast<float *>(s.hash);
+      uint32_t *xi = s.hash + R;
+      const uint32_t id = lane < cnt ? (s.pi[c + lane] & ID_MASK) : 0u;
+      const float ex = ints ? batch_dist<true>(a.base, a.d, id, cnt, s.qv, lane, qn, a.d <= 128 ? a.xnorm : nullptr)
+                            : batch_dist<false>(a.base, a.d, id, cnt, s.qv, lane);
+      if (lane < cnt) {
+        xd[c + lane] = ex;
+        xi[c + lane] = id;
+      }
+    } else {
+      const uint32_t *ids = kind == BT_FRESH ? s.si : s.pi;
+      float *out = kind == BT_FRESH ? s.sd : s.pd;
+      const uint32_t my = lane < cnt ? ids[c + lane] : 0u;
+      const float dist = beam_dist<DK>(a, ints, lo, s.qf, my, cnt, s.qv, qn, lane);
+      if (lane < cnt) out[c + lane] = dist;
+    }
+  }
+}
+
+// the leader's side of a distance pass over n items
+template <int DK>
+__device__ void beam_pass(const SearchArgs &a, const BeamSmem &s, uint32_t kind, int n, bool ints, bool lo, float qn,
+                          int grp, int qw, int lane) {
+  __syncwarp();
+  if (qw > 1) {
+    if (lane == 0) {
+      s.task[0] = kind;
+      s.task[1] = (uint32_t)n;
+      s.task[2] = __float_as_uint(qn);
+      s.task[3] = (ints ? 1u : 0u) | (lo ? 2u : 0u);
+    }
+    group_bar(grp, qw);
+  }
+  beam_share<DK>(a, s, kind, n, ints, lo, qn, 0, qw, lane);
+  if (qw > 1) group_bar(grp, qw);
+  __syncwarp();
+}
+
+// a member warp's loop (until the leader posts BT_EXIT)
+template <int DK>
+__device__ void beam_member(const SearchArgs &a, const BeamSmem &s, int grp, int mem, int qw, int lane) {
+  while (true) {
+    group_bar(grp, qw);
+    const uint32_t kind = s.task[0];
+    if (kind == BT_EXIT) return;
+    const int n = (int)s.task[1];
+    const float qn = __uint_as_float(s.task[2]);
+    const uint32_t fl = s.task[3];
+    beam_share<DK>(a, s, kind, n, (fl & 1u) != 0, (fl & 2u) != 0, qn, mem, qw, lane);
+    group_bar(grp, qw);
+  }
 }
 
 // the ncand accepted candidates (cd, ci; visit order) sorted stably by
@@ -327,9 +405,16 @@ __global__ void __maxnreg__(128) k_beam(SearchArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int W = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // query groups of QW warps (the launch keeps W a multiple of QW)
+  const int QW = a.query_warps > 1 ? a.query_warps : 1;
+  const int grp = warp / QW, mem = warp % QW;
   const size_t wbytes = beam_warp_bytes(a.d, a.Lmax, a.cap, a.hcap);
-  const BeamSmem s = beam_carve(smem + warp * wbytes, a.d, a.Lmax, a.cap, a.hcap);
-  const uint32_t slot = blockIdx.x * W + warp;
+  const BeamSmem s = beam_carve(smem + grp * wbytes, a.d, a.Lmax, a.cap, a.hcap);
+  if (mem != 0) {
+    beam_member<DK>(a, s, grp, mem, QW, lane);
+    return;
+  }
+  const uint32_t slot = blockIdx.x * (W / QW) + grp;
   const uint32_t hs = hash_slots(a.Lmax, a.hcap);
   const uint32_t nq = a.nq_dev ? *a.nq_dev : a.nq;
   const int E = (int)min(max(a.parents, 1u), BEAM_MAX_PARENTS);
@@ -375,19 +460,16 @@ __global__ void __maxnreg__(128) k_beam(SearchArgs a) {
     // ---- seeds: distances in drawn order, sorted, then entered into the
     // visited set in pool order (a repeated seed keeps its first entry)
     const uint32_t *seeds = a.seeds + (size_t)q * a.seed_stride;
-    DI *drawn = reinterpret_cast<DI *>(s.pd);
-    for (int b = 0; b < L; b += 32) {
-      const int cnt = min(32, L - b);
-      uint32_t id = lane < cnt ? seeds[b + lane] : 0u;
-      if (lane < cnt && id >= a.n) {
+    for (int i = lane; i < L; i += 32) {
+      uint32_t id = seeds[i];
+      if (id >= a.n) {
         set_err(a.status, DEV_BAD_ID);
         id = 0;
       }
-      const float dist = beam_dist<DK>(a, ints, lo, s.qf, id, cnt, s.qv, qn, lane);
-      if (lane < cnt) drawn[b + lane] = DI{dist, id};
+      pi[i] = id;
     }
+    beam_pass<DK>(a, s, BT_SEEDS, L, ints, lo, qn, grp, QW, lane);  // pd[i]: distance of pi[i]
     dcount += L;
-    __syncwarp();
     beam_sort_seeds(s, L, lane);
     vis.clear(lane);
     int m = 0;  // pool entries kept
@@ -504,12 +586,14 @@ __global__ void __maxnreg__(128) k_beam(SearchArgs a) {
         }
       }
       __syncwarp();
-      // distances; the ones closer than the pool's last entry are accepted
+      // distances (into sd); the ones closer than the pool's last entry are
+      // accepted
+      if (nfresh > 0) beam_pass<DK>(a, s, BT_FRESH, (int)nfresh, ints, lo, qn, grp, QW, lane);
       int ncand = 0;
       for (uint32_t b = 0; b < nfresh; b += 32) {
         const int cnt = (int)min(32u, nfresh - b);
         const uint32_t my = lane < cnt ? s.si[b + lane] : 0u;
-        const float dist = beam_dist<DK>(a, ints, lo, s.qf, my, cnt, s.qv, qn, lane);
+        const float dist = lane < cnt ? s.sd[b + lane] : 0.f;
         const bool acc = lane < cnt && dist < thr;
         const unsigned am = __ballot_sync(FULL, acc);
         if (acc) {
@@ -566,18 +650,8 @@ __global__ void __maxnreg__(128) k_beam(SearchArgs a) {
       const int R = min((int)a.rerank, lower_bound_of(pd, L, __int_as_float(0x7f800000)));
       float *xd = reinterpret_cast<float *>(s.hash);
       uint32_t *xi = s.hash + R;
-      for (int b = 0; b < R; b += 32) {
-        const int cnt = min(32, R - b);
-        const uint32_t id = lane < cnt ? (pi[b + lane] & ID_MASK) : 0u;
-        const float ex = ints ? batch_dist<true>(a.base, a.d, id, cnt, s.qv, lane, qn, a.d <= 128 ? a.xnorm : nullptr)
-                              : batch_dist<false>(a.base, a.d, id, cnt, s.qv, lane);
-        if (lane < cnt) {
-          xd[b + lane] = ex;
-          xi[b + lane] = id;
-        }
-      }
+      beam_pass<DK>(a, s, BT_RERANK, R, ints, lo, qn, grp, QW, lane);  // xd, xi
       dcount += R;
-      __syncwarp();
       for (int c = lane; c < R; c += 32) {
         const float dc = xd[c];
         int r = 0;
@@ -597,6 +671,12 @@ __global__ void __maxnreg__(128) k_beam(SearchArgs a) {
       }
     __syncwarp();
     vis.clear(lane);
+  }
+  // the member warps leave with the leader
+  if (QW > 1) {
+    __syncwarp();
+    if (lane == 0) s.task[0] = BT_EXIT;
+    group_bar(grp, QW);
   }
   if (lane == 0 && a.counters) {
     atomicAdd(a.counters + 0, dcount);
@@ -627,9 +707,14 @@ uint32_t beam_cap(uint32_t gw, uint32_t parents) {
   return e * gw + 32;
 }
 
+bool beam_shape_ok(const SearchShape &sh) {
+  return (sh.wpb == 1 || sh.wpb == 2 || sh.wpb == 4 || sh.wpb == 8) && (sh.qw == 1 || sh.qw == 2 || sh.qw == 4) &&
+         sh.wpb % sh.qw == 0;
+}
+
 int beam_grid(uint32_t d, uint32_t Lmax, uint32_t gw, uint32_t parents, int device, SearchShape sh) {
-  if (!(sh.wpb == 1 || sh.wpb == 2 || sh.wpb == 4 || sh.wpb == 8)) return 0;
-  const size_t smem = (size_t)sh.wpb * beam_warp_bytes(d, Lmax, beam_cap(gw, parents), sh.hcap);
+  if (!beam_shape_ok(sh)) return 0;
+  const size_t smem = (size_t)(sh.wpb / sh.qw) * beam_warp_bytes(d, Lmax, beam_cap(gw, parents), sh.hcap);
   if (smem > 227 * 1024) return 0;
   int per_sm = 1 << 30;
   // every distance path a launch may pick must fit
@@ -647,12 +732,13 @@ int beam_grid(uint32_t d, uint32_t Lmax, uint32_t gw, uint32_t parents, int devi
 }
 
 cudaError_t launch_beam(const SearchArgs &a, SearchShape sh, int blocks, cudaStream_t stream) {
-  if (!(sh.wpb == 1 || sh.wpb == 2 || sh.wpb == 4 || sh.wpb == 8)) return cudaErrorInvalidValue;
+  if (!beam_shape_ok(sh)) return cudaErrorInvalidValue;
   SearchArgs b = a;
   b.cap = beam_cap(a.gw, a.parents);
   b.hcap = sh.hcap;
   b.wide_hash = sh.wide ? 1 : 0;
-  const size_t smem = (size_t)sh.wpb * beam_warp_bytes(b.d, b.Lmax, b.cap, b.hcap);
+  b.query_warps = sh.qw;
+  const size_t smem = (size_t)(sh.wpb / sh.qw) * beam_warp_bytes(b.d, b.Lmax, b.cap, b.hcap);
   switch (beam_kind(b)) {
     case BD_BF16_128: k_beam<BD_BF16_128><<<blocks, sh.wpb * 32, smem, stream>>>(b); break;
     case BD_BF16_96: k_beam<BD_BF16_96><<<blocks, sh.wpb * 32, smem, stream>>>(b); break;

@@ -347,10 +347,20 @@ int wv_plan_tune(wv_plan *p, uint32_t nq, wv_tune_report *rep) {
   for (int w : {1, 2, 4, 8})
     for (uint32_t h : areas) cand.push_back(SearchShape{w, h});
   // the throughput form also tries 32-bit visited-hash entries (half the
-  // slots in the same bytes, but a native compare-and-swap per probe)
-  if (c->parents > 0)
+  // slots in the same bytes, but a native compare-and-swap per probe) and
+  // 2 or 4 warps per query (the query's shared memory serving more rows in
+  // flight)
+  if (c->parents > 0) {
     for (int w : {1, 2, 4, 8})
       for (uint32_t h : {0u, 2 * h0}) cand.push_back(SearchShape{w, h, true});
+    for (int w : {2, 4, 8})
+      for (int qw : {2, 4})
+        if (w % qw == 0) {
+          SearchShape sh{w, 0u};
+          sh.qw = qw;
+          cand.push_back(sh);
+        }
+  }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   WV_CUDA(c, cudaEventCreate(&e0));
   WV_CUDA(c, cudaEventCreate(&e1));
@@ -371,7 +381,7 @@ int wv_plan_tune(wv_plan *p, uint32_t nq, wv_tune_report *rep) {
       break;
     }
     if (r.n < WV_TUNE_MAX) {
-      r.tried[r.n] = wv_plan_shape{sh.wpb, search_hash_slots(p->Lcap, sh.hcap), sh.wide ? 1 : 0, blocks, ms};
+      r.tried[r.n] = wv_plan_shape{sh.wpb, search_hash_slots(p->Lcap, sh.hcap), sh.wide ? 1 : 0, blocks, ms, sh.qw};
       if (ms < best) {
         best = ms;
         chosen = sh;
@@ -406,7 +416,7 @@ int wv_plan_search_ms(wv_plan *p, float *ms) {
 int wv_plan_shape_of(wv_plan *p, wv_plan_shape *out) {
   if (!p || !out) return WV_ERR_ARG;
   *out = wv_plan_shape{p->shape.wpb, search_hash_slots(p->Lcap, p->shape.hcap), p->shape.wide ? 1 : 0, p->blocks,
-                       0.f};
+                       0.f, p->shape.qw};
   return WV_OK;
 }
 
@@ -420,6 +430,10 @@ int wv_plan_set_shape(wv_plan *p, const wv_plan_shape *sh) {
            WV_ERR_ARG, "warps_per_block must be 1, 2, 4 or 8");
   WV_CHECK(c, sh->hash_words == 0 || (sh->hash_words & (sh->hash_words - 1)) == 0, WV_ERR_ARG,
            "hash_words must be 0 or a power of two");
+  WV_CHECK(c, sh->query_warps <= 1 || (c->parents > 0 && (sh->query_warps == 2 || sh->query_warps == 4) &&
+                                       sh->warps_per_block % sh->query_warps == 0),
+           WV_ERR_ARG, "query_warps %d: 1, or 2 / 4 dividing warps_per_block with the throughput form",
+           sh->query_warps);
   WV_CHECK(c, sh->hash_words == 0 || sh->hash_words >= search_hash_min(p->Lcap, c->n), WV_ERR_ARG,
            "hash_words=%u below the least area %u for L=%u, n=%u", sh->hash_words, search_hash_min(p->Lcap, c->n),
            p->Lcap, c->n);
@@ -427,6 +441,7 @@ int wv_plan_set_shape(wv_plan *p, const wv_plan_shape *sh) {
   if (rc) return rc;
   const SearchShape old = p->shape;
   p->shape = SearchShape{sh->warps_per_block, sh->hash_words, sh->wide_hash != 0};
+  p->shape.qw = sh->query_warps > 0 ? sh->query_warps : 1;
   rc = capture(p);
   if (rc) {
     const std::string msg = c->err;

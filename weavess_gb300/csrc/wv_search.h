@@ -65,6 +65,9 @@ struct SearchArgs {
   // E >= 1: the throughput form (k_beam, wv_beam.cu), E pool entries
   // expanded per step, tensor-core row distances where the layout allows
   uint32_t parents;
+  // the throughput form: warps per query (1, 2 or 4; set by launch_beam
+  // from the shape) -- the others join the leader's distance passes
+  int query_warps;
 };
 
 constexpr uint32_t SEARCH_MAX_WIDTH = 256;  // graph row width the kernel accepts
@@ -80,6 +83,10 @@ struct SearchShape {
   int wpb = 4;
   uint32_t hcap = 0;
   bool wide = false;  // 32-bit visited-hash entries even where 16-bit ones would do
+  // the throughput form only: warps per query (1, 2 or 4; wpb a multiple):
+  // the leader warp runs the search, the others take shares of its
+  // distance passes (more rows in flight per query's shared memory)
+  int qw = 1;
 };
 
 // bytes of dynamic shared memory per block and warps per block

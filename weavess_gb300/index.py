@@ -395,7 +395,7 @@ class Plan:
         r = _lib.TuneReport()
         self.ctx._check(self.L.wv_plan_tune(self.h, nq, C.byref(r)))
         tried = [{"warps_per_block": t.warps_per_block, "hash_words": t.hash_words, "wide_hash": t.wide_hash,
-                  "blocks": t.blocks, "ms": round(t.ms, 4)} for t in r.tried[:r.n]]
+                  "blocks": t.blocks, "ms": round(t.ms, 4), "query_warps": t.query_warps} for t in r.tried[:r.n]]
         return {"tried": tried, "chosen": tried[r.chosen] if r.chosen >= 0 else None}
 
     def search_ms(self) -> float:
@@ -408,10 +408,10 @@ class Plan:
         sh = _lib.PlanShape()
         self.ctx._check(self.L.wv_plan_shape_of(self.h, C.byref(sh)))
         return {"warps_per_block": sh.warps_per_block, "hash_words": sh.hash_words, "wide_hash": sh.wide_hash,
-                "blocks": sh.blocks}
+                "blocks": sh.blocks, "query_warps": sh.query_warps}
 
-    def set_shape(self, warps_per_block=4, hash_words=0, wide_hash=False):
-        sh = _lib.PlanShape(warps_per_block, hash_words, 1 if wide_hash else 0, 0, 0.0)
+    def set_shape(self, warps_per_block=4, hash_words=0, wide_hash=False, query_warps=1):
+        sh = _lib.PlanShape(warps_per_block, hash_words, 1 if wide_hash else 0, 0, 0.0, query_warps)
         self.ctx._check(self.L.wv_plan_set_shape(self.h, C.byref(sh)))
 
     def close(self):
