@@ -62,28 +62,6 @@ __device__ __forceinline__ float l2g(const float *__restrict__ base, uint32_t d,
   return acc;
 }
 
-// the same distance on integer data in [0, 255] with d <= 128 (xnorm: the
-// rows' squared norms): |x|^2 + |y|^2 - 2 x.y, every partial sum an integer
-// below 2^24, so the value equals the ordered sum; the dot product runs in
-// four independent chains so that its loads are not queued behind ordered
-// additions
-__device__ __forceinline__ float l2n(const float *__restrict__ base, const float *__restrict__ xnorm, uint32_t d,
-                                     uint32_t a, uint32_t b) {
-  const float4 *x = reinterpret_cast<const float4 *>(base + (size_t)a * d);
-  const float4 *y = reinterpret_cast<const float4 *>(base + (size_t)b * d);
-  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-  const uint32_t d4 = d >> 2;
-#pragma unroll 8
-  for (uint32_t g = 0; g < d4; g++) {
-    const float4 u = __ldg(x + g), v = __ldg(y + g);
-    s0 = fmaf(u.x, v.x, s0);
-    s1 = fmaf(u.y, v.y, s1);
-    s2 = fmaf(u.z, v.z, s2);
-    s3 = fmaf(u.w, v.w, s3);
-  }
-  return (__ldg(xnorm + a) + __ldg(xnorm + b)) - 2.f * ((s0 + s1) + (s2 + s3));
-}
-
 struct HeapItem {  // Index::MinHeap<float, SimpleNeighbor>::Item
   float key;
   DI data;
@@ -108,7 +86,6 @@ struct PruneArgs {
   const uint32_t *g_deg;
   uint32_t gw;
   int clean;            // Vamana: a short pool is sorted too (clean mode)
-  const float *xnorm;   // integer data, d <= 128: row norms for l2n (else null: l2g)
   int *gscr;            // per warp: 2 * vcap + 256 ints
   HeapItem *hscr;       // per warp: vcap items (VAMANA refill)
   uint32_t *out_ids;    // rows of width R, indexed by node
@@ -161,7 +138,7 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
           set_err(a.status, DEV_BAD_ID);
           id = 0;
         }
-        if (m + j < a.vcap) pool[m + j] = DI{a.xnorm ? l2n(a.base, a.xnorm, a.d, node, id) : l2g(a.base, a.d, node, id), id};
+        if (m + j < a.vcap) pool[m + j] = DI{l2g(a.base, a.d, node, id), id};
       }
       if (m + deg > a.vcap) set_err(a.status, DEV_OVERFLOW);
       m = min(m + deg, a.vcap);
@@ -216,7 +193,7 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
         for (uint32_t j = 0; j < np && !s1; j++) {
           if (NSG && pid[j] == cand.i) s1 = true;
           else {
-            float dd = a.xnorm ? l2n(a.base, a.xnorm, a.d, pid[j], cand.i) : l2g(a.base, a.d, pid[j], cand.i);
+            float dd = l2g(a.base, a.d, pid[j], cand.i);
             s1 = MODE == 2 ? ssg_occludes(cand.d, pd[j], dd, a.threshold)
                            : (NSG ? (dd < cand.d) : (__fmul_rn(a.alpha, dd) < cand.d));
           }
@@ -234,7 +211,7 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
             hit = true;
             if (cv) dupo |= 1u << b;
           } else {
-            float dd = a.xnorm ? l2n(a.base, a.xnorm, a.d, bid, cand.i) : l2g(a.base, a.d, bid, cand.i);
+            float dd = l2g(a.base, a.d, bid, cand.i);
             hit = MODE == 2 ? ssg_occludes(cand.d, bd, dd, a.threshold)
                             : (NSG ? (dd < cand.d) : (__fmul_rn(a.alpha, dd) < cand.d));
           }
@@ -1004,7 +981,6 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
       if (rc) return rc;
       PruneArgs pa{};
       pa.base = c->base.as<float>();
-      pa.xnorm = (c->base_int && c->d <= 128) ? c->xnorm.as<float>() : nullptr;
       pa.d = c->d;
       pa.n = n;
       pa.vis = vis;
