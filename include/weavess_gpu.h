@@ -384,8 +384,8 @@ typedef struct {
   int wide_hash;       /* 1: 32-bit entries; 0: 16-bit entries where n allows (twice the slots) */
   int blocks;
   float ms;        /* measured search time (tuning) */
-  int query_warps; /* throughput form (wv_set_search_expansion > 0): warps per query, 1, 2 or 4 (a divisor of
-                      warps_per_block); 0 reads as 1 */
+  int query_warps; /* throughput form (wv_set_search_expansion > 0): warps per query, 1, or 2 / 4 equal to
+                      warps_per_block (one query per block); 0 reads as 1 */
 } wv_plan_shape;
 #define WV_TUNE_MAX 32
 typedef struct {

@@ -269,15 +269,18 @@ __device__ void beam_sort_seeds(const BeamSmem &s, int L, int lane) {
   __syncwarp();
 }
 
-// ---- the warps of one query (query_warps > 1): a leader warp runs the
-// search; at each distance pass it posts the task in shared memory and the
-// group's named barrier (id 1 + group) releases the member warps, which take
+// ---- the warps of one query (query_warps > 1, one query group per block):
+// a leader warp runs the search; at each distance pass it posts the task in
+// shared memory and named barrier 1 releases the member warps, which take
 // 32-row chunks m, m + QW, ... of the pass; a second barrier joins them.
-// Kind 0 ends the members' loop (the leader has no more queries).
+// Kind 0 ends the members' loop (the leader has no more queries).  (A
+// constant barrier id keeps the kernel at two barriers per block; an id per
+// group made ptxas reserve all sixteen, which cut the resident blocks.)
 enum BeamTask : uint32_t { BT_EXIT = 0, BT_FRESH = 1, BT_SEEDS = 2, BT_RERANK = 3 };
 
 __device__ __forceinline__ void group_bar(int grp, int qw) {
-  asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "r"(qw * 32) : "memory");
+  (void)grp;  // (one query group per block when qw > 1)
+  asm volatile("bar.sync 1, %0;" ::"r"(qw * 32) : "memory");
 }
 
 // this warp's chunks of a distance pass
@@ -708,8 +711,9 @@ uint32_t beam_cap(uint32_t gw, uint32_t parents) {
 }
 
 bool beam_shape_ok(const SearchShape &sh) {
-  return (sh.wpb == 1 || sh.wpb == 2 || sh.wpb == 4 || sh.wpb == 8) && (sh.qw == 1 || sh.qw == 2 || sh.qw == 4) &&
-         sh.wpb % sh.qw == 0;
+  // several warps per query: one query group per block
+  return (sh.wpb == 1 || sh.wpb == 2 || sh.wpb == 4 || sh.wpb == 8) &&
+         (sh.qw == 1 || ((sh.qw == 2 || sh.qw == 4) && sh.wpb == sh.qw));
 }
 
 int beam_grid(uint32_t d, uint32_t Lmax, uint32_t gw, uint32_t parents, int device, SearchShape sh) {

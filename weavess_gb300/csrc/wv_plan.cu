@@ -353,13 +353,14 @@ int wv_plan_tune(wv_plan *p, uint32_t nq, wv_tune_report *rep) {
   if (c->parents > 0) {
     for (int w : {1, 2, 4, 8})
       for (uint32_t h : {0u, 2 * h0}) cand.push_back(SearchShape{w, h, true});
-    for (int w : {2, 4, 8})
-      for (int qw : {2, 4})
-        if (w % qw == 0) {
-          SearchShape sh{w, 0u};
-          sh.qw = qw;
-          cand.push_back(sh);
-        }
+    for (int qw : {2, 4}) {  // one query per block
+      SearchShape sh{qw, 0u};
+      sh.qw = qw;
+      cand.push_back(sh);
+      SearchShape sh2{qw, 2 * h0};
+      sh2.qw = qw;
+      cand.push_back(sh2);
+    }
   }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   WV_CUDA(c, cudaEventCreate(&e0));
@@ -431,8 +432,8 @@ int wv_plan_set_shape(wv_plan *p, const wv_plan_shape *sh) {
   WV_CHECK(c, sh->hash_words == 0 || (sh->hash_words & (sh->hash_words - 1)) == 0, WV_ERR_ARG,
            "hash_words must be 0 or a power of two");
   WV_CHECK(c, sh->query_warps <= 1 || (c->parents > 0 && (sh->query_warps == 2 || sh->query_warps == 4) &&
-                                       sh->warps_per_block % sh->query_warps == 0),
-           WV_ERR_ARG, "query_warps %d: 1, or 2 / 4 dividing warps_per_block with the throughput form",
+                                       sh->warps_per_block == sh->query_warps),
+           WV_ERR_ARG, "query_warps %d: 1, or 2 / 4 equal to warps_per_block with the throughput form",
            sh->query_warps);
   WV_CHECK(c, sh->hash_words == 0 || sh->hash_words >= search_hash_min(p->Lcap, c->n), WV_ERR_ARG,
            "hash_words=%u below the least area %u for L=%u, n=%u", sh->hash_words, search_hash_min(p->Lcap, c->n),

@@ -83,7 +83,8 @@ struct SearchShape {
   int wpb = 4;
   uint32_t hcap = 0;
   bool wide = false;  // 32-bit visited-hash entries even where 16-bit ones would do
-  // the throughput form only: warps per query (1, 2 or 4; wpb a multiple):
+  // the throughput form only: warps per query (1, or 2 / 4 = wpb: one query
+  // per block):
   // the leader warp runs the search, the others take shares of its
   // distance passes (more rows in flight per query's shared memory)
   int qw = 1;
