@@ -403,17 +403,20 @@ __device__ int beam_merge(const BeamSmem &s, int L, int ncand, int lane) {
   return mink;
 }
 
-template <int DK>
+// COOP: the variant with several warps per query (launches with
+// query_warps > 1); the single-warp variant keeps its distances in registers
+// and uses no named barrier
+template <int DK, bool COOP>
 __global__ void __maxnreg__(128) k_beam(SearchArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   const int W = blockDim.x >> 5;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // query groups of QW warps (the launch keeps W a multiple of QW)
-  const int QW = a.query_warps > 1 ? a.query_warps : 1;
+  const int QW = COOP && a.query_warps > 1 ? a.query_warps : 1;
   const int grp = warp / QW, mem = warp % QW;
   const size_t wbytes = beam_warp_bytes(a.d, a.Lmax, a.cap, a.hcap);
   const BeamSmem s = beam_carve(smem + grp * wbytes, a.d, a.Lmax, a.cap, a.hcap);
-  if (mem != 0) {
+  if (COOP && mem != 0) {
     beam_member<DK>(a, s, grp, mem, QW, lane);
     return;
   }
@@ -589,14 +592,15 @@ __global__ void __maxnreg__(128) k_beam(SearchArgs a) {
         }
       }
       __syncwarp();
-      // distances (into sd); the ones closer than the pool's last entry are
-      // accepted
-      if (nfresh > 0) beam_pass<DK>(a, s, BT_FRESH, (int)nfresh, ints, lo, qn, grp, QW, lane);
+      // distances (in registers, or with several warps per query through sd);
+      // the ones closer than the pool's last entry are accepted
+      if (COOP && nfresh > 0) beam_pass<DK>(a, s, BT_FRESH, (int)nfresh, ints, lo, qn, grp, QW, lane);
       int ncand = 0;
       for (uint32_t b = 0; b < nfresh; b += 32) {
         const int cnt = (int)min(32u, nfresh - b);
         const uint32_t my = lane < cnt ? s.si[b + lane] : 0u;
-        const float dist = lane < cnt ? s.sd[b + lane] : 0.f;
+        const float dist = COOP ? (lane < cnt ? s.sd[b + lane] : 0.f)
+                                : beam_dist<DK>(a, ints, lo, s.qf, my, cnt, s.qv, qn, lane);
         const bool acc = lane < cnt && dist < thr;
         const unsigned am = __ballot_sync(FULL, acc);
         if (acc) {
@@ -676,7 +680,7 @@ __global__ void __maxnreg__(128) k_beam(SearchArgs a) {
     vis.clear(lane);
   }
   // the member warps leave with the leader
-  if (QW > 1) {
+  if (COOP && QW > 1) {
     __syncwarp();
     if (lane == 0) s.task[0] = BT_EXIT;
     group_bar(grp, QW);
@@ -694,13 +698,35 @@ int beam_kind(const SearchArgs &a) {
   return BD_GENERIC;
 }
 
-template <int DK>
+template <int DK, bool COOP>
 int beam_blocks_per_sm(int threads, size_t smem) {
-  if (cudaFuncSetAttribute(k_beam<DK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_beam<DK, COOP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return -1;
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_beam<DK>, threads, smem) != cudaSuccess) return -1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_beam<DK, COOP>, threads, smem) != cudaSuccess)
+    return -1;
   return per_sm;
+}
+
+template <bool COOP>
+int beam_blocks_all(int threads, size_t smem) {
+  int per_sm = 1 << 30;
+  // every distance path a launch may pick must fit
+  for (int v : {beam_blocks_per_sm<BD_GENERIC, COOP>(threads, smem), beam_blocks_per_sm<BD_BF16_128, COOP>(threads, smem),
+                beam_blocks_per_sm<BD_BF16_96, COOP>(threads, smem),
+                beam_blocks_per_sm<BD_F32INT_128, COOP>(threads, smem)})
+    per_sm = std::min(per_sm, v);
+  return per_sm;
+}
+
+template <bool COOP>
+void beam_launch(int dk, int blocks, int threads, size_t smem, cudaStream_t stream, const SearchArgs &b) {
+  switch (dk) {
+    case BD_BF16_128: k_beam<BD_BF16_128, COOP><<<blocks, threads, smem, stream>>>(b); break;
+    case BD_BF16_96: k_beam<BD_BF16_96, COOP><<<blocks, threads, smem, stream>>>(b); break;
+    case BD_F32INT_128: k_beam<BD_F32INT_128, COOP><<<blocks, threads, smem, stream>>>(b); break;
+    default: k_beam<BD_GENERIC, COOP><<<blocks, threads, smem, stream>>>(b); break;
+  }
 }
 
 }  // namespace
@@ -720,12 +746,7 @@ int beam_grid(uint32_t d, uint32_t Lmax, uint32_t gw, uint32_t parents, int devi
   if (!beam_shape_ok(sh)) return 0;
   const size_t smem = (size_t)(sh.wpb / sh.qw) * beam_warp_bytes(d, Lmax, beam_cap(gw, parents), sh.hcap);
   if (smem > 227 * 1024) return 0;
-  int per_sm = 1 << 30;
-  // every distance path a launch may pick must fit
-  for (int v : {beam_blocks_per_sm<BD_GENERIC>(sh.wpb * 32, smem), beam_blocks_per_sm<BD_BF16_128>(sh.wpb * 32, smem),
-                beam_blocks_per_sm<BD_BF16_96>(sh.wpb * 32, smem),
-                beam_blocks_per_sm<BD_F32INT_128>(sh.wpb * 32, smem)})
-    per_sm = std::min(per_sm, v);
+  const int per_sm = sh.qw > 1 ? beam_blocks_all<true>(sh.wpb * 32, smem) : beam_blocks_all<false>(sh.wpb * 32, smem);
   if (per_sm <= 0) {
     cudaGetLastError();
     return 0;
@@ -743,12 +764,8 @@ cudaError_t launch_beam(const SearchArgs &a, SearchShape sh, int blocks, cudaStr
   b.wide_hash = sh.wide ? 1 : 0;
   b.query_warps = sh.qw;
   const size_t smem = (size_t)(sh.wpb / sh.qw) * beam_warp_bytes(b.d, b.Lmax, b.cap, b.hcap);
-  switch (beam_kind(b)) {
-    case BD_BF16_128: k_beam<BD_BF16_128><<<blocks, sh.wpb * 32, smem, stream>>>(b); break;
-    case BD_BF16_96: k_beam<BD_BF16_96><<<blocks, sh.wpb * 32, smem, stream>>>(b); break;
-    case BD_F32INT_128: k_beam<BD_F32INT_128><<<blocks, sh.wpb * 32, smem, stream>>>(b); break;
-    default: k_beam<BD_GENERIC><<<blocks, sh.wpb * 32, smem, stream>>>(b); break;
-  }
+  if (sh.qw > 1) beam_launch<true>(beam_kind(b), blocks, sh.wpb * 32, smem, stream, b);
+  else beam_launch<false>(beam_kind(b), blocks, sh.wpb * 32, smem, stream, b);
   return cudaGetLastError();
 }
 
