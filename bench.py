@@ -37,7 +37,7 @@ from weavess_gb300 import datasets as ds  # noqa: E402
 
 CFG = dict(n=1_000_000, d=128, centers=256, nq=10_000, seed=7, S=20, K=64, L=80, ITER=8, R=100, expansions=(0, 1, 2, 3, 4),
            R_refine=32, L_refine=64, C_refine=500, k=10, target_recall=0.95,
-           n_train=200_000, n_val=2000, clusters=64, L_trace=1024, L_max_learned=512, epochs=6,
+           n_train=200_000, n_val=2000, clusters=64, L_trace=1024, L_max_learned=256, epochs=6,
            L_grid=[16, 24, 32, 48, 64, 96, 128, 160, 192, 256, 320, 384, 448, 512, 640, 768, 896, 1024, 1280,
                    1536])
 METRIC = "QPS at recall@10>=0.95 (learned+BF16 vs plain FP32, 1 GB300); build sec"
@@ -746,28 +746,33 @@ def run_precision96(args):
         ctx.set_precision(storage, rerank=0)
         got = ctx.candidate_distances(qs, ids).astype(np.float64)
         err = np.abs(got - exact)
-        sweep, Lsel = {}, cfg["L_grid"][-1]
-        for L in cfg["L_grid"]:
-            ctx.srand(777)  # the timed steps' seeds
-            res, _, _ = ctx.search(query, L, K)
-            sweep[L] = round(recall(res, gt, K), 4)
-            if sweep[L] >= cfg["target_recall"]:
-                Lsel = L
-                break
-        ctx.srand(777)
-        seeds = torch.from_numpy(ctx.draw_seeds(nq, Lsel, "rand").astype(np.int32)).to(dev)
-        plan = ctx.plan(nq, K, dq.data_ptr(), dout.data_ptr(), L_max=Lsel, mode="seeds", d_seeds=seeds.data_ptr())
-        tune = plan.tune(nq)
-        ms, kms, (dc, hc), clk = _timed_plan(torch, plan, nq, args, stream, flush)
-        plan.close()
-        r = recall(dout.cpu().numpy().astype(np.uint32), gt, K)
-        out[storage] = {"qps": round(nq / (ms / 1e3), 1), "L_search": Lsel, "recall@10": round(r, 4),
+        for E in (0, 2):
+            # the exact traversal, and the throughput form (bf16 rows of d = 96
+            # on the tensor cores with a hi + lo bf16 query)
+            ctx.set_expansion(E)
+
+            def rec(L):
+                ctx.srand(777)  # the timed steps' seeds
+                res, _, _ = ctx.search(query, L, K)
+                return recall(res, gt, K)
+
+            Lsel, sweep = bisect_beam(rec, cfg["L_grid"], cfg["target_recall"])
+            ctx.srand(777)
+            seeds = torch.from_numpy(ctx.draw_seeds(nq, Lsel, "rand").astype(np.int32)).to(dev)
+            plan = ctx.plan(nq, K, dq.data_ptr(), dout.data_ptr(), L_max=Lsel, mode="seeds", d_seeds=seeds.data_ptr())
+            tune = plan.tune(nq)
+            ms, kms, (dc, hc), clk = _timed_plan(torch, plan, nq, args, stream, flush)
+            plan.close()
+            ctx.set_expansion(0)
+            r = recall(dout.cpu().numpy().astype(np.uint32), gt, K)
+            key = storage if E == 0 else f"{storage}_E{E}"
+            out[key] = {"qps": round(nq / (ms / 1e3), 1), "L_search": Lsel, "recall@10": round(r, 4),
                         "recall_sweep": sweep, "search_kernel_ms": round(kms, 4), "dist_count": dc,
                         "tuned_shape": tune["chosen"], "clocks": clk,
                         "err_vs_fp64": {"max_abs": float(err.max()), "mean_abs": float(err.mean()),
                                         "max_rel_to_mean_dist": float(err.max() / exact.mean()),
                                         "mean_rel": float((err / np.maximum(exact, 1e-12)).mean())}}
-        log(f"{storage}: {out[storage]}")
+            log(f"{key}: {out[key]}")
     ctx.set_precision("fp32")
     best = max(out, key=lambda k: out[k]["qps"])
     line = {"metric": "QPS at recall@10>=0.95 per candidate precision (1M x 96 unit vectors)",
