@@ -649,15 +649,13 @@ def run_reference(args):
     build_s = time.time() - t
     log(f"reference build {build_s:.1f}s (NN-Descent {t_nnd:.1f}s) on {threads} threads")
     gt = ds.groundtruth_fp64(base, query, 10)
-    Lsel = cfg["L_grid"][-1]
-    sweep = {}
-    for L in cfg["L_grid"]:
+
+    def rec(L):
         res, _, _ = O.search(base, query, g, L, O.Rand(5), threads=threads)
-        sweep[L] = round(recall(res, gt), 4)
-        log(f"reference L={L} recall={sweep[L]}")
-        if sweep[L] >= cfg["target_recall"]:
-            Lsel = L
-            break
+        return recall(res, gt)
+
+    # the smallest beam reaching the target, bisected as for the GPU search
+    Lsel, sweep = bisect_beam(rec, cfg["L_grid"], cfg["target_recall"])
     for _ in range(args.warmup):
         O.search(base, query, g, Lsel, O.Rand(5), threads=threads)
     ts = []
