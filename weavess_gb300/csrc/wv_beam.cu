@@ -28,7 +28,15 @@
 //    integer below 2^24, so the result is exact).  Distance = |q|^2 + |x|^2 -
 //    2 q.x with the stored rows' squared norms;
 //  * the seeds are marked visited when they enter the pool (a seed met again
-//    as a neighbour is not re-scored), duplicate seeds keep one entry.
+//    as a neighbour is not re-scored), duplicate seeds keep one entry;
+//  * the rows of the next step's parents are read before the merge that
+//    settles them (the next parents are the E closest of the pool's next
+//    unexpanded entries and the sorted candidates), so the row reads of a
+//    step overlap the previous merge;
+//  * with query_warps = 2 or 4 (a launch-shape dimension; one query per
+//    block) member warps take shares of the leader warp's distance passes
+//    through a named barrier -- the separately compiled COOP variant; the
+//    single-warp variant keeps its distances in registers.
 //
 // Other row layouts (fp8, other d) use warp-cooperative row distances (a
 // warp per row, coalesced; FP32 rows of real-valued data in an order that is
