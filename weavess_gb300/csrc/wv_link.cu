@@ -33,8 +33,11 @@
 //    insertions from higher ids, read from their snapshots.  Each warp keeps
 //    the vectors' pairwise distances of its row in shared memory, so an
 //    insertion costs one new distance column.
+#include <cuda_bf16.h>
+
 #include <algorithm>
 #include <cmath>
+#include <string>
 #include <vector>
 
 #include "warp_sort.cuh"
@@ -86,6 +89,7 @@ struct PruneArgs {
   const uint32_t *g_deg;
   uint32_t gw;
   int clean;            // Vamana: a short pool is sorted too (clean mode)
+  const float *xnorm;   // integer data, d % 32 == 0, d <= 128, R <= 32: the Gram-tile variant's row norms
   int *gscr;            // per warp: 2 * vcap + 256 ints
   HeapItem *hscr;       // per warp: vcap items (VAMANA refill)
   uint32_t *out_ids;    // rows of width R, indexed by node
@@ -106,8 +110,76 @@ __device__ __forceinline__ bool ssg_occludes(float pd, float rd, float djk, floa
   return cos_ij > threshold;
 }
 
-// MODE: 0 Vamana, 1 NSG, 2 SSG
-template <int MODE>
+// ---- pair distances of a prune batch as Gram tiles (integer data)
+// On integer data in [0, 255] with d a multiple of 32 up to 128, the exact
+// distance of rows x, y equals |x|^2 + |y|^2 - 2 x.y computed in FP32 (every
+// value an integer below 2^24), and x.y comes from BF16 tensor-core tiles
+// (integers up to 255 are exact in BF16).  Per warp, shared memory holds the
+// rows picked so far and the batch's 32 candidate rows as BF16 (row stride
+// an odd multiple of 64 bytes: the fragment loads are free of bank
+// conflicts), and the two tiles candidate x picked and candidate x candidate.
+constexpr uint32_t PT_ROWS = 32;  // rows picked (R <= 32) and candidates per batch
+
+__host__ __device__ inline uint32_t pt_stride(uint32_t d) { return (d * 2) % 128 == 64 ? d * 2 : d * 2 + 64; }
+__host__ __device__ inline size_t pt_warp_bytes(uint32_t d) {
+  return 2 * (size_t)PT_ROWS * pt_stride(d) + 2 * (size_t)PT_ROWS * PT_ROWS * 4 + PT_ROWS * 4;
+}
+
+__device__ __forceinline__ uint32_t pt_pack(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+// row `id` of the FP32 base into slot `r` of a BF16 row area (16 lanes per row)
+__device__ __forceinline__ void pt_stage_row(uint8_t *area, uint32_t stride, uint32_t r, const float *base,
+                                             uint32_t d, uint32_t id, int sub) {
+  for (uint32_t k = (uint32_t)sub * 8; k < d; k += 16 * 8) {
+    const float4 *src = reinterpret_cast<const float4 *>(base + (size_t)id * d + k);
+    const float4 x0 = __ldg(src), x1 = __ldg(src + 1);
+    *reinterpret_cast<uint4 *>(area + (size_t)r * stride + k * 2) =
+        make_uint4(pt_pack(x0.x, x0.y), pt_pack(x0.z, x0.w), pt_pack(x1.x, x1.y), pt_pack(x1.z, x1.w));
+  }
+}
+
+__device__ __forceinline__ void pt_mma(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                       uint32_t b1) {
+  asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// G[x][y] = X_x . Y_y for the 32 rows of X and the first ncol (a multiple of
+// 8, <= 32) rows of Y; lane (g, j) loads dimensions 32t + 8j .. +7 of its
+// rows (the dot product's terms permuted alike in A and B)
+__device__ void pt_gram(const uint8_t *X, const uint8_t *Y, uint32_t stride, uint32_t d, uint32_t ncol, float *G,
+                        int lane) {
+  const int g = lane >> 2, j = lane & 3;
+  const uint32_t T = d / 32;
+  for (int gi = 0; gi < 2; gi++) {
+    for (uint32_t nt = 0; nt * 8 < ncol; nt++) {
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      for (uint32_t t = 0; t < T; t++) {
+        const uint32_t off = (32 * t + 8 * j) * 2;
+        const uint4 a0 = *reinterpret_cast<const uint4 *>(X + (size_t)(16 * gi + g) * stride + off);
+        const uint4 a1 = *reinterpret_cast<const uint4 *>(X + (size_t)(16 * gi + g + 8) * stride + off);
+        const uint4 b = *reinterpret_cast<const uint4 *>(Y + (size_t)(8 * nt + g) * stride + off);
+        pt_mma(acc, a0.x, a1.x, a0.y, a1.y, b.x, b.y);
+        pt_mma(acc, a0.z, a1.z, a0.w, a1.w, b.z, b.w);
+      }
+      // lane (g, j): rows 16 gi + g (c0, c1) and + 8 (c2, c3), columns 8 nt + 2j, + 1
+      float *r0 = G + (size_t)(16 * gi + g) * PT_ROWS + 8 * nt + 2 * j;
+      float *r1 = G + (size_t)(16 * gi + g + 8) * PT_ROWS + 8 * nt + 2 * j;
+      r0[0] = acc[0];
+      r0[1] = acc[1];
+      r1[0] = acc[2];
+      r1[1] = acc[3];
+    }
+  }
+}
+
+// MODE: 0 Vamana, 1 NSG, 2 SSG.  TC: the pair distances from Gram tiles
+// (integer data, d a multiple of 32 up to 128, R <= 32; same values)
+template <int MODE, bool TC>
 __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
   constexpr bool NSG = MODE != 0;  // the NSG-style walk (SSG shares it with the angle test)
   __shared__ uint32_t pk_id[PR_WARPS][LINK_MAX_R];
@@ -118,6 +190,15 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
   HeapItem *heap = a.hscr + (size_t)gwarp * a.vcap;
   uint32_t *pid = pk_id[warp];
   float *pd = pk_d[warp];
+  // TC: per warp, the picked rows, the batch's rows, the two tiles, the
+  // picked rows' norms
+  extern __shared__ __align__(16) uint8_t pt_smem[];
+  const uint32_t pst = pt_stride(a.d);
+  uint8_t *prow = pt_smem + (TC ? (size_t)warp * pt_warp_bytes(a.d) : 0);
+  uint8_t *crow = prow + (size_t)PT_ROWS * pst;
+  float *G1 = reinterpret_cast<float *>(crow + (size_t)PT_ROWS * pst);
+  float *G2 = G1 + PT_ROWS * PT_ROWS;
+  float *pxn = G2 + PT_ROWS * PT_ROWS;
   for (uint32_t qi = gwarp; qi < a.cnt; qi += nwarps) {
     const uint32_t node = a.n0 + qi;
     DI *pool = a.vis + (size_t)qi * a.vcap;
@@ -177,11 +258,31 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
       ex = start + 1;
       end = MODE == 2 ? m : min(m, a.maxc);  // SSG examines the whole pool
       __syncwarp();
+      if (TC) {
+        const uint32_t id0 = pid[0];
+        if (lane < 16) pt_stage_row(prow, pst, 0, a.base, a.d, id0, lane);
+        if (lane == 0) pxn[0] = __ldg(a.xnorm + id0);
+        __syncwarp();
+      }
     }
     bool done = np >= a.R;
     while (!done && ex < end) {
       const uint32_t cnt = min(32u, end - ex);
       DI cand = lane < (int)cnt ? pool[ex + lane] : DI{0.f, 0u};
+      float cxn = 0.f;
+      if (TC) {
+        // the batch's rows (rows past cnt: row 0 of the base, never read) and
+        // the tiles candidate x picked-before-the-batch, candidate x candidate
+        for (uint32_t r = lane >> 4; r < PT_ROWS; r += 2) {
+          const uint32_t id = __shfl_sync(0xffffffffu, cand.i, r);
+          pt_stage_row(crow, pst, r, a.base, a.d, r < cnt ? id : 0u, lane & 15);
+        }
+        cxn = lane < (int)cnt ? __ldg(a.xnorm + cand.i) : 0.f;
+        __syncwarp();
+        if (np > 0) pt_gram(crow, prow, pst, a.d, (np + 7) & ~7u, G1, lane);
+        pt_gram(crow, crow, pst, a.d, (cnt + 7) & ~7u, G2, lane);
+        __syncwarp();
+      }
       // against the rows picked before this batch
       bool s1 = false, dup1 = false;  // dup1 (clean Vamana): the node itself or an id picked before
       if (lane < (int)cnt) {
@@ -193,7 +294,7 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
         for (uint32_t j = 0; j < np && !s1; j++) {
           if (NSG && pid[j] == cand.i) s1 = true;
           else {
-            float dd = l2g(a.base, a.d, pid[j], cand.i);
+            float dd = TC ? (pxn[j] + cxn) - 2.f * G1[lane * PT_ROWS + j] : l2g(a.base, a.d, pid[j], cand.i);
             s1 = MODE == 2 ? ssg_occludes(cand.d, pd[j], dd, a.threshold)
                            : (NSG ? (dd < cand.d) : (__fmul_rn(a.alpha, dd) < cand.d));
           }
@@ -205,13 +306,14 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
       for (int b = 0; b < (int)cnt; b++) {
         const uint32_t bid = __shfl_sync(FULL, cand.i, b);
         const float bd = __shfl_sync(FULL, cand.d, b);
+        const float bxn = TC ? __shfl_sync(FULL, cxn, b) : 0.f;
         if (b < lane && lane < (int)cnt) {
           bool hit;
           if ((NSG || cv) && bid == cand.i) {
             hit = true;
             if (cv) dupo |= 1u << b;
           } else {
-            float dd = l2g(a.base, a.d, bid, cand.i);
+            float dd = TC ? (bxn + cxn) - 2.f * G2[lane * PT_ROWS + b] : l2g(a.base, a.d, bid, cand.i);
             hit = MODE == 2 ? ssg_occludes(cand.d, bd, dd, a.threshold)
                             : (NSG ? (dd < cand.d) : (__fmul_rn(a.alpha, dd) < cand.d));
           }
@@ -219,6 +321,7 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
         }
       }
       // the sequential walk of the reference over this batch
+      const uint32_t np0 = np;
       uint32_t pm = 0;
       uint32_t stop = cnt;
       for (int b = 0; b < (int)cnt; b++) {
@@ -245,6 +348,19 @@ __global__ void __launch_bounds__(PR_WARPS * 32) k_prune(PruneArgs a) {
         }
       }
       __syncwarp();
+      if (TC) {
+        // the rows picked in this batch join the picked rows (and norms)
+        uint32_t k = np0;
+        for (uint32_t mm = pm; mm; mm &= mm - 1, k++) {
+          const int b = __ffs(mm) - 1;
+          const float bxn = __shfl_sync(FULL, cxn, b);
+          for (uint32_t o = (uint32_t)lane * 16; o < a.d * 2; o += 32 * 16)
+            *reinterpret_cast<uint4 *>(prow + (size_t)k * pst + o) =
+                *reinterpret_cast<const uint4 *>(crow + (size_t)b * pst + o);
+          if (lane == 0) pxn[k] = bxn;
+        }
+        __syncwarp();
+      }
       ex += stop;
     }
     if (!NSG && np < a.R && nskip > 0) {
@@ -1002,9 +1118,29 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
       pa.out_dist = p_dist;
       pa.out_deg = p_deg;
       pa.status = c->d_status();
-      if (ssg) k_prune<2><<<prune_blocks, PR_WARPS * 32, 0, c->stream>>>(pa);
-      else if (!vamana) k_prune<1><<<prune_blocks, PR_WARPS * 32, 0, c->stream>>>(pa);
-      else k_prune<0><<<prune_blocks, PR_WARPS * 32, 0, c->stream>>>(pa);
+      // integer data (d % 32 == 0, d <= 128) and R <= 32: the pair distances
+      // from Gram tiles, the same values (WV_LINK_PRUNE=fp32 keeps the
+      // exact-order FP32 sums)
+      const char *pr_env = getenv("WV_LINK_PRUNE");
+      const bool tc = c->base_int && c->d % 32 == 0 && c->d <= 128 && R <= PT_ROWS &&
+                      !(pr_env && std::string(pr_env) == "fp32");
+      pa.xnorm = tc ? c->xnorm.as<float>() : nullptr;
+      const size_t tsm = tc ? (size_t)PR_WARPS * pt_warp_bytes(c->d) : 0;
+      if (tc) {
+        if (ssg) WV_CUDA(c, cudaFuncSetAttribute(k_prune<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+        else if (!vamana) WV_CUDA(c, cudaFuncSetAttribute(k_prune<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+        else WV_CUDA(c, cudaFuncSetAttribute(k_prune<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+      }
+      if (ssg) {
+        if (tc) k_prune<2, true><<<prune_blocks, PR_WARPS * 32, tsm, c->stream>>>(pa);
+        else k_prune<2, false><<<prune_blocks, PR_WARPS * 32, 0, c->stream>>>(pa);
+      } else if (!vamana) {
+        if (tc) k_prune<1, true><<<prune_blocks, PR_WARPS * 32, tsm, c->stream>>>(pa);
+        else k_prune<1, false><<<prune_blocks, PR_WARPS * 32, 0, c->stream>>>(pa);
+      } else {
+        if (tc) k_prune<0, true><<<prune_blocks, PR_WARPS * 32, tsm, c->stream>>>(pa);
+        else k_prune<0, false><<<prune_blocks, PR_WARPS * 32, 0, c->stream>>>(pa);
+      }
       WV_CUDA(c, cudaGetLastError());
       rc = check_device_status(c, "prune");
       if (rc) return rc;
