@@ -430,7 +430,8 @@ int wv_plan_destroy(wv_plan *plan);
  * array's address up and keeps it for later calls; make that first call
  * before any stream capture, and after a cudaDeviceReset the kept address is
  * stale (the library must then be reloaded).  The call returns once the
- * search has finished on `stream` (it reads the kernel's status back).
+ * search has finished on `stream` (it reads the kernel's status back), so
+ * it is synchronous and cannot itself be captured into a CUDA graph.
  * Returns WV_ERR_LIMIT when n is too large for the fixed array (n / 16
  * words per warp slot, four slots at least: about 67 million nodes) or L /
  * width exceed the search limits, WV_ERR_DEVICE if the kernel saw an id >= n. */

@@ -144,7 +144,13 @@ def test_vamana_clean_mode_matches_oracle_20k(ctx, mix20k, alpha, L_refine):
     assert rows_equal(ids, dist, deg, gv.ids, gv.dist, gv.deg) == 0, st
 
 
-def test_nsg_matches_oracle_20k(ctx, mix20k):
+@pytest.mark.parametrize("prune", ["gram", "fp32"])
+def test_nsg_matches_oracle_20k(ctx, mix20k, prune, monkeypatch):
+    # integer rows: the prune's pair distances come from BF16 Gram tiles by
+    # default, from ordered FP32 sums with WV_LINK_PRUNE=fp32; both must give
+    # the reference's graph
+    if prune == "fp32":
+        monkeypatch.setenv("WV_LINK_PRUNE", "fp32")
     base, query, g = mix20k
     ctx.upload_base(base)
     ctx.srand(1)
