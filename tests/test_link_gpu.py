@@ -239,3 +239,25 @@ def test_vamana_pipeline_matches_oracle_20k(ctx, mix20k, L):
     res, dc, hc = ctx.search(query, 64, 10, entry="centroid")
     eres, edc, ehc = O.search(base, query, g, 64, ro, entry="centroid")
     assert np.array_equal(res, eres) and (dc, hc) == (edc, ehc)
+
+
+def test_nsg_conn_batched_equals_serial(ctx, monkeypatch):
+    """ConnNSGDFS's greedy searches run in batches that the host takes in
+    repair order; with one search at a time (WV_CONN_BATCH=1), a small batch
+    and the default, the rows, the repairs and the rand() draws must agree."""
+    base, _ = ds.int_mixture(100_000, 128, 64, seed=5)
+    out = {}
+    for batch in ("1", "7", "4096"):
+        monkeypatch.setenv("WV_CONN_BATCH", batch)
+        ctx.upload_base(base)
+        ctx.srand(1)
+        ctx.init_random(10)
+        ctx.nnd_refine(10, 24, 40, 6, 50)
+        st = ctx.nsg_refine(32, 32, 500)
+        out[batch] = (st, ctx.get_graph())
+    s1, (i1, d1, g1, e1) = out["1"]
+    assert s1["conn_added"] >= 10, s1
+    for batch in ("7", "4096"):
+        s, (i, d, g, e) = out[batch]
+        assert s["conn_added"] == s1["conn_added"] and s["rand_draws"] == s1["rand_draws"], (batch, s, s1)
+        assert e == e1 and rows_equal(i, d, g, i1, d1, g1) == 0, batch

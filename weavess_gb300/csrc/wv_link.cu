@@ -9,8 +9,9 @@
 // (component_candidate.cpp:10-109), ComponentPruneVAMANA / ComponentPruneNSG /
 // ComponentPruneSSG (component_prune.cpp:20-122, 245-300) and
 // ComponentRefineEntryCentroid (component_entry.cpp:9-92).
-// ComponentConnNSGDFS runs on the host (a serial depth-first walk), with its
-// greedy searches on the GPU; ComponentConnSSGDFS (component_conn.cpp:
+// ComponentConnNSGDFS walks on the host (the depth-first walk fixes which
+// nodes get linked), with its greedy searches batched on the GPU and taken
+// in repair order; ComponentConnSSGDFS (component_conn.cpp:
 // 169-225) walks on the GPU (frontier kernels) with the repairs on the device.
 //
 // Plain form, bit-exact with the single-threaded reference:
@@ -37,6 +38,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -739,10 +741,6 @@ __global__ void k_centroid(const float *base, uint32_t n, uint32_t d, float *cen
   center[j] = __fdiv_rn(acc, (float)n);
 }
 
-__global__ void k_pair_l2(const float *base, uint32_t d, uint32_t a, uint32_t b, float *out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) *out = l2g(base, d, a, b);
-}
-
 // ---------------------------------------------------------------- Propagation2
 // ComponentCandidatePropagation2::CandidateInner (component_candidate.cpp:90-109):
 // the pool takes the unseen neighbours of the node's neighbours, walking the
@@ -1265,12 +1263,57 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
   return WV_OK;
 }
 
+// The conn edges root -> id at row position pos, applied on the device: the
+// id, the distance compare(base[root], base[id]) (ComponentConnNSGDFS::
+// findroot, component_conn.cpp:94-97) and the row's degree; h[i] keeps the
+// distance for the host copy of the rows.
+struct ConnEdge {
+  uint32_t root, id, pos;
+};
+
+__global__ void k_conn_edges(const float *base, uint32_t d, const ConnEdge *e, uint32_t ne, uint32_t *gids,
+                             float *gdist, uint32_t *gdeg, uint32_t w, float *h) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ne; i += gridDim.x * blockDim.x) {
+    const ConnEdge x = e[i];
+    const float dv = l2g(base, d, x.root, x.id);
+    gids[(size_t)x.root * w + x.pos] = x.id;
+    gdist[(size_t)x.root * w + x.pos] = dv;
+    atomicMax(gdeg + x.root, x.pos + 1);
+    h[i] = dv;
+  }
+}
+
+// rows ids[0..B) of the base, packed (the queries of a batch of searches)
+__global__ void k_conn_rows(const float *base, uint32_t d, const uint32_t *ids, uint32_t B, float *out) {
+  const size_t total = (size_t)B * d;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x)
+    out[t] = base[(size_t)ids[t / d] * d + t % d];
+}
+
 int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
-  // ComponentConnNSGDFS::tree_grow (component_conn.cpp:14-28): host DFS over
-  // the graph; each unreached node is linked from the nearest reached node a
-  // greedy search finds (GPU), or a random reached node.  The searches read
-  // the graph with the edges added so far, so each new edge is written into
-  // the device rows at once (rows carry spare width for them).
+  // ComponentConnNSGDFS::tree_grow (component_conn.cpp:14-98).
+  //
+  // Which nodes get linked, and in which order, follows from the rows alone:
+  // everything reachable from a flagged node is flagged, so the DFS after a
+  // repair leaves the new root only through the new edge, the flagged set
+  // after repair k is the closure of ep and the first k linked nodes over
+  // the rows as they were, and the next linked node is the smallest
+  // unflagged id.  The host walks that first: ft[x] is the repair after
+  // which x is flagged (0: the walk from ep), tgt the linked nodes in order.
+  //
+  // The roots come from greedy searches (get_neighbors from ep's row) that
+  // read the rows with the edges added so far and draw rand() for their
+  // seeds.  They run as one batch over the linked nodes still to do, all on
+  // the rows and the rand() stream as they stand at the batch's start (the
+  // seeds from a copy of the stream).  The host then takes the results in
+  // repair order and accepts search k while (a) the real stream, at k's
+  // turn, gives the same seeds (the fallback's extra draws and an edge
+  // appended to a short ep row change them) and (b) none of the rows it
+  // read -- its seeds' and its visits' -- got an edge earlier in the batch.
+  // The first search that fails starts the next batch, so every accepted
+  // search is the one the serial walk runs and the first of a batch is
+  // always accepted.  With a caller's rand() function (the stream cannot be
+  // copied) each batch is one search.
   const uint32_t n = c->n, ep = c->fg_ep;
   uint32_t w = c->fg_w;
   std::vector<uint32_t> deg(n), ids((size_t)n * w);
@@ -1279,6 +1322,44 @@ int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
   WV_CUDA(c, cudaMemcpyAsync(ids.data(), c->fg_ids.p, (size_t)n * w * 4, cudaMemcpyDeviceToHost, c->stream));
   WV_CUDA(c, cudaMemcpyAsync(dist.data(), c->fg_dist.p, (size_t)n * w * 4, cudaMemcpyDeviceToHost, c->stream));
   WV_CUDA(c, cudaStreamSynchronize(c->stream));
+  *added = 0;
+  // the walk: flag times and the linked nodes
+  constexpr uint32_t NONE = 0xffffffffu;
+  std::vector<uint32_t> ft(n, NONE), tgt, st;
+  for (uint32_t v = 0; v < n; v++)
+    for (uint32_t j = 0; j < deg[v]; j++)
+      WV_CHECK(c, ids[(size_t)v * w + j] < n, WV_ERR_STATE, "row %u holds id %u >= n", v, ids[(size_t)v * w + j]);
+  auto walk = [&](uint32_t start, uint32_t t) {  // DFS (component_conn.cpp:31-57)
+    st.assign(1, start);
+    ft[start] = t;
+    uint32_t tmp = start;
+    while (!st.empty()) {
+      uint32_t next = NONE;
+      for (uint32_t j = 0; j < deg[tmp]; j++)
+        if (ft[ids[(size_t)tmp * w + j]] == NONE) {
+          next = ids[(size_t)tmp * w + j];
+          break;
+        }
+      if (next == NONE) {
+        st.pop_back();
+        if (st.empty()) break;
+        tmp = st.back();
+        continue;
+      }
+      tmp = next;
+      ft[tmp] = t;
+      st.push_back(tmp);
+    }
+  };
+  walk(ep, 0);
+  for (uint32_t cur = 0;;) {  // findroot's first unflagged id only grows
+    while (cur < n && ft[cur] != NONE) cur++;
+    if (cur == n) break;
+    tgt.push_back(cur);
+    walk(cur, (uint32_t)tgt.size());
+  }
+  const uint32_t m = (uint32_t)tgt.size();
+  if (m == 0) return WV_OK;
   // re-lays rows out with width nw (host arrays and device copy)
   auto relayout = [&](uint32_t nw) -> int {
     std::vector<uint32_t> i2((size_t)n * nw, 0);
@@ -1299,115 +1380,151 @@ int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
     c->fg_w = w;
     return WV_OK;
   };
-  std::vector<char> flag(n, 0);
-  uint32_t root = ep, cnt = 0;
-  *added = 0;
-  cudaError_t e = cudaSuccess;
-  float *dd = c->buf<float>("conn_d", 4, &e);
-  uint32_t *dseed = c->buf<uint32_t>("conn_seed", L_refine, &e);
-  uint32_t *one = c->buf<uint32_t>("conn_one", 4, &e);
-  DI *vis = c->buf<DI>("conn_vis", (size_t)n + L_refine + 64, &e);
-  WV_CUDA(c, e);
-  std::vector<DI> hv;
-  bool widened = false;
-  while (cnt < n) {
-    std::vector<uint32_t> st;
-    uint32_t tmp = root;
-    st.push_back(root);
-    if (!flag[root]) cnt++;
-    flag[root] = 1;
-    while (!st.empty()) {
-      uint32_t next = n + 1;
-      for (uint32_t j = 0; j < deg[tmp]; j++)
-        if (!flag[ids[(size_t)tmp * w + j]]) {
-          next = ids[(size_t)tmp * w + j];
-          break;
-        }
-      if (next == n + 1) {
-        st.pop_back();
-        if (st.empty()) break;
-        tmp = st.back();
+  // accepted edges not yet in the device rows; their distances come back
+  // into the host rows
+  std::vector<ConnEdge> edges;
+  std::vector<float> hbuf;
+  auto flush = [&]() -> int {
+    if (edges.empty()) return WV_OK;
+    const uint32_t ne = (uint32_t)edges.size();
+    cudaError_t e2 = cudaSuccess;
+    ConnEdge *de = c->buf<ConnEdge>("conn_e", ne, &e2);
+    float *dh = c->buf<float>("conn_h", ne, &e2);
+    WV_CUDA(c, e2);
+    WV_CUDA(c, cudaMemcpyAsync(de, edges.data(), (size_t)ne * sizeof(ConnEdge), cudaMemcpyHostToDevice, c->stream));
+    k_conn_edges<<<(ne + 127) / 128, 128, 0, c->stream>>>(c->base.as<float>(), c->d, de, ne, c->fg_ids.as<uint32_t>(),
+                                                          c->fg_dist.as<float>(), c->fg_deg.as<uint32_t>(), w, dh);
+    WV_CUDA(c, cudaGetLastError());
+    hbuf.resize(ne);
+    WV_CUDA(c, cudaMemcpyAsync(hbuf.data(), dh, (size_t)ne * 4, cudaMemcpyDeviceToHost, c->stream));
+    WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (uint32_t i = 0; i < ne; i++) dist[(size_t)edges[i].root * w + edges[i].pos] = hbuf[i];
+    edges.clear();
+    return WV_OK;
+  };
+  int rc = relayout(w + 16);  // spare width for the edges this pass adds
+  if (rc) return rc;
+  const bool own = c->rnd.fn == nullptr;
+  // searches per batch at most (WV_CONN_BATCH=1 runs them one at a time)
+  uint32_t batch_max = 4096;
+  if (const char *be = getenv("WV_CONN_BATCH")) batch_max = (uint32_t)std::min(4096L, std::max(1L, atol(be)));
+  uint32_t vcap = L_refine + std::max<uint32_t>(1024, 16 * L_refine);
+  std::vector<uint32_t> sd, real(L_refine), vcnt_h;
+  std::vector<DI> vis_h, hv;
+  std::vector<char> changed(n, 0);
+  std::vector<uint32_t> changed_list;
+  uint32_t k0 = 0;
+  while (k0 < m) {
+    rc = flush();  // the rows as they stand
+    if (rc) return rc;
+    for (uint32_t v : changed_list) changed[v] = 0;
+    changed_list.clear();
+    const uint32_t B = own ? std::min(m - k0, batch_max) : 1;
+    sd.resize((size_t)B * L_refine);
+    if (own) {
+      RandSource spec = c->rnd;
+      for (uint32_t b = 0; b < B; b++)
+        draw_seeds_row(spec, L_refine, n, ids.data() + (size_t)ep * w, deg[ep], sd.data() + (size_t)b * L_refine);
+    } else {
+      draw_seeds_row(c->rnd, L_refine, n, ids.data() + (size_t)ep * w, deg[ep], sd.data());
+    }
+    cudaError_t e = cudaSuccess;
+    uint32_t *dseed = c->buf<uint32_t>("conn_seed", (size_t)B * L_refine, &e);
+    uint32_t *dtg = c->buf<uint32_t>("conn_tg", B, &e);
+    float *dq = c->buf<float>("conn_q", (size_t)B * c->d, &e);
+    uint32_t *dvc = c->buf<uint32_t>("conn_vc", B, &e);
+    uint32_t *dout = c->buf<uint32_t>("conn_out", B, &e);
+    WV_CUDA(c, e);
+    WV_CUDA(c, cudaMemcpyAsync(dseed, sd.data(), (size_t)B * L_refine * 4, cudaMemcpyHostToDevice, c->stream));
+    WV_CUDA(c, cudaMemcpyAsync(dtg, tgt.data() + k0, (size_t)B * 4, cudaMemcpyHostToDevice, c->stream));
+    {
+      const size_t total = (size_t)B * c->d;
+      const int nb = (int)std::min<size_t>((total + 255) / 256, (size_t)c->sms * 8);
+      k_conn_rows<<<nb, 256, 0, c->stream>>>(c->base.as<float>(), c->d, dtg, B, dq);
+      WV_CUDA(c, cudaGetLastError());
+    }
+    DI *vis = nullptr;
+    while (true) {  // get_neighbors(base[id]) from ep's row (component_conn.cpp:100-160)
+      vis = c->buf<DI>("conn_vis", (size_t)B * vcap, &e);
+      WV_CUDA(c, e);
+      rc = run_build_search(c, dq, B, dseed, L_refine, L_refine, c->fg_ids.as<uint32_t>(), c->fg_deg.as<uint32_t>(),
+                            w, vis, dvc, vcap, dout, 1);
+      if (rc) return rc;
+      int st0 = 0;
+      WV_CUDA(c, cudaMemcpyAsync(&st0, c->d_status(), 4, cudaMemcpyDeviceToHost, c->stream));
+      WV_CUDA(c, cudaStreamSynchronize(c->stream));
+      if (st0 == DEV_OVERFLOW) {  // a visit list outgrew vcap: redo the batch with room
+        WV_CUDA(c, cudaMemsetAsync(c->d_status(), 0, 4, c->stream));
+        vcap *= 2;
         continue;
       }
-      tmp = next;
-      flag[tmp] = 1;
-      st.push_back(tmp);
-      cnt++;
-    }
-    if (cnt >= n) break;
-    uint32_t id = n;
-    for (uint32_t i = 0; i < n; i++)
-      if (!flag[i]) {
-        id = i;
-        break;
-      }
-    if (id == n) break;
-    if (!widened) {  // spare width for the edges this pass adds
-      int rc = relayout(w + 16);
+      rc = check_device_status(c, "conn search");
       if (rc) return rc;
-      widened = true;
+      break;
     }
-    // get_neighbors(base[id]) from ep's row (component_conn.cpp:94-160)
-    std::vector<uint32_t> sd(L_refine);
-    draw_seeds_row(c->rnd, L_refine, n, ids.data() + (size_t)ep * w, deg[ep], sd.data());
-    WV_CUDA(c, cudaMemcpyAsync(dseed, sd.data(), L_refine * 4, cudaMemcpyHostToDevice, c->stream));
-    int rc = run_build_search(c, c->base.as<float>() + (size_t)id * c->d, 1, dseed, L_refine, L_refine,
-                              c->fg_ids.as<uint32_t>(), c->fg_deg.as<uint32_t>(), w, vis, one + 1,
-                              n + L_refine + 64, one, 1);
-    if (rc) return rc;
-    uint32_t nv = 0;
-    WV_CUDA(c, cudaMemcpyAsync(&nv, one + 1, 4, cudaMemcpyDeviceToHost, c->stream));
+    vcnt_h.resize(B);
+    vis_h.resize((size_t)B * vcap);
+    WV_CUDA(c, cudaMemcpyAsync(vcnt_h.data(), dvc, (size_t)B * 4, cudaMemcpyDeviceToHost, c->stream));
+    WV_CUDA(c, cudaMemcpyAsync(vis_h.data(), vis, (size_t)B * vcap * sizeof(DI), cudaMemcpyDeviceToHost, c->stream));
     WV_CUDA(c, cudaStreamSynchronize(c->stream));
-    rc = check_device_status(c, "conn search");
-    if (rc) return rc;
-    // fullset = the expansion visits (the seeds are not part of it)
-    hv.resize(nv > L_refine ? nv - L_refine : 0);
-    if (!hv.empty())
-      WV_CUDA(c, cudaMemcpy(hv.data(), vis + L_refine, hv.size() * sizeof(DI), cudaMemcpyDeviceToHost));
-    stl::sort(hv.data(), (int)hv.size(), DILess());
-    bool found = false;
-    for (auto &x : hv)
-      if (flag[x.i]) {
-        root = x.i;
-        found = true;
-        break;
-      }
-    if (!found) {
-      while (true) {
-        uint32_t rid = (uint32_t)c->rnd.next() % n;
-        if (flag[rid]) {
-          root = rid;
+    uint32_t acc = 0;
+    for (uint32_t b = 0; b < B; b++) {
+      const uint32_t k = k0 + b, u = tgt[k];
+      const uint32_t nv = std::min(vcnt_h[b], vcap);
+      const DI *v = vis_h.data() + (size_t)b * vcap;
+      bool stale = false;
+      for (uint32_t j = 0; j < nv && !stale; j++) stale = v[j].i < n && changed[v[j].i];
+      if (stale) break;
+      if (own) {
+        const RandSource keep = c->rnd;
+        draw_seeds_row(c->rnd, L_refine, n, ids.data() + (size_t)ep * w, deg[ep], real.data());
+        if (!std::equal(real.begin(), real.end(), sd.data() + (size_t)b * L_refine)) {
+          c->rnd = keep;
           break;
         }
       }
+      // the pool: the expansion visits (the seeds are not part of it), sorted
+      hv.assign(v + std::min(nv, L_refine), v + nv);
+      stl::sort(hv.data(), (int)hv.size(), DILess());
+      uint32_t root = NONE;
+      for (auto &x : hv)
+        if (x.i < n && ft[x.i] <= k) {
+          root = x.i;
+          break;
+        }
+      if (root == NONE) {
+        while (true) {
+          const uint32_t rid = (uint32_t)c->rnd.next() % n;
+          if (ft[rid] <= k) {
+            root = rid;
+            break;
+          }
+        }
+      }
+      if (deg[root] == w) {
+        rc = flush();
+        if (rc) return rc;
+        rc = relayout(w + 16);
+        if (rc) return rc;
+      }
+      const uint32_t pos = deg[root]++;
+      ids[(size_t)root * w + pos] = u;
+      edges.push_back(ConnEdge{root, u, pos});
+      if (!changed[root]) {
+        changed[root] = 1;
+        changed_list.push_back(root);
+      }
+      (*added)++;
+      acc++;
     }
-    k_pair_l2<<<1, 32, 0, c->stream>>>(c->base.as<float>(), c->d, root, id, dd);
-    float h = 0;
-    WV_CUDA(c, cudaMemcpyAsync(&h, dd, 4, cudaMemcpyDeviceToHost, c->stream));
-    WV_CUDA(c, cudaStreamSynchronize(c->stream));
-    if (deg[root] == w) {
-      rc = relayout(w + 16);
-      if (rc) return rc;
-    }
-    const uint32_t pos = deg[root]++;
-    ids[(size_t)root * w + pos] = id;
-    dist[(size_t)root * w + pos] = h;
-    WV_CUDA(c, cudaMemcpyAsync(c->fg_ids.as<uint32_t>() + (size_t)root * w + pos, &id, 4, cudaMemcpyHostToDevice,
-                               c->stream));
-    WV_CUDA(c, cudaMemcpyAsync(c->fg_dist.as<float>() + (size_t)root * w + pos, &h, 4, cudaMemcpyHostToDevice,
-                               c->stream));
-    WV_CUDA(c, cudaMemcpyAsync(c->fg_deg.as<uint32_t>() + root, &deg[root], 4, cudaMemcpyHostToDevice, c->stream));
-    WV_CUDA(c, cudaStreamSynchronize(c->stream));
-    (*added)++;
+    WV_CHECK(c, acc > 0, WV_ERR_STATE, "conn: the first search of a batch was not accepted");
+    k0 += acc;
   }
-  if (widened) {  // trim to the widest row
-    uint32_t nw = 1;
-    for (uint32_t v = 0; v < n; v++) nw = std::max(nw, deg[v]);
-    if (nw != w) {
-      int rc = relayout(nw);
-      if (rc) return rc;
-    }
-  }
+  rc = flush();
+  if (rc) return rc;
+  uint32_t nw = 1;  // trim to the widest row
+  for (uint32_t v = 0; v < n; v++) nw = std::max(nw, deg[v]);
+  if (nw != w) return relayout(nw);
   return WV_OK;
 }
 
