@@ -551,10 +551,30 @@ __device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t &rs, 
   __syncwarp();
   ii_slot_entry(a, w, vs, rs + 1, rs, lane);
   const uint32_t T = rs + 1;
-  for (uint32_t j = lane; j < T; j += 32) w.tmp[j] = w.row[j];
-  __syncwarp();
-  if (lane == 0) stl::sort(w.tmp, (int)T, Ent3Less());
-  __syncwarp();
+  // std::sort(temp_pool) (component_refine.cpp:503 / 901): with distinct keys
+  // the sorted array is unique, so each lane places its entries by rank;
+  // tied keys take the one-lane replica of std::sort
+  {
+    const Ent3 e0 = lane < T ? w.row[lane] : Ent3{0.f, 0u, 0u};
+    const Ent3 e1 = lane + 32 < T ? w.row[lane + 32] : Ent3{0.f, 0u, 0u};
+    uint32_t r0 = 0, r1 = 0;
+    bool tie = false;
+    for (uint32_t t = 0; t < T; t++) {
+      const float kt = w.row[t].d;
+      r0 += kt < e0.d;
+      r1 += kt < e1.d;
+      tie |= (lane < T && t != lane && kt == e0.d) || (lane + 32 < T && t != lane + 32 && kt == e1.d);
+    }
+    if (__any_sync(FULL, tie)) {
+      for (uint32_t j = lane; j < T; j += 32) w.tmp[j] = w.row[j];
+      __syncwarp();
+      if (lane == 0) stl::sort(w.tmp, (int)T, Ent3Less());
+    } else {
+      if (lane < T) w.tmp[r0] = e0;
+      if (lane + 32 < T) w.tmp[r1] = e1;
+    }
+    __syncwarp();
+  }
   uint32_t nres = 0;
   if (a.vamana) {
     // compat: farthest first, every candidate against temp_pool[i].d (the
@@ -593,6 +613,32 @@ __device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t &rs, 
       nres = __shfl_sync(FULL, nres, 0);
       __syncwarp();
     }
+  } else if (!a.ssg) {
+    // NSG (component_refine.cpp:505-526): bit r of o0 / o1 is set when sorted
+    // entry r < p occludes this lane's entry p = lane / lane + 32 (the same
+    // id, or nearer to p than p is to the node); the walk then takes entry 0
+    // and each later entry that no taken entry occludes, up to R
+    const Ent3 p0 = lane < T ? w.tmp[lane] : Ent3{0.f, 0u, 0u};
+    const Ent3 p1 = lane + 32 < T ? w.tmp[lane + 32] : Ent3{0.f, 0u, 0u};
+    unsigned long long o0 = 0, o1 = 0;
+    for (uint32_t r = 0; r + 1 < T; r++) {
+      const Ent3 q = w.tmp[r];
+      if (r < lane && lane < T && (q.i == p0.i || w.D[q.slot * S + p0.slot] < p0.d)) o0 |= 1ull << r;
+      if (r < lane + 32 && lane + 32 < T && (q.i == p1.i || w.D[q.slot * S + p1.slot] < p1.d)) o1 |= 1ull << r;
+    }
+    unsigned long long taken = 1ull;
+    nres = 1;
+    for (uint32_t st = 1; nres < R && st < T; st++) {
+      const unsigned long long o = st < 32 ? __shfl_sync(FULL, o0, st) : __shfl_sync(FULL, o1, st - 32);
+      if (!(o & taken)) {
+        taken |= 1ull << st;
+        nres++;
+      }
+    }
+    if (lane < T && ((taken >> lane) & 1ull)) w.res[__popcll(taken & ((1ull << lane) - 1ull))] = lane;
+    if (lane + 32 < T && ((taken >> (lane + 32)) & 1ull))
+      w.res[__popcll(taken & ((1ull << (lane + 32)) - 1ull))] = lane + 32;
+    __syncwarp();
   } else {
     if (lane == 0) w.res[0] = 0;
     nres = 1;
