@@ -402,6 +402,7 @@ struct IIArgs {
   int vamana;
   int clean;               // Vamana re-prune closest first, each candidate against its own distance
   int ssg;                 // SSG re-prune: angle test, sentinel after a short result
+  int ints;                // integer rows in [0, 255], d <= 256: any summation order is exact
   float threshold;
   const uint32_t *p_ids;   // pruned rows (width R)
   const float *p_dist;
@@ -479,8 +480,22 @@ __device__ __forceinline__ float ii_dist(const IIArgs &a, const IIWarp &w, uint3
   if (!w.V) return l2g(a.base, a.d, w.sid[x], w.sid[y]);
   const float4 *p = reinterpret_cast<const float4 *>(w.V + (size_t)x * vs);
   const float4 *q = reinterpret_cast<const float4 *>(w.V + (size_t)y * vs);
-  float acc = 0.f;
   const uint32_t d4 = a.d >> 2;
+  if (a.ints) {
+    // every partial sum is an integer below 2^24, so four chains give the
+    // exact-order value
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    uint32_t g = 0;
+    for (; g + 4 <= d4; g += 4) {
+      s0 = __fadd_rn(s0, group4(p[g], q[g]));
+      s1 = __fadd_rn(s1, group4(p[g + 1], q[g + 1]));
+      s2 = __fadd_rn(s2, group4(p[g + 2], q[g + 2]));
+      s3 = __fadd_rn(s3, group4(p[g + 3], q[g + 3]));
+    }
+    for (; g < d4; g++) s0 = __fadd_rn(s0, group4(p[g], q[g]));
+    return __fadd_rn(__fadd_rn(s0, s1), __fadd_rn(s2, s3));
+  }
+  float acc = 0.f;
 #pragma unroll 4
   for (uint32_t g = 0; g < d4; g++) acc = __fadd_rn(acc, group4(p[g], q[g]));
   return acc;
@@ -1251,6 +1266,7 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
   ia.vamana = vamana;
   ia.clean = p.clean ? 1 : 0;
   ia.ssg = ssg;
+  ia.ints = c->base_int && c->d <= 256;
   ia.threshold = threshold;
   ia.p_ids = p_ids;
   ia.p_dist = p_dist;
@@ -1311,21 +1327,18 @@ int link_gpu(wv_ctx *c, const LinkParams &p, LinkStats *st) {
 
 // The conn edges root -> id at row position pos, applied on the device: the
 // id, the distance compare(base[root], base[id]) (ComponentConnNSGDFS::
-// findroot, component_conn.cpp:94-97) and the row's degree; h[i] keeps the
-// distance for the host copy of the rows.
+// findroot, component_conn.cpp:94-97) and the row's degree.
 struct ConnEdge {
   uint32_t root, id, pos;
 };
 
 __global__ void k_conn_edges(const float *base, uint32_t d, const ConnEdge *e, uint32_t ne, uint32_t *gids,
-                             float *gdist, uint32_t *gdeg, uint32_t w, float *h) {
+                             float *gdist, uint32_t *gdeg, uint32_t w) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ne; i += gridDim.x * blockDim.x) {
     const ConnEdge x = e[i];
-    const float dv = l2g(base, d, x.root, x.id);
     gids[(size_t)x.root * w + x.pos] = x.id;
-    gdist[(size_t)x.root * w + x.pos] = dv;
+    gdist[(size_t)x.root * w + x.pos] = l2g(base, d, x.root, x.id);
     atomicMax(gdeg + x.root, x.pos + 1);
-    h[i] = dv;
   }
 }
 
@@ -1334,6 +1347,19 @@ __global__ void k_conn_rows(const float *base, uint32_t d, const uint32_t *ids, 
   const size_t total = (size_t)B * d;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x)
     out[t] = base[(size_t)ids[t / d] * d + t % d];
+}
+
+// the rows (width w0) re-laid out with width w1, entries past a row's
+// degree zero
+__global__ void k_conn_relayout(const uint32_t *ids, const float *dist, const uint32_t *deg, uint32_t n, uint32_t w0,
+                                uint32_t w1, uint32_t *ids1, float *dist1) {
+  const size_t total = (size_t)n * w1;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t v = (uint32_t)(t / w1), j = (uint32_t)(t % w1);
+    const bool in = j < w0 && j < deg[v];
+    ids1[t] = in ? ids[(size_t)v * w0 + j] : 0u;
+    dist1[t] = in ? dist[(size_t)v * w0 + j] : 0.f;
+  }
 }
 
 int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
@@ -1360,21 +1386,25 @@ int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
   // search is the one the serial walk runs and the first of a batch is
   // always accepted.  With a caller's rand() function (the stream cannot be
   // copied) each batch is one search.
-  const uint32_t n = c->n, ep = c->fg_ep;
-  uint32_t w = c->fg_w;
-  std::vector<uint32_t> deg(n), ids((size_t)n * w);
-  std::vector<float> dist((size_t)n * w);
+  //
+  // The rows stay on the device (edges appended there, widths changed by a
+  // copy kernel); the host keeps the rows as they were, for the walk, and
+  // ep's row with its new edges, for the seeds.
+  const uint32_t n = c->n, ep = c->fg_ep, w0 = c->fg_w;
+  uint32_t w = w0;
+  std::vector<uint32_t> deg(n), ids((size_t)n * w0);
   WV_CUDA(c, cudaMemcpyAsync(deg.data(), c->fg_deg.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
-  WV_CUDA(c, cudaMemcpyAsync(ids.data(), c->fg_ids.p, (size_t)n * w * 4, cudaMemcpyDeviceToHost, c->stream));
-  WV_CUDA(c, cudaMemcpyAsync(dist.data(), c->fg_dist.p, (size_t)n * w * 4, cudaMemcpyDeviceToHost, c->stream));
+  WV_CUDA(c, cudaMemcpyAsync(ids.data(), c->fg_ids.p, (size_t)n * w0 * 4, cudaMemcpyDeviceToHost, c->stream));
   WV_CUDA(c, cudaStreamSynchronize(c->stream));
   *added = 0;
   // the walk: flag times and the linked nodes
   constexpr uint32_t NONE = 0xffffffffu;
   std::vector<uint32_t> ft(n, NONE), tgt, st;
-  for (uint32_t v = 0; v < n; v++)
+  for (uint32_t v = 0; v < n; v++) {
+    WV_CHECK(c, deg[v] <= w0, WV_ERR_STATE, "row %u: degree %u > width %u", v, deg[v], w0);
     for (uint32_t j = 0; j < deg[v]; j++)
-      WV_CHECK(c, ids[(size_t)v * w + j] < n, WV_ERR_STATE, "row %u holds id %u >= n", v, ids[(size_t)v * w + j]);
+      WV_CHECK(c, ids[(size_t)v * w0 + j] < n, WV_ERR_STATE, "row %u holds id %u >= n", v, ids[(size_t)v * w0 + j]);
+  }
   auto walk = [&](uint32_t start, uint32_t t) {  // DFS (component_conn.cpp:31-57)
     st.assign(1, start);
     ft[start] = t;
@@ -1382,8 +1412,8 @@ int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
     while (!st.empty()) {
       uint32_t next = NONE;
       for (uint32_t j = 0; j < deg[tmp]; j++)
-        if (ft[ids[(size_t)tmp * w + j]] == NONE) {
-          next = ids[(size_t)tmp * w + j];
+        if (ft[ids[(size_t)tmp * w0 + j]] == NONE) {
+          next = ids[(size_t)tmp * w0 + j];
           break;
         }
       if (next == NONE) {
@@ -1406,45 +1436,36 @@ int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
   }
   const uint32_t m = (uint32_t)tgt.size();
   if (m == 0) return WV_OK;
-  // re-lays rows out with width nw (host arrays and device copy)
+  std::vector<uint32_t> ep_row(ids.begin() + (size_t)ep * w0, ids.begin() + (size_t)ep * w0 + deg[ep]);
+  // re-lays the device rows out with width nw
   auto relayout = [&](uint32_t nw) -> int {
-    std::vector<uint32_t> i2((size_t)n * nw, 0);
-    std::vector<float> d2((size_t)n * nw, 0.f);
-    for (uint32_t v = 0; v < n; v++)
-      for (uint32_t j = 0; j < deg[v]; j++) {
-        i2[(size_t)v * nw + j] = ids[(size_t)v * w + j];
-        d2[(size_t)v * nw + j] = dist[(size_t)v * w + j];
-      }
-    ids.swap(i2);
-    dist.swap(d2);
+    DevBuf &ti = c->work["conn_ri"], &td = c->work["conn_rd"];
+    WV_CUDA(c, ti.ensure((size_t)n * nw * 4));
+    WV_CUDA(c, td.ensure((size_t)n * nw * 4));
+    const size_t total = (size_t)n * nw;
+    const int nb = (int)std::min<size_t>((total + 255) / 256, (size_t)c->sms * 16);
+    k_conn_relayout<<<nb, 256, 0, c->stream>>>(c->fg_ids.as<uint32_t>(), c->fg_dist.as<float>(),
+                                                c->fg_deg.as<uint32_t>(), n, w, nw, ti.as<uint32_t>(),
+                                                td.as<float>());
+    WV_CUDA(c, cudaGetLastError());
+    std::swap(c->fg_ids, ti);
+    std::swap(c->fg_dist, td);
     w = nw;
-    WV_CUDA(c, c->fg_ids.ensure((size_t)n * w * 4));
-    WV_CUDA(c, c->fg_dist.ensure((size_t)n * w * 4));
-    WV_CUDA(c, cudaMemcpyAsync(c->fg_ids.p, ids.data(), (size_t)n * w * 4, cudaMemcpyHostToDevice, c->stream));
-    WV_CUDA(c, cudaMemcpyAsync(c->fg_dist.p, dist.data(), (size_t)n * w * 4, cudaMemcpyHostToDevice, c->stream));
-    WV_CUDA(c, cudaStreamSynchronize(c->stream));
     c->fg_w = w;
     return WV_OK;
   };
-  // accepted edges not yet in the device rows; their distances come back
-  // into the host rows
+  // accepted edges not yet in the device rows
   std::vector<ConnEdge> edges;
-  std::vector<float> hbuf;
   auto flush = [&]() -> int {
     if (edges.empty()) return WV_OK;
     const uint32_t ne = (uint32_t)edges.size();
     cudaError_t e2 = cudaSuccess;
     ConnEdge *de = c->buf<ConnEdge>("conn_e", ne, &e2);
-    float *dh = c->buf<float>("conn_h", ne, &e2);
     WV_CUDA(c, e2);
     WV_CUDA(c, cudaMemcpyAsync(de, edges.data(), (size_t)ne * sizeof(ConnEdge), cudaMemcpyHostToDevice, c->stream));
     k_conn_edges<<<(ne + 127) / 128, 128, 0, c->stream>>>(c->base.as<float>(), c->d, de, ne, c->fg_ids.as<uint32_t>(),
-                                                          c->fg_dist.as<float>(), c->fg_deg.as<uint32_t>(), w, dh);
+                                                          c->fg_dist.as<float>(), c->fg_deg.as<uint32_t>(), w);
     WV_CUDA(c, cudaGetLastError());
-    hbuf.resize(ne);
-    WV_CUDA(c, cudaMemcpyAsync(hbuf.data(), dh, (size_t)ne * 4, cudaMemcpyDeviceToHost, c->stream));
-    WV_CUDA(c, cudaStreamSynchronize(c->stream));
-    for (uint32_t i = 0; i < ne; i++) dist[(size_t)edges[i].root * w + edges[i].pos] = hbuf[i];
     edges.clear();
     return WV_OK;
   };
@@ -1470,9 +1491,9 @@ int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
     if (own) {
       RandSource spec = c->rnd;
       for (uint32_t b = 0; b < B; b++)
-        draw_seeds_row(spec, L_refine, n, ids.data() + (size_t)ep * w, deg[ep], sd.data() + (size_t)b * L_refine);
+        draw_seeds_row(spec, L_refine, n, ep_row.data(), (uint32_t)ep_row.size(), sd.data() + (size_t)b * L_refine);
     } else {
-      draw_seeds_row(c->rnd, L_refine, n, ids.data() + (size_t)ep * w, deg[ep], sd.data());
+      draw_seeds_row(c->rnd, L_refine, n, ep_row.data(), (uint32_t)ep_row.size(), sd.data());
     }
     cudaError_t e = cudaSuccess;
     uint32_t *dseed = c->buf<uint32_t>("conn_seed", (size_t)B * L_refine, &e);
@@ -1523,7 +1544,7 @@ int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
       if (stale) break;
       if (own) {
         const RandSource keep = c->rnd;
-        draw_seeds_row(c->rnd, L_refine, n, ids.data() + (size_t)ep * w, deg[ep], real.data());
+        draw_seeds_row(c->rnd, L_refine, n, ep_row.data(), (uint32_t)ep_row.size(), real.data());
         if (!std::equal(real.begin(), real.end(), sd.data() + (size_t)b * L_refine)) {
           c->rnd = keep;
           break;
@@ -1554,8 +1575,8 @@ int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
         if (rc) return rc;
       }
       const uint32_t pos = deg[root]++;
-      ids[(size_t)root * w + pos] = u;
       edges.push_back(ConnEdge{root, u, pos});
+      if (root == ep) ep_row.push_back(u);
       if (!changed[root]) {
         changed[root] = 1;
         changed_list.push_back(root);
@@ -1570,7 +1591,9 @@ int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
   if (rc) return rc;
   uint32_t nw = 1;  // trim to the widest row
   for (uint32_t v = 0; v < n; v++) nw = std::max(nw, deg[v]);
-  if (nw != w) return relayout(nw);
+  if (nw != w) rc = relayout(nw);
+  if (rc) return rc;
+  WV_CUDA(c, cudaStreamSynchronize(c->stream));
   return WV_OK;
 }
 
