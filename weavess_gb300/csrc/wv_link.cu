@@ -1532,10 +1532,23 @@ int conn_dfs_gpu(wv_ctx *c, uint32_t L_refine, uint32_t *added) {
     vcnt_h.resize(B);
     vis_h.resize((size_t)B * vcap);
     WV_CUDA(c, cudaMemcpyAsync(vcnt_h.data(), dvc, (size_t)B * 4, cudaMemcpyDeviceToHost, c->stream));
-    WV_CUDA(c, cudaMemcpyAsync(vis_h.data(), vis, (size_t)B * vcap * sizeof(DI), cudaMemcpyDeviceToHost, c->stream));
     WV_CUDA(c, cudaStreamSynchronize(c->stream));
+    // the visit lists come back in growing chunks, each list only as far as
+    // the chunk's longest: a batch is usually cut after a few searches
+    uint32_t have = 0, chunk = 16;
     uint32_t acc = 0;
     for (uint32_t b = 0; b < B; b++) {
+      if (b == have) {
+        const uint32_t hi = std::min(B, have + chunk);
+        uint32_t wmax = 1;
+        for (uint32_t q = have; q < hi; q++) wmax = std::max(wmax, std::min(vcnt_h[q], vcap));
+        WV_CUDA(c, cudaMemcpy2DAsync(vis_h.data() + (size_t)have * vcap, (size_t)vcap * sizeof(DI),
+                                     vis + (size_t)have * vcap, (size_t)vcap * sizeof(DI), (size_t)wmax * sizeof(DI),
+                                     hi - have, cudaMemcpyDeviceToHost, c->stream));
+        WV_CUDA(c, cudaStreamSynchronize(c->stream));
+        have = hi;
+        chunk *= 2;
+      }
       const uint32_t k = k0 + b, u = tgt[k];
       const uint32_t nv = std::min(vcnt_h[b], vcap);
       const DI *v = vis_h.data() + (size_t)b * vcap;
