@@ -527,9 +527,15 @@ __device__ void ii_slot_entry(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t 
 }
 
 // applies "insert `s` (distance dist, sender index i) into this row" exactly
-// as InterInsert does to des_pool (component_refine.cpp:484-540 / 884-949)
-__device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t &rs, bool &dvalid, uint32_t s, float dist,
-                         uint32_t i, int lane) {
+// as InterInsert does to des_pool (component_refine.cpp:484-540 / 884-949).
+// `kept` (NSG): the last re-prune took R entries with distinct keys, so the
+// row is sorted and no entry is occluded by a nearer one.  Re-pruning such a
+// row with s gives the same row when s ties no key and is either farther
+// than every entry (the walk is full before it reaches s) or occluded by a
+// nearer entry (s is skipped and every entry is taken again), so those
+// insertions stop early.
+__device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t &rs, bool &dvalid, bool &kept, uint32_t s,
+                         float dist, uint32_t i, int lane) {
   bool dup = false;
   for (uint32_t j = lane; j < rs; j += 32) dup |= w.row[j].i == s;
   if (__any_sync(FULL, dup)) return;
@@ -539,7 +545,20 @@ __device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t &rs, 
     __syncwarp();
     if (dvalid) ii_slot_entry(a, w, vs, rs + 1, rs, lane);
     rs++;
+    kept = false;
     return;
+  }
+  const bool nsg = !a.vamana && !a.ssg;
+  bool tie_s = false;
+  if (nsg && kept) {
+    bool far = true;
+    for (uint32_t j = lane; j < rs; j += 32) {
+      const float rd = w.row[j].d;
+      tie_s |= rd == dist;
+      far &= rd < dist;
+    }
+    tie_s = __any_sync(FULL, tie_s);
+    if (!tie_s && __all_sync(FULL, far)) return;
   }
   // a re-prune needs the pairwise distances of row + s
   if (!dvalid) {
@@ -565,7 +584,17 @@ __device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t &rs, 
   if (lane == 0) w.row[rs] = Ent3{dist, s, INVALID};
   __syncwarp();
   ii_slot_entry(a, w, vs, rs + 1, rs, lane);
+  if (nsg && kept && !tie_s) {
+    const uint32_t fs = w.row[rs].slot;
+    bool occ = false;
+    for (uint32_t j = lane; j < rs; j += 32) {
+      const Ent3 r = w.row[j];
+      occ |= r.d < dist && w.D[r.slot * S + fs] < dist;
+    }
+    if (__any_sync(FULL, occ)) return;
+  }
   const uint32_t T = rs + 1;
+  bool any_tie = false;
   // std::sort(temp_pool) (component_refine.cpp:503 / 901): with distinct keys
   // the sorted array is unique, so each lane places its entries by rank;
   // tied keys take the one-lane replica of std::sort
@@ -580,7 +609,8 @@ __device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t &rs, 
       r1 += kt < e1.d;
       tie |= (lane < T && t != lane && kt == e0.d) || (lane + 32 < T && t != lane + 32 && kt == e1.d);
     }
-    if (__any_sync(FULL, tie)) {
+    any_tie = __any_sync(FULL, tie);
+    if (any_tie) {
       for (uint32_t j = lane; j < T; j += 32) w.tmp[j] = w.row[j];
       __syncwarp();
       if (lane == 0) stl::sort(w.tmp, (int)T, Ent3Less());
@@ -679,6 +709,7 @@ __device__ void ii_apply(const IIArgs &a, IIWarp &w, uint32_t vs, uint32_t &rs, 
   // positions result.size()..R-1 stay in the row; SSG writes the sentinel.
   for (uint32_t j = lane; j < nres; j += 32) w.row[j] = w.tmp[w.res[j]];
   __syncwarp();
+  kept = nsg && nres == R && !any_tie;
   if (a.vamana || a.ssg) rs = nres;  // SSG writes a sentinel after a short result
   __syncwarp();
 }
@@ -698,7 +729,7 @@ __global__ void __launch_bounds__(II_WARPS * 32) k_ii_forward(IIArgs a, uint32_t
     const uint32_t n = a.nodes[t];
     uint32_t rs = a.p_deg[n];
     ii_load_row(w, a.p_ids + (size_t)n * a.R, a.p_dist + (size_t)n * a.R, rs, lane);
-    bool dvalid = false;
+    bool dvalid = false, kept = false;
     const uint32_t off = a.req_off[n], cnt = a.req_cnt[n];
     for (uint32_t r = 0; r < cnt; r++) {
       const uint32_t m = (uint32_t)(a.req[off + r] >> 32);
@@ -711,7 +742,7 @@ __global__ void __launch_bounds__(II_WARPS * 32) k_ii_forward(IIArgs a, uint32_t
         while (hits) {
           const uint32_t pos = b + __ffs(hits) - 1;
           hits &= hits - 1;
-          ii_apply(a, w, vs, rs, dvalid, m, a.s_dist[(size_t)m * a.R + pos], pos, lane);
+          ii_apply(a, w, vs, rs, dvalid, kept, m, a.s_dist[(size_t)m * a.R + pos], pos, lane);
         }
       }
     }
@@ -732,12 +763,12 @@ __global__ void __launch_bounds__(II_WARPS * 32) k_ii_backward(IIArgs a, uint32_
   for (uint32_t r = blockIdx.x * II_WARPS + warp; r < a.n; r += gridDim.x * II_WARPS) {
     uint32_t rs = a.s_deg[r];
     ii_load_row(w, a.s_ids + (size_t)r * a.R, a.s_dist + (size_t)r * a.R, rs, lane);
-    bool dvalid = false;
+    bool dvalid = false, kept = false;
     const uint32_t off = a.req_off[r], cnt = a.req_cnt[r];
     for (uint32_t q = 0; q < cnt; q++) {
       const unsigned long long key = a.req[off + q];
       const uint32_t m = (uint32_t)(key >> 32), pos = (uint32_t)key;
-      ii_apply(a, w, vs, rs, dvalid, m, a.s_dist[(size_t)m * a.R + pos], pos, lane);
+      ii_apply(a, w, vs, rs, dvalid, kept, m, a.s_dist[(size_t)m * a.R + pos], pos, lane);
     }
     for (uint32_t j = lane; j < rs; j += 32) {
       a.f_ids[(size_t)r * a.R + j] = w.row[j].i;
